@@ -1,0 +1,160 @@
+/*
+ * libpffrg_gpu: GB300 (sm_103a) flow right-hand side of the pseudo-fermion
+ * functional renormalisation group, as a C ABI for the host code of
+ * PFFRGSolver.jl (Julia ccall) or any other host language.
+ *
+ * Data ownership follows the reference: the caller owns every host array
+ * (Julia Vector/Array{Float64}, column-major, site index fastest) and the
+ * output arrays are overwritten in place.  Index tables are passed 1-based
+ * exactly as the reference stores them.  A context owns all device memory
+ * (device-resident actions and scratch) and one CUDA stream; calls on one
+ * context are synchronous on return and must come from one host thread at a
+ * time; separate contexts are independent.
+ *
+ * Errors: every int-returning entry point returns 0 on success and a
+ * PFFRG_E_* code otherwise; pffrg_last_error() gives the message.  (The
+ * reference raises Julia AssertionErrors; a Julia shim turns a nonzero code
+ * into error(pffrg_last_error(ctx)).)  There is no CPU fallback: without a
+ * usable CUDA device pffrg_create() returns NULL and
+ * pffrg_last_error(NULL) says why.
+ */
+#ifndef PFFRG_GPU_H
+#define PFFRG_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PFFRG_OK 0
+#define PFFRG_E_ARGS 1     /* bad dimensions / arguments (reference: @assert) */
+#define PFFRG_E_CUDA 2     /* CUDA runtime error */
+#define PFFRG_E_LIMIT 3    /* a fixed capacity was exceeded (mesh length, sites, GK segments) */
+#define PFFRG_E_NONFINITE 4
+
+#define PFFRG_FP64 0       /* FP64 integrand (the comparator path) */
+#define PFFRG_MIXED 1      /* FP32 integrand + compensated sums, FP64 quadrature bookkeeping */
+
+#define PFFRG_SU2 0
+#define PFFRG_U1_DM 1
+
+typedef struct pffrg_ctx pffrg_ctx;
+
+/* Reduced_lattice tables (src/Lattice/reduced.jl:13-24). overlap_rows holds
+ * the rows of r.overlap[i] (a, b, multiplicity) for i = 1..Ns back to back,
+ * overlap_offsets[i] the first row of site i (offsets[Ns] = total rows). */
+typedef struct pffrg_lattice_view {
+    int64_t num_sites;
+    const int64_t* exchange;        /* [Ns], 1-based */
+    const int64_t* mult;            /* [Ns] */
+    const int64_t* overlap_offsets; /* [Ns+1] */
+    const int64_t* overlap_rows;    /* [3*R], 1-based site indices */
+} pffrg_lattice_view;
+
+/* Mesh (src/Frequency/mesh.jl:16-27); num_* are the array lengths. */
+typedef struct pffrg_mesh_view {
+    int64_t num_sigma, num_omega, num_nu;
+    const double* sigma;
+    const double* omega_s;
+    const double* nu_s;
+    const double* omega_t;
+    const double* nu_t;
+} pffrg_mesh_view;
+
+/* Action_su2 / Action_u1_dm (src/Action/action_lib/action_su2.jl:8-12):
+ * a.Σ, a.Γ[c].bare and a.Γ[c].ch_{s,t,u}.{q1,q2_1,q2_2,q3}; channel index
+ * 0 = s, 1 = t, 2 = u; components 0..1 (su2) or 0..5 (u1-dm).  The pointers
+ * may alias one packed buffer (then a single copy moves the whole action). */
+typedef struct pffrg_action_view {
+    double* sigma;
+    double* bare[6];
+    double* q1[6][3];
+    double* q2_1[6][3];
+    double* q2_2[6][3];
+    double* q3[6][3];
+} pffrg_action_view;
+
+/* Create a context for one lattice / mesh size / symmetry.  Replaces the
+ * set-up of compute buffers in launch_1l!/2l!/ml! (src/Launcher/launcher_1l.jl:37-54).
+ * device: CUDA device ordinal.  precision: PFFRG_FP64 or PFFRG_MIXED. */
+pffrg_ctx* pffrg_create(const pffrg_lattice_view* lattice, const pffrg_mesh_view* mesh, int symmetry, double S,
+                        int precision, int device);
+void pffrg_destroy(pffrg_ctx* ctx);
+const char* pffrg_last_error(const pffrg_ctx* ctx);
+
+/* New frequency meshes after every accepted ODE step (resample_from_to,
+ * src/Action/Action.jl:451-527; launcher_1l.jl:177); sizes must not change. */
+int pffrg_set_mesh(pffrg_ctx* ctx, const pffrg_mesh_view* mesh);
+int pffrg_set_precision(pffrg_ctx* ctx, int precision);
+
+/* compute_dΣ!(Λ, r, m, a, da, Σ_tol) (src/Flow/flow_self.jl:2-20): writes da.Σ[2:end]. */
+int pffrg_dsigma(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, pffrg_action_view* da, double atol,
+                 double rtol);
+
+/* compute_dΓ_1l!/2l!/ml! (src/Flow/compute.jl:57-287) for loops = 1, 2, >= 3.
+ * da.Σ must already hold compute_dΣ!'s result (the Katanin propagator reads it).
+ * Writes every vertex entry of da (bare untouched).  For loops >= 3 and
+ * sigma_corr != 0 also applies compute_dΣ_corr! (flow_self.jl:23-51) to
+ * da.Σ, as launcher_ml.jl:95 does.  The scratch actions da_l, da_c, da_temp,
+ * da_Σ of the reference live on the device inside the context. */
+int pffrg_dgamma(pffrg_ctx* ctx, int loops, double Lam, const pffrg_action_view* a, pffrg_action_view* da,
+                 int eval, double gamma_atol, double gamma_rtol, int sigma_corr, double sigma_atol,
+                 double sigma_rtol);
+
+/* Parquet iteration kernels (src/Launcher/parquet.jl:43-80):
+ * compute_Σ!(Λ, r, m, a1, a2, ...) (src/Flow/SDE.jl:58-96) writes a2's
+ * s-channel q1/q2_2 and a2.Σ[2:end]; compute_Γ!(Λ, r, m, a1, a2, ...)
+ * (src/Flow/compute.jl:2-54) writes a2's vertex, reusing the boundary
+ * corrections of the last pffrg_sde call on this context, as the reference
+ * reuses its corrs buffer. */
+int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval,
+              double gamma_atol, double gamma_rtol, double sigma_atol, double sigma_rtol);
+int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval,
+              double atol, double rtol);
+
+/* ---- device-resident interface (no host copies inside the step) ---- */
+
+/* Number of doubles of one packed action (Σ, then per component bare and
+ * ch_s, ch_t, ch_u each as q1, q2_1, q2_2, q3, all column-major). */
+int64_t pffrg_action_size(const pffrg_ctx* ctx);
+
+/* Device-resident action slots owned by the context. */
+#define PFFRG_SLOT_A 0       /* state a */
+#define PFFRG_SLOT_DA 1      /* derivative / stage result */
+#define PFFRG_SLOT_INTER 2   /* a_inter of the ODE step */
+#define PFFRG_SLOT_ERR 3     /* a_err of the ODE step */
+#define PFFRG_SLOT_NEXT 4    /* da of the ODE step (the 3rd-order solution) */
+#define PFFRG_NUM_SLOTS 5
+int pffrg_upload(pffrg_ctx* ctx, int slot, const pffrg_action_view* a);
+int pffrg_download(pffrg_ctx* ctx, int slot, pffrg_action_view* a);
+
+/* One full RHS on device slots: compute_dΣ! then compute_dΓ_*! (and
+ * compute_dΣ_corr! for loops >= 3 when sigma_corr != 0). */
+int pffrg_rhs(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, int eval, double gamma_atol,
+              double gamma_rtol, double sigma_atol, double sigma_rtol, int sigma_corr);
+
+/* One Bogacki-Shampine step of launch_1l!/2l!/ml! (src/Launcher/launcher_1l.jl:80-116)
+ * on the device from slot A at cutoff Lam with step dLam: leaves the
+ * 3rd-order solution in PFFRG_SLOT_NEXT (the reference's a_inter after k4)
+ * and returns the error ratio err = max|a_err| / (atol + max(|a_next|,|a|) rtol)
+ * and max|q3| of the new solution. */
+int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, double gamma_atol,
+                  double gamma_rtol, double sigma_atol, double sigma_rtol, int sigma_corr, double ode_atol,
+                  double ode_rtol, double* err, double* abs_max_next);
+/* accept the step: slot A <- slot NEXT (the reference keeps a_inter for the resampling) */
+int pffrg_accept(pffrg_ctx* ctx);
+
+/* Integrand evaluations of the last pffrg_rhs / pffrg_dgamma (dΓ passes only),
+ * for throughput and algorithmic-byte accounting. */
+int64_t pffrg_last_integrand_evals(const pffrg_ctx* ctx);
+
+/* Pinned host memory for fast copies (cudaHostAlloc); NULL on failure. */
+void* pffrg_host_alloc(int64_t bytes);
+void pffrg_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

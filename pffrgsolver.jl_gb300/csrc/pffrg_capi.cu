@@ -1,0 +1,856 @@
+// C ABI of libpffrg_gpu.so: context, device-resident actions and the
+// sequencing of the flow right-hand side (src/Flow/compute.jl,
+// src/Flow/flow_self.jl, src/Flow/SDE.jl, src/Launcher/launcher_{1l,2l,ml}.jl).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pffrg_gpu.h"
+#include "pffrg_internal.h"
+
+using namespace pffrg;
+
+namespace {
+thread_local std::string g_create_error;
+constexpr int kPartials = 512;
+}  // namespace
+
+struct pffrg_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    Layout L{};
+    int symmetry = 0;
+    double S = 0.5;
+    int precision = PFFRG_FP64;
+    DevLattice lat;
+    double* mesh = nullptr;  // [σ|Ωs|νs|Ωt|νt]
+    double* slot[PFFRG_NUM_SLOTS] = {};
+    double* da_l = nullptr;
+    double* da_c = nullptr;
+    double* da_temp = nullptr;
+    double* da_sig = nullptr;
+    double* sig_tmp = nullptr;  // [Nsig]
+    float* f_a = nullptr;       // FP32 copies for the mixed path
+    float* f_da = nullptr;
+    float* f_dal = nullptr;
+    float* f_dtemp = nullptr;
+    std::vector<double> h_mesh;    // host copy of [σ|Ωs|νs|Ωt|νt]
+    double* log_bounds = nullptr;  // [2][NO][eval+1]
+    int bounds_cap = 0;            // eval the buffer holds
+    std::vector<double> h_bounds;
+    double* corrs = nullptr;       // [2,3,NO]
+    double* corrs_sde = nullptr;   // corrs left by the last SDE call
+    double* partial = nullptr;     // [kPartials]
+    double* scalars = nullptr;     // [4]
+    double* h_scalars = nullptr;   // pinned [4]
+    int* status = nullptr;
+    unsigned long long* counter = nullptr;
+    int4* tasks_sym = nullptr;
+    int4* tasks_full = nullptr;
+    int4* tasks_red = nullptr;
+    int n_sym = 0, n_full = 0, n_red = 0;
+    int64_t last_evals = 0;
+    std::string err;
+
+    int fail(int code, const char* fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+};
+
+#define CK(call)                                                                                          \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return ctx->fail(PFFRG_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                             __LINE__);                                                                   \
+    } while (0)
+
+namespace {
+
+std::vector<int4> make_tasks(int NO, int Nn, int mode) {
+    // mode 0: w2 >= w3 (compute.jl:73-107), 1: all w2 (compute.jl:135-170), 2: reduced s bubble (SDE.jl:76-86)
+    std::vector<int4> T;
+    for (int w1 = 0; w1 < NO; ++w1) {
+        T.push_back(make_int4(1, w1, -1, -1));
+        for (int w3 = 0; w3 < Nn; ++w3) {
+            if (mode != 2) T.push_back(make_int4(2, w1, w3, -1));
+            T.push_back(make_int4(3, w1, -1, w3));
+            if (mode == 2) continue;
+            for (int w2 = (mode == 0 ? w3 : 0); w2 < Nn; ++w2) T.push_back(make_int4(4, w1, w2, w3));
+        }
+    }
+    return T;
+}
+
+int check_mesh(pffrg_ctx* ctx, const pffrg_mesh_view* m) {
+    if (!m || !m->sigma || !m->omega_s || !m->nu_s || !m->omega_t || !m->nu_t)
+        return ctx->fail(PFFRG_E_ARGS, "mesh view has null arrays");
+    if (m->num_sigma < 2 || m->num_omega < 2 || m->num_nu < 2)
+        return ctx->fail(PFFRG_E_ARGS, "meshes need at least two frequencies");
+    if (m->num_sigma > kMaxMesh || m->num_omega > kMaxMesh || m->num_nu > kMaxMesh)
+        return ctx->fail(PFFRG_E_LIMIT, "mesh longer than %d frequencies", kMaxMesh);
+    return 0;
+}
+
+int upload_mesh(pffrg_ctx* ctx, const pffrg_mesh_view* m) {
+    if (int rc = check_mesh(ctx, m)) return rc;
+    if (m->num_sigma != ctx->L.Nsig || m->num_omega != ctx->L.NO || m->num_nu != ctx->L.Nn)
+        return ctx->fail(PFFRG_E_ARGS, "mesh sizes differ from the context's");
+    std::vector<double> h;
+    h.insert(h.end(), m->sigma, m->sigma + m->num_sigma);
+    h.insert(h.end(), m->omega_s, m->omega_s + m->num_omega);
+    h.insert(h.end(), m->nu_s, m->nu_s + m->num_nu);
+    h.insert(h.end(), m->omega_t, m->omega_t + m->num_omega);
+    h.insert(h.end(), m->nu_t, m->nu_t + m->num_nu);
+    CK(cudaMemcpyAsync(ctx->mesh, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->h_mesh = h;
+    return 0;
+}
+
+// Subdomain end points ξ^k a of integrate_log! (quadrature.jl:113-139) for every task
+// frequency w1 of both bosonic meshes at cutoff Λ, with libm's pow as in the reference.
+int upload_log_bounds(pffrg_ctx* ctx, double Lam, int eval) {
+    const Layout& L = ctx->L;
+    if (eval > ctx->bounds_cap) {
+        if (ctx->log_bounds) CK(cudaFree(ctx->log_bounds));
+        ctx->log_bounds = nullptr;
+        CK(cudaMalloc(&ctx->log_bounds, sizeof(double) * 2 * L.NO * (eval + 1)));
+        ctx->bounds_cap = eval;
+    }
+    const double* Os = ctx->h_mesh.data() + L.Nsig;
+    const double* ns = Os + L.NO;
+    const double* Ot = ns + L.Nn;
+    const double* nt = Ot + L.NO;
+    std::vector<double>& hb = ctx->h_bounds;
+    hb.assign((size_t)2 * L.NO * (eval + 1), 0.0);
+    for (int m = 0; m < 2; ++m) {
+        const double* Om = m ? Ot : Os;
+        const double* nu = m ? nt : ns;
+        const double val = Om[L.NO - 1] + nu[L.Nn - 1];
+        for (int w1 = 0; w1 < L.NO; ++w1) {
+            const double ref = Lam + 0.5 * Om[w1];
+            const double a = 2.0 * ref, b = 1.0 * val;
+            if (!(b > a)) continue;
+            const double xi = std::pow(b / a, 1.0 / eval);
+            double* o = hb.data() + (size_t)(m * L.NO + w1) * (eval + 1);
+            for (int k = 0; k <= eval; ++k) o[k] = std::pow(xi, (double)k) * a;
+        }
+    }
+    CK(cudaMemcpyAsync(ctx->log_bounds, hb.data(), sizeof(double) * hb.size(), cudaMemcpyHostToDevice, ctx->st));
+    return 0;
+}
+
+// host view <-> device packed action (one copy per array, or one copy when packed)
+int copy_view(pffrg_ctx* ctx, double* dev, const pffrg_action_view* v, bool to_device) {
+    const Layout& L = ctx->L;
+    if (!v || !v->sigma) return ctx->fail(PFFRG_E_ARGS, "action view has null arrays");
+    auto kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    // packed fast path: every array at its packed offset from sigma
+    bool packed = true;
+    for (int c = 0; c < L.C && packed; ++c) {
+        if (v->bare[c] != v->sigma + L.bare(c)) packed = false;
+        for (int ch = 0; ch < 3 && packed; ++ch) {
+            if (v->q1[c][ch] != v->sigma + L.qbase(c, ch, 0) || v->q2_1[c][ch] != v->sigma + L.qbase(c, ch, 1) ||
+                v->q2_2[c][ch] != v->sigma + L.qbase(c, ch, 2) || v->q3[c][ch] != v->sigma + L.qbase(c, ch, 3))
+                packed = false;
+        }
+    }
+    if (packed) {
+        if (to_device) CK(cudaMemcpyAsync(dev, v->sigma, sizeof(double) * L.total, kind, ctx->st));
+        else CK(cudaMemcpyAsync(v->sigma, dev, sizeof(double) * L.total, kind, ctx->st));
+        return 0;
+    }
+    auto cp = [&](double* host, int64_t off, int64_t n) -> int {
+        if (!host) return ctx->fail(PFFRG_E_ARGS, "action view has a null array");
+        if (to_device) CK(cudaMemcpyAsync(dev + off, host, sizeof(double) * n, kind, ctx->st));
+        else CK(cudaMemcpyAsync(host, dev + off, sizeof(double) * n, kind, ctx->st));
+        return 0;
+    };
+    if (int rc = cp(v->sigma, 0, L.Nsig)) return rc;
+    for (int c = 0; c < L.C; ++c) {
+        if (int rc = cp(v->bare[c], L.bare(c), L.Ns)) return rc;
+        for (int ch = 0; ch < 3; ++ch) {
+            if (int rc = cp(v->q1[c][ch], L.qbase(c, ch, 0), L.K1)) return rc;
+            if (int rc = cp(v->q2_1[c][ch], L.qbase(c, ch, 1), L.K2)) return rc;
+            if (int rc = cp(v->q2_2[c][ch], L.qbase(c, ch, 2), L.K2)) return rc;
+            if (int rc = cp(v->q3[c][ch], L.qbase(c, ch, 3), L.K3)) return rc;
+        }
+    }
+    return 0;
+}
+
+template <typename R>
+PassArgs<R> base_pass(pffrg_ctx* ctx, double Lam, int eval, double atol, double rtol) {
+    PassArgs<R> p;
+    std::memset(&p, 0, sizeof(p));
+    p.L = ctx->L;
+    p.exch = ctx->lat.exch;
+    p.ov_off = ctx->lat.ov_off;
+    p.ov_ab = ctx->lat.ov_ab;
+    if constexpr (sizeof(R) == 8) p.ov_m = (const R*)ctx->lat.ov_m;
+    else p.ov_m = (const R*)ctx->lat.ov_mf;
+    p.mesh = ctx->mesh;
+    p.log_bounds = ctx->log_bounds;
+    p.corrs = ctx->corrs;
+    p.Lam = Lam;
+    p.eval = eval;
+    p.atol = atol;
+    p.rtol = rtol;
+    p.twoS = 2.0 * ctx->S;
+    p.nchan = 3;
+    p.chan_of_y[0] = 1;  // t-channel CTAs (the heaviest) first
+    p.chan_of_y[1] = 0;
+    p.chan_of_y[2] = 2;
+    p.node_counter = ctx->counter;
+    return p;
+}
+
+template <typename R>
+void set_tasks(PassArgs<R>& p, pffrg_ctx* ctx, bool full) {
+    p.tasks = full ? ctx->tasks_full : ctx->tasks_sym;
+    p.ntasks = full ? ctx->n_full : ctx->n_sym;
+}
+
+// slot sources and, per channel X = s, t, u, the channels each slot reads
+template <typename R>
+void set_slots(PassArgs<R>& p, const R* s0, const R* s1, const R* s2, const R* s3, const int (&m)[3][4]) {
+    p.src[0] = s0;
+    p.src[1] = s1;
+    p.src[2] = s2;
+    p.src[3] = s3;
+    for (int X = 0; X < 3; ++X)
+        for (int k = 0; k < 4; ++k) p.mask[X][k] = m[X][k];
+}
+
+// Katanin kernels (flow_su2_{s,t,u}.jl:2-55): every slot reads all channels
+constexpr int kMaskKat[3][4] = {{CH_ALL, CH_ALL, CH_ALL, CH_ALL}, {CH_ALL, CH_ALL, CH_ALL, CH_ALL},
+                                {CH_ALL, CH_ALL, CH_ALL, CH_ALL}};
+// left kernels (flow_su2_s.jl:57-109, flow_su2_t.jl:89-173, flow_su2_u.jl:57-109) and the parquet BSE
+// kernels (BSE_su2_{s,t,u}.jl): slot 1 without the own channel, t-channel slot 3 without u
+constexpr int kMaskLeft[3][4] = {{CH_T | CH_U, CH_ALL, CH_ALL, CH_ALL},
+                                 {CH_S | CH_U, CH_ALL, CH_S | CH_T, CH_ALL},
+                                 {CH_S | CH_T, CH_ALL, CH_ALL, CH_ALL}};
+// central kernels (flow_su2_s.jl:112-159, flow_su2_t.jl:176-255, flow_su2_u.jl:112-159): slot 2 only
+// the own channel of da_l, t-channel slot 4 only its u channel
+constexpr int kMaskCentral[3][4] = {{CH_ALL, CH_S, CH_ALL, CH_ALL},
+                                    {CH_ALL, CH_T, CH_ALL, CH_U},
+                                    {CH_ALL, CH_U, CH_ALL, CH_ALL}};
+// reduced s bubble (SDE_su2.jl:2-42): slot 1 is the bare vertex
+constexpr int kMaskReduced[3][4] = {{0, CH_ALL, CH_ALL, CH_ALL}, {0, CH_ALL, CH_ALL, CH_ALL},
+                                    {0, CH_ALL, CH_ALL, CH_ALL}};
+
+// typed views of the vertex sources: FP64 uses the action itself, FP32 its converted copy
+template <typename R>
+struct Src {
+    const R* a;
+    const R* da;
+    const R* dal;
+    const R* dtemp;
+};
+
+template <typename R>
+int corrs_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* da, double atol, double rtol,
+              double* out) {
+    CorrsArgs<R> c;
+    c.NO = ctx->L.NO;
+    c.Nn = ctx->L.Nn;
+    c.Nsig = ctx->L.Nsig;
+    c.kind = kind;
+    c.a = a;
+    c.da = da;
+    c.mesh = ctx->mesh;
+    c.Lam = Lam;
+    c.atol = atol;
+    c.rtol = rtol;
+    c.corrs = out;
+    c.status = ctx->status;
+    CK(launch_corrs<R>(c, ctx->st));
+    return 0;
+}
+
+template <typename R>
+int sigma_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* aux, double* out, double atol,
+              double rtol) {
+    SigmaArgs<R> s;
+    s.L = ctx->L;
+    s.kind = kind;
+    s.a = a;
+    s.aux = aux;
+    s.out = out;
+    s.exch = ctx->lat.exch;
+    s.mult = ctx->lat.mult;
+    s.mesh = ctx->mesh;
+    s.Lam = Lam;
+    s.atol = atol;
+    s.rtol = rtol;
+    s.twoS = 2.0 * ctx->S;
+    s.status = ctx->status;
+    CK(launch_sigma<R>(s, ctx->st));
+    return 0;
+}
+
+int to_f(pffrg_ctx* ctx, const double* x, float* y) {
+    CK(launch_to_float(x, y, ctx->L.total, ctx->st));
+    return 0;
+}
+
+int check_status(pffrg_ctx* ctx) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (h) {
+        CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
+        return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity exceeded (status %d)", h);
+    }
+    return 0;
+}
+
+// compute_dΣ! on device actions
+template <typename R>
+int dsigma_dev(pffrg_ctx* ctx, double Lam, const double* a, double* da, double atol, double rtol) {
+    const R* ra;
+    if constexpr (sizeof(R) == 8) {
+        ra = (const R*)a;
+    } else {
+        if (int rc = to_f(ctx, a, ctx->f_a)) return rc;
+        ra = (const R*)ctx->f_a;
+    }
+    return sigma_run<R>(ctx, SIG_FLOW, Lam, ra, nullptr, da, atol, rtol);
+}
+
+// compute_dΓ_{1l,2l,ml}! (+ compute_dΣ_corr!) on device actions
+template <typename R>
+int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* da, int eval, double gatol,
+               double grtol, int sigma_corr, double satol, double srtol) {
+    const Layout& L = ctx->L;
+    Src<R> s;
+    if constexpr (sizeof(R) == 8) {
+        s.a = (const R*)a;
+        s.da = (const R*)da;
+        s.dal = (const R*)ctx->da_l;
+        s.dtemp = (const R*)ctx->da_temp;
+    } else {
+        if (int rc = to_f(ctx, a, ctx->f_a)) return rc;
+        if (int rc = to_f(ctx, da, ctx->f_da)) return rc;  // dΣ for the Katanin propagator
+        s.a = (const R*)ctx->f_a;
+        s.da = (const R*)ctx->f_da;
+        s.dal = (const R*)ctx->f_dal;
+        s.dtemp = (const R*)ctx->f_dtemp;
+    }
+    CK(cudaMemsetAsync(ctx->counter, 0, sizeof(unsigned long long), ctx->st));
+    if (int rc = upload_log_bounds(ctx, Lam, eval)) return rc;
+    // 1 loop (compute.jl:57-112)
+    if (int rc = corrs_run<R>(ctx, PROP_KAT, Lam, s.a, s.da, gatol, grtol, ctx->corrs)) return rc;
+    {
+        PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
+        set_tasks(p, ctx, false);
+        set_slots<R>(p, s.a, s.a, s.a, s.a, kMaskKat);
+        p.prop_kind = PROP_KAT;
+        p.prop_a = s.a;
+        p.prop_da = s.da;
+        p.out = da;
+        CK(launch_pass<R>(p, ctx->st));
+        CK(launch_symmetrize(L, ctx->lat.exch, da, ctx->st));
+    }
+    if (loops >= 2) {
+        // 2 loop (compute.jl:115-174)
+        if constexpr (sizeof(R) == 4) {
+            if (int rc = to_f(ctx, da, ctx->f_da)) return rc;
+        }
+        if (int rc = corrs_run<R>(ctx, PROP_PLAIN, Lam, s.a, s.a, gatol, grtol, ctx->corrs)) return rc;
+        PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
+        set_tasks(p, ctx, true);
+        set_slots<R>(p, s.da, s.a, s.da, s.a, kMaskLeft);
+        p.prop_kind = PROP_PLAIN;
+        p.prop_a = s.a;
+        p.prop_da = s.a;
+        p.out = ctx->da_l;
+        CK(launch_pass<R>(p, ctx->st));
+        CK(launch_symmetrize_add_to(L, ctx->lat.exch, ctx->da_l, da, ctx->st));
+    }
+    if (loops >= 3) {
+        // multiloop (compute.jl:177-287)
+        CK(launch_axpby(L, 0.0, nullptr, 0.0, ctx->da_temp, false, true, ctx->st));
+        CK(launch_axpby(L, 0.0, nullptr, 0.0, ctx->da_sig, false, true, ctx->st));
+        CK(launch_symmetrize_add_to(L, ctx->lat.exch, ctx->da_l, ctx->da_temp, ctx->st));
+        for (int loop = 3; loop <= loops; ++loop) {
+            if constexpr (sizeof(R) == 4) {
+                if (int rc = to_f(ctx, ctx->da_l, ctx->f_dal)) return rc;
+                if (int rc = to_f(ctx, ctx->da_temp, ctx->f_dtemp)) return rc;
+            }
+            {
+                // central kernels (flow_su2_s.jl:112-159, t :176-255, u :112-159)
+                PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
+                set_tasks(p, ctx, false);
+                p.prop_kind = PROP_PLAIN;
+                p.prop_a = s.a;
+                p.prop_da = s.a;
+                p.out = ctx->da_c;
+                set_slots<R>(p, s.a, s.dal, s.a, s.dal, kMaskCentral);
+                CK(launch_pass<R>(p, ctx->st));
+            }
+            {
+                PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
+                set_tasks(p, ctx, true);
+                p.prop_kind = PROP_PLAIN;
+                p.prop_a = s.a;
+                p.prop_da = s.a;
+                p.out = ctx->da_l;
+                set_slots<R>(p, s.dtemp, s.a, s.dtemp, s.a, kMaskLeft);
+                CK(launch_pass<R>(p, ctx->st));
+            }
+            CK(launch_symmetrize(L, ctx->lat.exch, ctx->da_c, ctx->st));
+            CK(cudaMemcpyAsync(ctx->da_temp, ctx->da_c, sizeof(double) * L.total, cudaMemcpyDeviceToDevice, ctx->st));
+            CK(launch_symmetrize_add_to(L, ctx->lat.exch, ctx->da_l, ctx->da_temp, ctx->st));
+            CK(launch_axpby(L, 1.0, ctx->da_c, 1.0, ctx->da_sig, false, true, ctx->st));
+            CK(launch_axpby(L, 1.0, ctx->da_temp, 1.0, da, false, true, ctx->st));
+        }
+        if (sigma_corr) {
+            // compute_dΣ_corr! (flow_self.jl:23-51)
+            const R* sig_src;
+            if constexpr (sizeof(R) == 8) {
+                sig_src = (const R*)ctx->da_sig;
+            } else {
+                if (int rc = to_f(ctx, ctx->da_sig, ctx->f_dtemp)) return rc;
+                sig_src = (const R*)ctx->f_dtemp;
+            }
+            if (int rc = sigma_run<R>(ctx, SIG_CORR1, Lam, s.a, sig_src, ctx->da_sig, satol, srtol)) return rc;
+            if constexpr (sizeof(R) == 4) {
+                if (int rc = to_f(ctx, ctx->da_sig, ctx->f_dtemp)) return rc;
+            }
+            CK(cudaMemsetAsync(ctx->sig_tmp, 0, sizeof(double) * L.Nsig, ctx->st));
+            if (int rc = sigma_run<R>(ctx, SIG_CORR2, Lam, s.a, sig_src, ctx->sig_tmp, satol, srtol)) return rc;
+            // da.Σ += da_Σ.Σ + corr2 (index 0 included: both are zero there)
+            CK(launch_axpby(L, 1.0, ctx->da_sig, 1.0, da, true, false, ctx->st));
+            CK(launch_axpby(L, 1.0, ctx->sig_tmp, 1.0, da, true, false, ctx->st));
+        }
+    }
+    return 0;
+}
+
+int rhs_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* da, int eval, double gatol,
+            double grtol, double satol, double srtol, int sigma_corr) {
+    int rc;
+    if (ctx->precision == PFFRG_FP64) {
+        rc = dsigma_dev<double>(ctx, Lam, a, da, satol, srtol);
+        if (!rc) rc = dgamma_dev<double>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
+    } else {
+        rc = dsigma_dev<float>(ctx, Lam, a, da, satol, srtol);
+        if (!rc) rc = dgamma_dev<float>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
+    }
+    return rc;
+}
+
+int read_evals(pffrg_ctx* ctx) {
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, ctx->counter, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->last_evals = (int64_t)h;
+    return 0;
+}
+
+int absmax(pffrg_ctx* ctx, const double* a, double* dst) {
+    CK(launch_absmax_q3(ctx->L, a, ctx->partial, kPartials, dst, ctx->st));
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pffrg_last_error(const pffrg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int64_t pffrg_action_size(const pffrg_ctx* ctx) { return ctx ? ctx->L.total : 0; }
+
+int64_t pffrg_last_integrand_evals(const pffrg_ctx* ctx) { return ctx ? ctx->last_evals : 0; }
+
+void pffrg_destroy(pffrg_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    void* ptrs[] = {ctx->lat.exch, ctx->lat.mult, ctx->lat.ov_off, ctx->lat.ov_ab, ctx->lat.ov_m, ctx->lat.ov_mf,
+                    ctx->mesh, ctx->log_bounds, ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig, ctx->sig_tmp, ctx->f_a, ctx->f_da,
+                    ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
+                    ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
+        if (ctx->slot[k]) cudaFree(ctx->slot[k]);
+    if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* mesh, int symmetry, double S,
+                        int precision, int device) {
+    g_create_error.clear();
+    if (!lat || !mesh || !lat->exchange || !lat->mult || !lat->overlap_offsets || lat->num_sites <= 0) {
+        g_create_error = "invalid lattice view";
+        return nullptr;
+    }
+    if (symmetry != PFFRG_SU2) {
+        g_create_error = "only su2 symmetry is supported by this build";
+        return nullptr;
+    }
+    if (precision != PFFRG_FP64 && precision != PFFRG_MIXED) {
+        g_create_error = "unknown precision";
+        return nullptr;
+    }
+    if (lat->num_sites > 256) {
+        g_create_error = "more than 256 irreducible sites";
+        return nullptr;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev <= device || device < 0) {
+        g_create_error = std::string("no usable CUDA device: ") + cudaGetErrorString(e);
+        return nullptr;
+    }
+    pffrg_ctx* ctx = new pffrg_ctx();
+    ctx->device = device;
+    ctx->symmetry = symmetry;
+    ctx->S = S;
+    ctx->precision = precision;
+    auto bail = [&](const std::string& msg) -> pffrg_ctx* {
+        g_create_error = msg;
+        pffrg_destroy(ctx);
+        return nullptr;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return bail("cudaSetDevice failed");
+    if (check_mesh(ctx, mesh)) return bail(ctx->err);
+    const int Ns = (int)lat->num_sites;
+    ctx->L = make_layout(Ns, (int)mesh->num_sigma, (int)mesh->num_omega, (int)mesh->num_nu, 2);
+    const Layout& L = ctx->L;
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return bail("stream creation failed");
+
+    // lattice tables (0-based on the device)
+    std::vector<int> exch(Ns), mult(Ns), off(Ns + 1);
+    for (int i = 0; i < Ns; ++i) {
+        exch[i] = (int)lat->exchange[i] - 1;
+        mult[i] = (int)lat->mult[i];
+        if (exch[i] < 0 || exch[i] >= Ns) return bail("exchange table out of range");
+    }
+    for (int i = 0; i <= Ns; ++i) off[i] = (int)lat->overlap_offsets[i];
+    const int64_t R = off[Ns];
+    std::vector<int> ab(R > 0 ? R : 1);
+    std::vector<double> m64(R > 0 ? R : 1);
+    std::vector<float> m32(R > 0 ? R : 1);
+    for (int64_t j = 0; j < R; ++j) {
+        const int a = (int)lat->overlap_rows[3 * j] - 1, b = (int)lat->overlap_rows[3 * j + 1] - 1;
+        if (a < 0 || a >= Ns || b < 0 || b >= Ns) return bail("overlap table out of range");
+        ab[j] = a | (b << 16);
+        m64[j] = (double)lat->overlap_rows[3 * j + 2];
+        m32[j] = (float)m64[j];
+    }
+    ctx->lat.Ns = Ns;
+    ctx->lat.rows = R;
+    auto dalloc = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes > 0 ? bytes : 8) == cudaSuccess; };
+    bool ok = dalloc((void**)&ctx->lat.exch, sizeof(int) * Ns) && dalloc((void**)&ctx->lat.mult, sizeof(int) * Ns) &&
+              dalloc((void**)&ctx->lat.ov_off, sizeof(int) * (Ns + 1)) &&
+              dalloc((void**)&ctx->lat.ov_ab, sizeof(int) * ab.size()) &&
+              dalloc((void**)&ctx->lat.ov_m, sizeof(double) * m64.size()) &&
+              dalloc((void**)&ctx->lat.ov_mf, sizeof(float) * m32.size()) &&
+              dalloc((void**)&ctx->mesh, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn));
+    for (int k = 0; k < PFFRG_NUM_SLOTS && ok; ++k) ok = dalloc((void**)&ctx->slot[k], sizeof(double) * L.total);
+    ok = ok && dalloc((void**)&ctx->da_l, sizeof(double) * L.total) &&
+         dalloc((void**)&ctx->da_c, sizeof(double) * L.total) &&
+         dalloc((void**)&ctx->da_temp, sizeof(double) * L.total) &&
+         dalloc((void**)&ctx->da_sig, sizeof(double) * L.total) &&
+         dalloc((void**)&ctx->sig_tmp, sizeof(double) * L.Nsig) &&
+         dalloc((void**)&ctx->f_a, sizeof(float) * L.total) && dalloc((void**)&ctx->f_da, sizeof(float) * L.total) &&
+         dalloc((void**)&ctx->f_dal, sizeof(float) * L.total) &&
+         dalloc((void**)&ctx->f_dtemp, sizeof(float) * L.total) &&
+         dalloc((void**)&ctx->corrs, sizeof(double) * 6 * L.NO) &&
+         dalloc((void**)&ctx->corrs_sde, sizeof(double) * 6 * L.NO) &&
+         dalloc((void**)&ctx->partial, sizeof(double) * kPartials) &&
+         dalloc((void**)&ctx->scalars, sizeof(double) * 4) && dalloc((void**)&ctx->status, sizeof(int)) &&
+         dalloc((void**)&ctx->counter, sizeof(unsigned long long));
+    if (!ok) return bail("device allocation failed");
+    if (cudaHostAlloc((void**)&ctx->h_scalars, sizeof(double) * 4, cudaHostAllocDefault) != cudaSuccess)
+        return bail("pinned allocation failed");
+    std::vector<int4> ts = make_tasks(L.NO, L.Nn, 0), tf = make_tasks(L.NO, L.Nn, 1), tr = make_tasks(L.NO, L.Nn, 2);
+    ctx->n_sym = (int)ts.size();
+    ctx->n_full = (int)tf.size();
+    ctx->n_red = (int)tr.size();
+    ok = dalloc((void**)&ctx->tasks_sym, sizeof(int4) * ts.size()) &&
+         dalloc((void**)&ctx->tasks_full, sizeof(int4) * tf.size()) &&
+         dalloc((void**)&ctx->tasks_red, sizeof(int4) * tr.size());
+    if (!ok) return bail("device allocation failed");
+    cudaStream_t st = ctx->st;
+    bool cp = cudaMemcpyAsync(ctx->lat.exch, exch.data(), sizeof(int) * Ns, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->lat.mult, mult.data(), sizeof(int) * Ns, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->lat.ov_off, off.data(), sizeof(int) * (Ns + 1), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->lat.ov_ab, ab.data(), sizeof(int) * ab.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->lat.ov_m, m64.data(), sizeof(double) * m64.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->lat.ov_mf, m32.data(), sizeof(float) * m32.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->tasks_sym, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->tasks_full, tf.data(), sizeof(int4) * tf.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->tasks_red, tr.data(), sizeof(int4) * tr.size(), cudaMemcpyHostToDevice, st) == cudaSuccess;
+    for (int k = 0; k < PFFRG_NUM_SLOTS && cp; ++k)
+        cp = cudaMemsetAsync(ctx->slot[k], 0, sizeof(double) * L.total, st) == cudaSuccess;
+    double* scr[] = {ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig};
+    for (double* p : scr)
+        if (cp) cp = cudaMemsetAsync(p, 0, sizeof(double) * L.total, st) == cudaSuccess;
+    cp = cp && cudaMemsetAsync(ctx->status, 0, sizeof(int), st) == cudaSuccess &&
+         cudaMemsetAsync(ctx->corrs_sde, 0, sizeof(double) * 6 * L.NO, st) == cudaSuccess &&
+         cudaStreamSynchronize(st) == cudaSuccess;
+    if (!cp) return bail("device initialisation failed");
+    // hand the ABI's pinned copies of the 1-based tables back: nothing else to keep
+    if (upload_mesh(ctx, mesh)) return bail(ctx->err);
+    return ctx;
+}
+
+int pffrg_set_mesh(pffrg_ctx* ctx, const pffrg_mesh_view* mesh) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    return upload_mesh(ctx, mesh);
+}
+
+int pffrg_set_precision(pffrg_ctx* ctx, int precision) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (precision != PFFRG_FP64 && precision != PFFRG_MIXED) return ctx->fail(PFFRG_E_ARGS, "unknown precision %d", precision);
+    ctx->precision = precision;
+    return 0;
+}
+
+int pffrg_upload(pffrg_ctx* ctx, int slot, const pffrg_action_view* a) {
+    if (!ctx || slot < 0 || slot >= PFFRG_NUM_SLOTS) return ctx ? ctx->fail(PFFRG_E_ARGS, "bad slot") : PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    if (int rc = copy_view(ctx, ctx->slot[slot], a, true)) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pffrg_download(pffrg_ctx* ctx, int slot, pffrg_action_view* a) {
+    if (!ctx || slot < 0 || slot >= PFFRG_NUM_SLOTS) return ctx ? ctx->fail(PFFRG_E_ARGS, "bad slot") : PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    if (int rc = copy_view(ctx, ctx->slot[slot], a, false)) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pffrg_dsigma(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, pffrg_action_view* da, double atol,
+                 double rtol) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    if (int rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_A], a, true)) return rc;
+    if (int rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, true)) return rc;
+    int rc = ctx->precision == PFFRG_FP64
+                 ? dsigma_dev<double>(ctx, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], atol, rtol)
+                 : dsigma_dev<float>(ctx, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], atol, rtol);
+    if (rc) return rc;
+    if ((rc = check_status(ctx))) return rc;
+    if ((rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, false))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pffrg_dgamma(pffrg_ctx* ctx, int loops, double Lam, const pffrg_action_view* a, pffrg_action_view* da, int eval,
+                 double gatol, double grtol, int sigma_corr, double satol, double srtol) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (loops < 1 || eval < 1) return ctx->fail(PFFRG_E_ARGS, "loops and eval must be positive");
+    CK(cudaSetDevice(ctx->device));
+    if (int rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_A], a, true)) return rc;
+    if (int rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, true)) return rc;
+    int rc = ctx->precision == PFFRG_FP64
+                 ? dgamma_dev<double>(ctx, loops, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], eval, gatol,
+                                      grtol, sigma_corr, satol, srtol)
+                 : dgamma_dev<float>(ctx, loops, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], eval, gatol,
+                                     grtol, sigma_corr, satol, srtol);
+    if (rc) return rc;
+    if ((rc = check_status(ctx))) return rc;
+    if ((rc = read_evals(ctx))) return rc;
+    if ((rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, false))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pffrg_rhs(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, int eval, double gatol,
+              double grtol, double satol, double srtol, int sigma_corr) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (a_slot < 0 || a_slot >= PFFRG_NUM_SLOTS || da_slot < 0 || da_slot >= PFFRG_NUM_SLOTS || a_slot == da_slot)
+        return ctx->fail(PFFRG_E_ARGS, "bad slots");
+    if (loops < 1 || eval < 1) return ctx->fail(PFFRG_E_ARGS, "loops and eval must be positive");
+    CK(cudaSetDevice(ctx->device));
+    int rc = rhs_dev(ctx, loops, Lam, ctx->slot[a_slot], ctx->slot[da_slot], eval, gatol, grtol, satol, srtol,
+                     sigma_corr);
+    if (rc) return rc;
+    if ((rc = check_status(ctx))) return rc;
+    return read_evals(ctx);
+}
+
+int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
+              double grtol, double satol, double srtol) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    double* d1 = ctx->slot[PFFRG_SLOT_A];
+    double* d2 = ctx->slot[PFFRG_SLOT_DA];
+    if (int rc = copy_view(ctx, d1, a1, true)) return rc;
+    if (int rc = copy_view(ctx, d2, a2, true)) return rc;
+    auto run = [&](auto tag) -> int {
+        using R = decltype(tag);
+        const R* r1;
+        const R* r2;
+        if constexpr (sizeof(R) == 8) {
+            r1 = (const R*)d1;
+            r2 = (const R*)d2;
+        } else {
+            if (int rc = to_f(ctx, d1, ctx->f_a)) return rc;
+            r1 = (const R*)ctx->f_a;
+            r2 = (const R*)ctx->f_da;
+        }
+        if (int rc = corrs_run<R>(ctx, PROP_PLAIN, Lam, r1, r1, gatol, grtol, ctx->corrs_sde)) return rc;
+        if (int rc = upload_log_bounds(ctx, Lam, eval)) return rc;
+        // reduced s bubble (SDE.jl:2-56): slot 1 is the bare vertex
+        PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
+        p.tasks = ctx->tasks_red;
+        p.ntasks = ctx->n_red;
+        p.corrs = ctx->corrs_sde;
+        p.nchan = 1;
+        p.chan_of_y[0] = 0;
+        set_slots<R>(p, r1, r1, r1, r1, kMaskReduced);
+        p.prop_kind = PROP_PLAIN;
+        p.prop_a = r1;
+        p.prop_da = r1;
+        p.out = d2;
+        CK(launch_pass<R>(p, ctx->st));
+        if constexpr (sizeof(R) == 4) {
+            if (int rc = to_f(ctx, d2, ctx->f_da)) return rc;
+        }
+        return sigma_run<R>(ctx, SIG_SDE, Lam, r1, r2, d2, satol, srtol);
+    };
+    int rc = ctx->precision == PFFRG_FP64 ? run(double{}) : run(float{});
+    if (rc) return rc;
+    if ((rc = check_status(ctx))) return rc;
+    if ((rc = copy_view(ctx, d2, a2, false))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double atol,
+              double rtol) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    double* d1 = ctx->slot[PFFRG_SLOT_A];
+    double* d2 = ctx->slot[PFFRG_SLOT_DA];
+    if (int rc = copy_view(ctx, d1, a1, true)) return rc;
+    if (int rc = copy_view(ctx, d2, a2, true)) return rc;
+    auto run = [&](auto tag) -> int {
+        using R = decltype(tag);
+        const R* r1;
+        if constexpr (sizeof(R) == 8) {
+            r1 = (const R*)d1;
+        } else {
+            if (int rc = to_f(ctx, d1, ctx->f_a)) return rc;
+            r1 = (const R*)ctx->f_a;
+        }
+        if (int rc = upload_log_bounds(ctx, Lam, eval)) return rc;
+        // BSE kernels (BSE_su2_{s,t,u}.jl): slot 1 without the own channel
+        PassArgs<R> p = base_pass<R>(ctx, Lam, eval, atol, rtol);
+        set_tasks(p, ctx, false);
+        p.corrs = ctx->corrs_sde;
+        p.prop_kind = PROP_PLAIN;
+        p.prop_a = r1;
+        p.prop_da = r1;
+        p.out = d2;
+        set_slots<R>(p, r1, r1, r1, r1, kMaskLeft);
+        CK(launch_pass<R>(p, ctx->st));
+        CK(launch_symmetrize(ctx->L, ctx->lat.exch, d2, ctx->st));
+        return 0;
+    };
+    int rc = ctx->precision == PFFRG_FP64 ? run(double{}) : run(float{});
+    if (rc) return rc;
+    if ((rc = copy_view(ctx, d2, a2, false))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, double gatol, double grtol,
+                  double satol, double srtol, int sigma_corr, double ode_atol, double ode_rtol, double* err,
+                  double* abs_max_next) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    const Layout& L = ctx->L;
+    double* A = ctx->slot[PFFRG_SLOT_A];
+    double* K = ctx->slot[PFFRG_SLOT_DA];
+    double* I = ctx->slot[PFFRG_SLOT_INTER];
+    double* E = ctx->slot[PFFRG_SLOT_ERR];
+    double* N = ctx->slot[PFFRG_SLOT_NEXT];
+    const size_t bytes = sizeof(double) * L.total;
+    auto rhs = [&](double lam, const double* src) {
+        return rhs_dev(ctx, loops, lam, src, K, eval, gatol, grtol, satol, srtol, sigma_corr);
+    };
+    // launcher_1l.jl:83-116
+    CK(cudaMemcpyAsync(N, A, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaMemcpyAsync(E, A, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    int64_t evals = 0;
+    if (int rc = rhs(Lam, A)) return rc;
+    if (int rc = read_evals(ctx)) return rc;
+    evals += ctx->last_evals;
+    CK(launch_axpby(L, 1.0, K, -2.0 * dLam / 9.0, N, true, true, ctx->st));
+    CK(launch_axpby(L, 1.0, K, -7.0 * dLam / 24.0, E, true, true, ctx->st));
+    CK(cudaMemcpyAsync(I, A, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    CK(launch_axpby(L, 1.0, K, -0.5 * dLam, I, true, true, ctx->st));
+    if (int rc = rhs(Lam - 0.5 * dLam, I)) return rc;
+    if (int rc = read_evals(ctx)) return rc;
+    evals += ctx->last_evals;
+    CK(launch_axpby(L, 1.0, K, -1.0 * dLam / 3.0, N, true, true, ctx->st));
+    CK(launch_axpby(L, 1.0, K, -1.0 * dLam / 4.0, E, true, true, ctx->st));
+    CK(cudaMemcpyAsync(I, A, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    CK(launch_axpby(L, 1.0, K, -0.75 * dLam, I, true, true, ctx->st));
+    if (int rc = rhs(Lam - 0.75 * dLam, I)) return rc;
+    if (int rc = read_evals(ctx)) return rc;
+    evals += ctx->last_evals;
+    CK(launch_axpby(L, 1.0, K, -4.0 * dLam / 9.0, N, true, true, ctx->st));
+    CK(launch_axpby(L, 1.0, K, -1.0 * dLam / 3.0, E, true, true, ctx->st));
+    CK(cudaMemcpyAsync(I, N, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    if (int rc = rhs(Lam - dLam, I)) return rc;
+    if (int rc = read_evals(ctx)) return rc;
+    evals += ctx->last_evals;
+    CK(launch_axpby(L, 1.0, K, -1.0 * dLam / 8.0, E, true, true, ctx->st));
+    // subtract_from!(a_inter, a_err) and the error ratio (launcher_1l.jl:112-116)
+    CK(launch_axpby(L, 1.0, I, -1.0, E, true, true, ctx->st));
+    if (int rc = absmax(ctx, E, ctx->scalars + 0)) return rc;
+    if (int rc = absmax(ctx, I, ctx->scalars + 1)) return rc;
+    if (int rc = absmax(ctx, A, ctx->scalars + 2)) return rc;
+    CK(cudaMemcpyAsync(ctx->h_scalars, ctx->scalars, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (int rc = check_status(ctx)) return rc;
+    const double delta = ctx->h_scalars[0];
+    const double scale = ode_atol + fmax(ctx->h_scalars[1], ctx->h_scalars[2]) * ode_rtol;
+    if (err) *err = delta / scale;
+    if (abs_max_next) *abs_max_next = ctx->h_scalars[1];
+    ctx->last_evals = evals;
+    return 0;
+}
+
+int pffrg_accept(pffrg_ctx* ctx) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_NEXT], sizeof(double) * ctx->L.total,
+                       cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+void* pffrg_host_alloc(int64_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void pffrg_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

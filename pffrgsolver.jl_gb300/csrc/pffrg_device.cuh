@@ -1,0 +1,339 @@
+// Device-side building blocks of the flow right-hand side (sm_103a).
+//
+// Everything here is templated on the arithmetic type R of the integrand:
+// double for the FP64 path, float for the mixed path (FP32 integrand, FP64
+// quadrature bookkeeping).  The functions restate the reference's frequency
+// lookups (src/Frequency/param.jl, buffer.jl), the self energy and propagators
+// (src/Action/Action.jl:8-26, src/Flow/bubbles.jl:2-96) and the vertex
+// interpolation (src/Action/channel.jl:55-305) in a form that precomputes, once
+// per node, the corner weights and offsets every site then reuses.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pffrg {
+
+constexpr int kMaxMesh = 128;  // longest supported mesh (num_* + 1)
+
+// Packed action layout: Σ[Nsig] | comp c: bare[Ns] | ch s,t,u: q1 q2_1 q2_2 q3
+// (all Julia column-major, site fastest).
+struct Layout {
+    int Ns, Nsig, NO, Nn, C;
+    int64_t K1, K2, K3, chan, comp, total;
+    __host__ __device__ int64_t bare(int c) const { return Nsig + c * comp; }
+    __host__ __device__ int64_t qbase(int c, int ch, int k) const {
+        int64_t b = Nsig + c * comp + Ns + ch * chan;
+        return b + (k == 0 ? 0 : (k == 1 ? K1 : (k == 2 ? K1 + K2 : K1 + 2 * K2)));
+    }
+};
+
+inline Layout make_layout(int Ns, int Nsig, int NO, int Nn, int C) {
+    Layout L;
+    L.Ns = Ns;
+    L.Nsig = Nsig;
+    L.NO = NO;
+    L.Nn = Nn;
+    L.C = C;
+    L.K1 = (int64_t)Ns * NO;
+    L.K2 = L.K1 * Nn;
+    L.K3 = L.K2 * Nn;
+    L.chan = L.K1 + 2 * L.K2 + L.K3;
+    L.comp = Ns + 3 * L.chan;
+    L.total = Nsig + C * L.comp;
+    return L;
+}
+
+// Meshes staged in shared memory: values and reciprocal spacings
+// inv[k] = 1 / (x[k+1] - x[k]) (the reference's d in get_param, param.jl:73).
+template <typename R>
+struct SMesh {
+    R sig[kMaxMesh], isig[kMaxMesh];
+    R Os[kMaxMesh], iOs[kMaxMesh];
+    R ns[kMaxMesh], ins[kMaxMesh];
+    R Ot[kMaxMesh], iOt[kMaxMesh];
+    R nt[kMaxMesh], int_[kMaxMesh];
+};
+
+// device mesh block written by the host: [σ | Ωs | νs | Ωt | νt] (FP64)
+template <typename R>
+__device__ inline void load_mesh(SMesh<R>& M, const double* mesh, int Nsig, int NO, int Nn) {
+    const double* sig = mesh;
+    const double* Os = sig + Nsig;
+    const double* ns = Os + NO;
+    const double* Ot = ns + Nn;
+    const double* nt = Ot + NO;
+    for (int k = threadIdx.x; k < Nsig; k += blockDim.x) {
+        M.sig[k] = (R)sig[k];
+        M.isig[k] = (k + 1 < Nsig) ? (R)(1.0 / (sig[k + 1] - sig[k])) : (R)0;
+    }
+    for (int k = threadIdx.x; k < NO; k += blockDim.x) {
+        M.Os[k] = (R)Os[k];
+        M.iOs[k] = (k + 1 < NO) ? (R)(1.0 / (Os[k + 1] - Os[k])) : (R)0;
+        M.Ot[k] = (R)Ot[k];
+        M.iOt[k] = (k + 1 < NO) ? (R)(1.0 / (Ot[k + 1] - Ot[k])) : (R)0;
+    }
+    for (int k = threadIdx.x; k < Nn; k += blockDim.x) {
+        M.ns[k] = (R)ns[k];
+        M.ins[k] = (k + 1 < Nn) ? (R)(1.0 / (ns[k + 1] - ns[k])) : (R)0;
+        M.nt[k] = (R)nt[k];
+        M.int_[k] = (k + 1 < Nn) ? (R)(1.0 / (nt[k + 1] - nt[k])) : (R)0;
+    }
+}
+
+template <typename R>
+struct Param {
+    int lo, hi;
+    R wl, wu;
+};
+
+// get_indices + get_param (param.jl:26-87) with a binary search that returns
+// the same pair as the reference's linear scan: hi = first k with x[k] >= val.
+template <typename R>
+__device__ __forceinline__ Param<R> get_param(R val, const R* x, const R* ix, int n) {
+    Param<R> p;
+    if (val >= x[n - 1]) {
+        p.lo = p.hi = n - 1;
+        p.wl = (R)1;
+        p.wu = (R)0;
+        return p;
+    }
+    int lo = 0, hi = n - 1;
+    if (!(val == val)) hi = 0;  // NaN: the linear scan stops at the first entry
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (x[mid] >= val) hi = mid;
+        else lo = mid + 1;
+    }
+    p.hi = lo;
+    p.lo = (val < x[lo]) ? lo - 1 : lo;
+    if (p.lo < 0) p.lo = 0;
+    if (p.lo < p.hi) {
+        R d = ix[p.lo];
+        p.wl = d * (x[p.hi] - val);
+        p.wu = d * (val - x[p.lo]);
+    } else {
+        p.wl = (R)1;
+        p.wu = (R)0;
+    }
+    return p;
+}
+
+// Interpolation plan of one buffer (one channel read of one vertex slot):
+// the asymptotic kernel, the channel actually read (s<->u mapping), the
+// site-exchange flag, the sign for the density component and the corner
+// weights and offsets of the (multi)linear interpolation in the reference's
+// term order (channel.jl:245-305).
+template <typename R>
+struct Plan {
+    int kernel;  // 0 none, 1 q1, 2 q2_1, 3 q2_2, 4 q3
+    int src_ch;  // 0 s, 1 t, 2 u
+    int exch;
+    R sgn_d;
+    R w[8];
+    int off[8];
+};
+
+template <typename R>
+__device__ __forceinline__ void make_plan(Plan<R>& P, int chan, R w, R v, R vp, const SMesh<R>& M, int Ns,
+                                          int NO, int Nn) {
+    bool ex = false, mp = false, sm = false, sn = false;
+    if (chan == 0) {  // get_buffer_s (buffer.jl:87-124)
+        if (w < (R)0) { w = -w; ex = !ex; }
+        if (v < (R)0) { v = -v; ex = !ex; mp = !mp; sm = !sm; }
+        if (vp < (R)0) { vp = -vp; mp = !mp; sn = !sn; }
+    } else if (chan == 1) {  // get_buffer_t (buffer.jl:126-160)
+        if (w < (R)0) { w = -w; }
+        if (v < (R)0) { v = -v; sm = !sm; }
+        if (vp < (R)0) { vp = -vp; sn = !sn; }
+    } else {  // get_buffer_u (buffer.jl:162-199)
+        if (w < (R)0) { w = -w; ex = !ex; }
+        if (v < (R)0) { v = -v; ex = !ex; mp = !mp; sn = !sn; }
+        if (vp < (R)0) { vp = -vp; mp = !mp; sn = !sn; }
+    }
+    const R* Om = chan == 1 ? M.Ot : M.Os;
+    const R* iOm = chan == 1 ? M.iOt : M.iOs;
+    const R* nu = chan == 1 ? M.nt : M.ns;
+    const R* inu = chan == 1 ? M.int_ : M.ins;
+    if (Om[NO - 1] < fabs(w)) {  // get_buffer (buffer.jl:51-84): beyond the bosonic mesh
+        P.kernel = 0;
+        return;
+    }
+    P.exch = ex ? 1 : 0;
+    P.src_ch = (chan == 1) ? 1 : ((chan == 0) == mp ? 2 : 0);
+    P.sgn_d = ((sm ? -1 : 1) * (sn ? -1 : 1)) < 0 ? (R)-1 : (R)1;
+    const Param<R> p1 = get_param(w, Om, iOm, NO);
+    const bool vin = !(nu[Nn - 1] < fabs(v));
+    const bool vpin = !(nu[Nn - 1] < fabs(vp));
+    if (!vin && !vpin) {
+        P.kernel = 1;
+        P.w[0] = p1.wl;
+        P.w[1] = p1.wu;
+        P.off[0] = Ns * p1.lo;
+        P.off[1] = Ns * p1.hi;
+    } else if (vin != vpin) {
+        P.kernel = vin ? 2 : 3;
+        const Param<R> pb = get_param(vin ? v : vp, nu, inu, Nn);
+        P.w[0] = p1.wl * pb.wl;
+        P.w[1] = p1.wu * pb.wl;
+        P.w[2] = p1.wl * pb.wu;
+        P.w[3] = p1.wu * pb.wu;
+        P.off[0] = Ns * (p1.lo + NO * pb.lo);
+        P.off[1] = Ns * (p1.hi + NO * pb.lo);
+        P.off[2] = Ns * (p1.lo + NO * pb.hi);
+        P.off[3] = Ns * (p1.hi + NO * pb.hi);
+    } else {
+        P.kernel = 4;
+        const Param<R> p2 = get_param(v, nu, inu, Nn);
+        const Param<R> p3 = get_param(vp, nu, inu, Nn);
+        const int NON = NO * Nn;
+        P.w[0] = p1.wl * p2.wl * p3.wl;
+        P.w[1] = p1.wu * p2.wl * p3.wl;
+        P.w[2] = p1.wl * p2.wu * p3.wl;
+        P.w[3] = p1.wu * p2.wu * p3.wl;
+        P.w[4] = p1.wl * p2.wl * p3.wu;
+        P.w[5] = p1.wu * p2.wl * p3.wu;
+        P.w[6] = p1.wl * p2.wu * p3.wu;
+        P.w[7] = p1.wu * p2.wu * p3.wu;
+        P.off[0] = Ns * (p1.lo + NO * p2.lo + NON * p3.lo);
+        P.off[1] = Ns * (p1.hi + NO * p2.lo + NON * p3.lo);
+        P.off[2] = Ns * (p1.lo + NO * p2.hi + NON * p3.lo);
+        P.off[3] = Ns * (p1.hi + NO * p2.hi + NON * p3.lo);
+        P.off[4] = Ns * (p1.lo + NO * p2.lo + NON * p3.hi);
+        P.off[5] = Ns * (p1.hi + NO * p2.lo + NON * p3.hi);
+        P.off[6] = Ns * (p1.lo + NO * p2.hi + NON * p3.hi);
+        P.off[7] = Ns * (p1.hi + NO * p2.hi + NON * p3.hi);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T ldg(const T* p) {
+    return __ldg(p);
+}
+
+// Σ_k w_k q[off_k + s] for one plan (kernel > 0), terms in the reference's order
+template <typename R>
+__device__ __forceinline__ R plan_read(const Plan<R>& P, const R* __restrict__ q, int s) {
+    R val;
+    switch (P.kernel) {
+        case 1:
+            val = P.w[0] * ldg(q + P.off[0] + s);
+            val += P.w[1] * ldg(q + P.off[1] + s);
+            return val;
+        case 2:
+        case 3:
+            val = P.w[0] * ldg(q + P.off[0] + s);
+            val += P.w[1] * ldg(q + P.off[1] + s);
+            val += P.w[2] * ldg(q + P.off[2] + s);
+            val += P.w[3] * ldg(q + P.off[3] + s);
+            return val;
+        default:
+            val = P.w[0] * ldg(q + P.off[0] + s);
+#pragma unroll
+            for (int k = 1; k < 8; ++k) val += P.w[k] * ldg(q + P.off[k] + s);
+            return val;
+    }
+}
+
+__host__ __device__ constexpr int corners_of(int kernel) {
+    return kernel == 0 ? 0 : (kernel == 1 ? 2 : (kernel == 4 ? 8 : 4));
+}
+
+// ---------------------------------------------------------------------------
+// self energy and propagators
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R jl_sign(R x) {
+    return x > (R)0 ? (R)1 : (x < (R)0 ? (R)-1 : x);
+}
+
+// get_Σ (Action.jl:8-26): Σ values of an action read from global memory
+template <typename R>
+__device__ __forceinline__ R get_sigma(const SMesh<R>& M, int Nsig, const R* __restrict__ Sig, R w) {
+    if (fabs(w) <= M.sig[Nsig - 1]) {
+        Param<R> p = get_param((R)fabs(w), M.sig, M.isig, Nsig);
+        return jl_sign(w) * (p.wl * ldg(Sig + p.lo) + p.wu * ldg(Sig + p.hi));
+    }
+    return M.sig[Nsig - 1] * ldg(Sig + Nsig - 1) / w;
+}
+
+__device__ __forceinline__ double expm1_r(double x) { return expm1(x); }
+__device__ __forceinline__ float expm1_r(float x) { return expm1f(x); }
+__device__ __forceinline__ double exp_r(double x) { return exp(x); }
+__device__ __forceinline__ float exp_r(float x) { return expf(x); }
+
+template <typename R>
+__device__ __forceinline__ R G_bare(R L, R w) {
+    if (fabs(w) > (R)1e-8) return -expm1_r(-(w * w) / (L * L)) / w;
+    return (R)0;
+}
+
+template <typename R>
+__device__ __forceinline__ R G_full(const SMesh<R>& M, int Nsig, const R* Sig, R L, R w) {
+    if (fabs(w) > (R)1e-8) {
+        R s = get_sigma(M, Nsig, Sig, w);
+        R g0 = G_bare(L, w);
+        R den = (w * s >= (R)0) ? (R)1 / g0 + s : (R)1 / g0;
+        return (R)1 / den;
+    }
+    return (R)0;
+}
+
+template <typename R>
+__device__ __forceinline__ R S_single(const SMesh<R>& M, int Nsig, const R* Sig, R L, R w) {
+    if (fabs(w) > (R)1e-8) {
+        R g = G_full(M, Nsig, Sig, L, w);
+        R g0 = G_bare(L, w);
+        R r = g / g0;
+        return r * r * exp_r(-(w * w) / (L * L)) * (R)2 * w / (L * L * L);
+    }
+    return (R)0;
+}
+
+template <typename R>
+__device__ __forceinline__ R two_pi() {
+    return (R)(2.0 * 3.14159265358979323846);
+}
+
+// get_propagator_kat (bubbles.jl:64-80)
+template <typename R>
+__device__ __forceinline__ R prop_kat(const SMesh<R>& M, int Nsig, const R* Sig, const R* dSig, R L, R w1, R w2) {
+    R ds = get_sigma(M, Nsig, dSig, w1);
+    R s1 = S_single(M, Nsig, Sig, L, w1);
+    R g1 = G_full(M, Nsig, Sig, L, w1);
+    R g2 = G_full(M, Nsig, Sig, L, w2);
+    return (s1 + g1 * g1 * ds) * g2 / two_pi<R>();
+}
+
+// get_propagator (bubbles.jl:83-96)
+template <typename R>
+__device__ __forceinline__ R prop_plain(const SMesh<R>& M, int Nsig, const R* Sig, R L, R w1, R w2) {
+    R g1 = G_full(M, Nsig, Sig, L, w1);
+    R g2 = G_full(M, Nsig, Sig, L, w2);
+    return g1 * g2 / two_pi<R>();
+}
+
+// one half of the bubble propagator of channel ch at node v and transfer W
+// (flow_su2_{s,t,u}.jl: first lines of every kernel, bubbles.jl:99-221)
+template <typename R>
+__device__ __forceinline__ R prop_half(int kind, int half, int ch, const SMesh<R>& M, int Nsig, const R* Sig,
+                                       const R* dSig, R L, R v, R W) {
+    R w1, w2;
+    const R hW = (R)0.5 * W;
+    if (ch == 0) {
+        w1 = v + hW;
+        w2 = hW - v;
+    } else if (ch == 1) {
+        w1 = v + hW;
+        w2 = v - hW;
+    } else {
+        w1 = v - hW;
+        w2 = v + hW;
+    }
+    if (kind == 0) {
+        return half == 0 ? prop_kat(M, Nsig, Sig, dSig, L, w1, w2) : prop_kat(M, Nsig, Sig, dSig, L, w2, w1);
+    }
+    return -prop_plain(M, Nsig, Sig, L, w1, w2);
+}
+
+}  // namespace pffrg

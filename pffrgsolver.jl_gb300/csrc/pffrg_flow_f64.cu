@@ -1,0 +1,11 @@
+// FP64 instantiation of the channel-task kernel.
+#include "pffrg_flow.cuh"
+
+namespace pffrg {
+
+template <>
+cudaError_t launch_pass<double>(const PassArgs<double>& a, cudaStream_t st) {
+    return launch_pass_impl<double>(a, st);
+}
+
+}  // namespace pffrg

@@ -1,0 +1,103 @@
+// Host-side interface between the translation units of libpffrg_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pffrg_device.cuh"
+
+namespace pffrg {
+
+enum PropKind { PROP_KAT = 0, PROP_PLAIN = 1 };
+enum ChannelMask { CH_S = 1, CH_T = 2, CH_U = 4, CH_ALL = 7 };
+
+// Lattice tables on the device (0-based site indices).
+struct DevLattice {
+    int Ns = 0;
+    int64_t rows = 0;
+    int* exch = nullptr;     // [Ns]
+    int* mult = nullptr;     // [Ns]
+    int* ov_off = nullptr;   // [Ns+1]
+    int* ov_ab = nullptr;    // [R] site a | (site b << 16)
+    double* ov_m = nullptr;  // [R] multiplicity
+    float* ov_mf = nullptr;  // [R] multiplicity (FP32 path)
+};
+
+// One pass of channel tasks (Katanin / left / central / BSE / reduced-s).
+template <typename R>
+struct PassArgs {
+    Layout L;
+    const R* src[4];   // vertex slot sources
+    int mask[3][4];    // [channel X][slot]: channels read (CH_*), 0 = bare only
+    int prop_kind;
+    const R* prop_a;   // Σ of the propagators
+    const R* prop_da;  // dΣ of the Katanin propagator
+    double* out;       // FP64 output action
+    const int* exch;
+    const int* ov_off;
+    const int* ov_ab;
+    const R* ov_m;
+    const double* mesh;
+    const double* corrs;  // [2,3,NO]
+    const double* log_bounds;  // [mesh s/u = 0, t = 1][w1][k = 0..eval]: ξ^k a of integrate_log!
+    const int4* tasks;    // (kernel 1..4, w1, w2, w3), 0-based frequency indices
+    int ntasks;
+    int nchan;            // channels launched (3, or 1 for the reduced s bubble)
+    int chan_of_y[3];     // blockIdx.y -> channel
+    double Lam, atol, rtol;
+    int eval;
+    double twoS;
+    unsigned long long* node_counter;  // optional: integrand evaluations
+};
+
+template <typename R>
+cudaError_t launch_pass(const PassArgs<R>& a, cudaStream_t st);
+
+// GK integrals of the self energy / corrections (QuadGK-equivalent)
+enum SigmaKind { SIG_FLOW = 0, SIG_CORR1 = 1, SIG_CORR2 = 2, SIG_SDE = 3 };
+
+template <typename R>
+struct SigmaArgs {
+    Layout L;
+    int kind;
+    const R* a;    // propagator action (Σ) and, for SIG_FLOW/SIG_CORR2, the vertex
+    const R* aux;  // vertex of SIG_CORR1/SIG_SDE; Σ of SIG_CORR2
+    double* out;   // FP64 [Nsig] (index 0 untouched)
+    const int* exch;
+    const int* mult;
+    const double* mesh;
+    double Lam, atol, rtol, twoS;
+    int* status;   // nonzero: segment capacity exceeded
+};
+
+template <typename R>
+cudaError_t launch_sigma(const SigmaArgs<R>& a, cudaStream_t st);
+
+template <typename R>
+struct CorrsArgs {
+    int NO, Nn, Nsig, kind;
+    const R* a;
+    const R* da;
+    const double* mesh;
+    double Lam, atol, rtol;
+    double* corrs;  // [2,3,NO]
+    int* status;
+};
+
+template <typename R>
+cudaError_t launch_corrs(const CorrsArgs<R>& a, cudaStream_t st);
+
+// elementwise action kernels (FP64)
+cudaError_t launch_symmetrize(const Layout& L, const int* exch, double* a, cudaStream_t st);
+cudaError_t launch_symmetrize_add_to(const Layout& L, const int* exch, const double* al, double* a,
+                                     cudaStream_t st);
+// y[gamma part] = alpha * y + beta * x over the vertex part (bare excluded); sigma_too adds Σ
+cudaError_t launch_axpby(const Layout& L, double alpha, const double* x, double beta, double* y, bool sigma_too,
+                         bool gamma_too, cudaStream_t st);
+cudaError_t launch_to_float(const double* x, float* y, int64_t n, cudaStream_t st);
+// max |q3| over all components/channels -> out[0] (double, via block partials)
+cudaError_t launch_absmax_q3(const Layout& L, const double* a, double* partial, int npartial, double* out,
+                             cudaStream_t st);
+// max over i of |x_i| for the vertex q3 part of (x - y) etc. are composed from the above
+
+}  // namespace pffrg

@@ -1,0 +1,132 @@
+"""Flow right-hand side on the GPU, behind the reference's function names.
+
+``FlowContext`` owns one libpffrg_gpu context (device memory, stream) for a
+lattice, a mesh size and a symmetry.  Its methods mirror the reference's
+internal API (same argument meaning, outputs written in place):
+
+* compute_dΣ!       src/Flow/flow_self.jl:2-20           -> ``compute_dsigma``
+* compute_dΓ_1l!    src/Flow/compute.jl:57-112            -> ``compute_dgamma(loops=1)``
+* compute_dΓ_2l!    src/Flow/compute.jl:115-174           -> ``compute_dgamma(loops=2)``
+* compute_dΓ_ml!    src/Flow/compute.jl:177-287 (+ compute_dΣ_corr!, flow_self.jl:23-51)
+* compute_Σ!        src/Flow/SDE.jl:58-96                 -> ``compute_sigma_sde``
+* compute_Γ!        src/Flow/compute.jl:2-54              -> ``compute_gamma_bse``
+
+A nonzero status from the library raises ``PffrgError`` with the library's
+message (the reference raises AssertionErrors on the same conditions).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from .action import Action
+
+
+class FlowContext:
+    def __init__(self, r, m, symmetry: str = "su2", S: float = 0.5, precision: str = "fp64", device: int = 0):
+        self.lib = _capi.load()
+        self._lat, self._lat_keep = _capi.lattice_view(r)
+        self._mesh, self._mesh_keep = _capi.mesh_view(m)
+        self.symmetry = symmetry
+        self.S = S
+        prec = _capi.PFFRG_FP64 if precision == "fp64" else _capi.PFFRG_MIXED
+        sym = _capi.PFFRG_SU2 if symmetry == "su2" else _capi.PFFRG_U1_DM
+        h = self.lib.pffrg_create(ctypes.byref(self._lat), ctypes.byref(self._mesh), sym, S, prec, device)
+        if not h:
+            raise _capi.PffrgError(self.lib.pffrg_last_error(None).decode())
+        self.h = h
+        self.num_sites = r.num_sites
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pffrg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------------
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.lib.pffrg_last_error(self.h).decode()
+            raise _capi.PffrgError(f"{what}: code {rc}: {msg}")
+
+    @property
+    def action_size(self) -> int:
+        return int(self.lib.pffrg_action_size(self.h))
+
+    def set_mesh(self, m) -> None:
+        self._mesh, self._mesh_keep = _capi.mesh_view(m)
+        self._check(self.lib.pffrg_set_mesh(self.h, ctypes.byref(self._mesh)), "set_mesh")
+
+    def set_precision(self, precision: str) -> None:
+        p = _capi.PFFRG_FP64 if precision == "fp64" else _capi.PFFRG_MIXED
+        self._check(self.lib.pffrg_set_precision(self.h, p), "set_precision")
+
+    @property
+    def last_integrand_evals(self) -> int:
+        return int(self.lib.pffrg_last_integrand_evals(self.h))
+
+    # ---- reference-facing calls (host arrays in, host arrays out) ----
+    def compute_dsigma(self, Lam: float, a: Action, da: Action, sigma_tol=(1e-8, 1e-4)) -> None:
+        av, dv = _capi.action_view(a), _capi.action_view(da)
+        self._check(self.lib.pffrg_dsigma(self.h, Lam, ctypes.byref(av), ctypes.byref(dv), *sigma_tol), "dsigma")
+
+    def compute_dgamma(self, Lam: float, a: Action, da: Action, eval_: int, gamma_tol=(1e-8, 1e-4),
+                       loops: int = 1, sigma_corr: bool = False, sigma_tol=(1e-8, 1e-4)) -> None:
+        av, dv = _capi.action_view(a), _capi.action_view(da)
+        self._check(self.lib.pffrg_dgamma(self.h, loops, Lam, ctypes.byref(av), ctypes.byref(dv), eval_,
+                                          gamma_tol[0], gamma_tol[1], int(sigma_corr), sigma_tol[0], sigma_tol[1]),
+                    "dgamma")
+
+    def compute_sigma_sde(self, Lam: float, a1: Action, a2: Action, eval_: int, gamma_tol=(1e-8, 1e-4),
+                          sigma_tol=(1e-8, 1e-4)) -> None:
+        v1, v2 = _capi.action_view(a1), _capi.action_view(a2)
+        self._check(self.lib.pffrg_sde(self.h, Lam, ctypes.byref(v1), ctypes.byref(v2), eval_, gamma_tol[0],
+                                       gamma_tol[1], sigma_tol[0], sigma_tol[1]), "sde")
+
+    def compute_gamma_bse(self, Lam: float, a1: Action, a2: Action, eval_: int, gamma_tol=(1e-8, 1e-4)) -> None:
+        v1, v2 = _capi.action_view(a1), _capi.action_view(a2)
+        self._check(self.lib.pffrg_bse(self.h, Lam, ctypes.byref(v1), ctypes.byref(v2), eval_, *gamma_tol), "bse")
+
+    # ---- device-resident interface ----
+    def upload(self, slot: int, a: Action) -> None:
+        v = _capi.action_view(a)
+        self._check(self.lib.pffrg_upload(self.h, slot, ctypes.byref(v)), "upload")
+
+    def download(self, slot: int, a: Action) -> None:
+        v = _capi.action_view(a)
+        self._check(self.lib.pffrg_download(self.h, slot, ctypes.byref(v)), "download")
+
+    def rhs(self, Lam: float, eval_: int, loops: int = 1, a_slot: int = _capi.SLOT_A, da_slot: int = _capi.SLOT_DA,
+            gamma_tol=(1e-8, 1e-4), sigma_tol=(1e-8, 1e-4), sigma_corr: bool = False) -> None:
+        self._check(self.lib.pffrg_rhs(self.h, loops, Lam, a_slot, da_slot, eval_, gamma_tol[0], gamma_tol[1],
+                                       sigma_tol[0], sigma_tol[1], int(sigma_corr)), "rhs")
+
+    def bs_step(self, Lam: float, dLam: float, eval_: int, loops: int = 1, gamma_tol=(1e-8, 1e-4),
+                sigma_tol=(1e-8, 1e-4), sigma_corr: bool = False, ode_tol=(1e-8, 1e-2)):
+        err = ctypes.c_double()
+        amax = ctypes.c_double()
+        self._check(self.lib.pffrg_bs_step(self.h, loops, Lam, dLam, eval_, gamma_tol[0], gamma_tol[1], sigma_tol[0],
+                                           sigma_tol[1], int(sigma_corr), ode_tol[0], ode_tol[1], ctypes.byref(err),
+                                           ctypes.byref(amax)), "bs_step")
+        return float(err.value), float(amax.value)
+
+    def accept(self) -> None:
+        self._check(self.lib.pffrg_accept(self.h), "accept")
+
+
+def get_eval(Lam: float, min_eval: int, max_eval: int) -> int:
+    """Subdomains per integration range (launcher_1l.jl:78)."""
+    return int(min(max(int(np.ceil(min_eval / np.sqrt(Lam))), min_eval), max_eval))

@@ -1,0 +1,95 @@
+"""GPU flow right-hand side vs the FP64 CPU oracle, through the C ABI.
+
+FP64 path: the GPU follows the same adaptive decisions as the oracle, so the
+results agree to rounding (tolerance 1e-10 relative in the max norm).
+Mixed path: FP32 integrand with compensated node sums; its error against the
+oracle is measured and bounded (tolerance written per test).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(x, ref):
+    return float(np.max(np.abs(x - ref)) / max(np.max(np.abs(ref)), 1e-300))
+
+
+def state(pkg, name="square-L3-1l", **kw):
+    import pffrg_gb300.workloads as wl
+
+    return wl.build_state(wl.WORKLOADS[name], **kw)
+
+
+def oracle_rhs(O, r, m, a, Lam, loops, eval_, sigma_corr=False):
+    P = O.Problem(r, m)
+    da = np.zeros_like(a.buf)
+    O.dsigma(P, Lam, a.buf, da)
+    O.dgamma(P, loops, Lam, a.buf, da, eval_, sigma_corr=sigma_corr)
+    return da
+
+
+SMALL = dict(num_sigma=12, num_omega=5, num_nu=4)
+
+
+@pytest.mark.parametrize("lattice,size", [("square", 3), ("honeycomb", 3), ("kagome", 3)])
+@pytest.mark.parametrize("loops", [1, 2, 3])
+def test_dgamma_fp64_small(pkg, O, lattice, size, loops):
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = wl.Workload("t", lattice, size, "heisenberg", [[1.0]], loops, 1.0, 12, 5, 4, 0.1, 7)
+    lat, r, m, a = wl.build_state(w)
+    ref = oracle_rhs(O, r, m, a, 1.0, loops, 3, sigma_corr=loops >= 3)
+    da = pkg.action.Action.empty_like(a)
+    with FlowContext(r, m, precision="fp64") as ctx:
+        ctx.compute_dsigma(1.0, a, da)
+        ctx.compute_dgamma(1.0, a, da, 3, loops=loops, sigma_corr=loops >= 3)
+        assert ctx.last_integrand_evals > 0
+    assert rel_err(da.Σ, ref[: m.num_sigma]) < 1e-10
+    assert rel_err(da.buf, ref) < 1e-10
+
+
+def test_dgamma_fp64_config1_full(pkg, O):
+    """BASELINE configs[0] shapes: square L=3, 50/15/10 frequencies, Λ=1, N(0, 0.1) seed 0, 1 loop."""
+    from pffrg_gb300.flow import FlowContext
+
+    lat, r, m, a = state(pkg)
+    ref = oracle_rhs(O, r, m, a, 1.0, 1, 10)
+    da = pkg.action.Action.empty_like(a)
+    with FlowContext(r, m, precision="fp64") as ctx:
+        ctx.compute_dsigma(1.0, a, da)
+        ctx.compute_dgamma(1.0, a, da, 10)
+    assert rel_err(da.buf, ref) < 1e-10
+
+
+def test_dgamma_mixed_config1(pkg, O):
+    """Mixed precision against the FP64 oracle (error bound 1e-4 relative in the max norm)."""
+    from pffrg_gb300.flow import FlowContext
+
+    lat, r, m, a = state(pkg)
+    ref = oracle_rhs(O, r, m, a, 1.0, 1, 10)
+    da = pkg.action.Action.empty_like(a)
+    with FlowContext(r, m, precision="mixed") as ctx:
+        ctx.compute_dsigma(1.0, a, da)
+        ctx.compute_dgamma(1.0, a, da, 10)
+    e = rel_err(da.buf, ref)
+    print(f"mixed vs FP64 oracle: {e:.3e}")
+    assert e < 1e-4
+
+
+def test_parquet_fp64_small(pkg, O):
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = wl.Workload("t", "square", 3, "heisenberg", [[1.0]], 1, 1.0, 12, 5, 4, 0.1, 11)
+    lat, r, m, a = wl.build_state(w)
+    P = O.Problem(r, m)
+    a2_ref = np.zeros_like(a.buf)
+    corrs = O.sde(P, 1.0, a.buf, a2_ref, 3)
+    O.bse(P, 1.0, a.buf, a2_ref, corrs, 3)
+    a2 = pkg.action.Action.empty_like(a)
+    with FlowContext(r, m, precision="fp64") as ctx:
+        ctx.compute_sigma_sde(1.0, a, a2, 3)
+        ctx.compute_gamma_bse(1.0, a, a2, 3)
+    assert rel_err(a2.buf, a2_ref) < 1e-10
