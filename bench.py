@@ -1,0 +1,387 @@
+#!/usr/bin/env python
+"""Benchmark of the flow right-hand side on GB300.
+
+A step is one right-hand-side evaluation of the pseudo-fermion FRG flow:
+compute_dΣ! followed by compute_dΓ_2l! (the reference's src/Flow/flow_self.jl
+and src/Flow/compute.jl) on a seeded synthetic state of the pyrochlore
+lattice, L = 6, nearest-neighbour Heisenberg J1 = 1, SU(2), 50/15/10 positive
+frequencies, Λ = 1, vertex entries N(0, 0.05) plus the bare coupling on the
+Ω = 0 slice of the t-channel spin component.  The metric is right-hand-side
+evaluations per second of the mixed-precision GPU path; the FP64 GPU path,
+the mixed path's error against it and the CPU oracle are reported beside it.
+
+``--impl reference`` times the CPU restatement of the reference's algorithm
+(the reference is Julia, which is not installed on these machines) on all
+host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__ as entry  # noqa: E402
+
+METRIC = "full-flow s & dΓ evals/s, mixed vs FP64 GPU on 1 GB300 at ≤1e-6 rel χ err"
+UNIT = "dΓ evals/s"
+WORKLOAD = "pyrochlore-L6-2l"
+GAMMA_TOL = (1e-8, 1e-4)
+SIGMA_TOL = (1e-8, 1e-4)
+EVAL = 10  # eval at Λ = 1 with min_eval = 10 (launcher_1l.jl:78)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default=WORKLOAD)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
+    return p.parse_args()
+
+
+def config(args, w, extra=None):
+    c = {"workload": w.name, "lattice": w.lattice, "L": w.size, "model": w.model, "J": w.J, "symmetry": w.symmetry,
+         "loops": w.loops, "Lambda": w.Lam, "num_sigma": w.num_sigma, "num_omega": w.num_omega, "num_nu": w.num_nu,
+         "eval": EVAL, "gamma_tol": list(GAMMA_TOL), "sigma_tol": list(SIGMA_TOL), "noise": w.noise, "seed": w.seed,
+         "l2": "flushed between timed steps (256 MiB write); the vertex (5.3 MB) is L2-resident within a step",
+         "parallelism": f"replicas x{args.gpus}"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------------------
+# clocks (nvidia-smi sampled during the timed region)
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.file = tempfile.NamedTemporaryFile(prefix="clocks_", suffix=".csv", delete=False)
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        self.file.close()
+
+    def summary(self, busy_frac: float = 0.0):
+        rows = []
+        try:
+            with open(self.file.name) as fh:
+                for r in csv.reader(fh):
+                    if len(r) >= 9:
+                        rows.append([x.strip() for x in r])
+        except OSError:
+            pass
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """DRAM bytes per channel-task-kernel launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "pass_kernel_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except (OSError, ValueError):
+            return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (CPU restatement) on a strided sample of the channel tasks
+# ---------------------------------------------------------------------------
+def cpu_rhs_rate(O, r, m, a, w, target_s: float):
+    threads = os.cpu_count() or 1
+    # probe with a coarse stride, then pick the stride that fits the target time
+    stride = 64
+    P = O.Problem(r, m, num_threads=threads, task_stride=stride)
+    da = np.zeros_like(a.buf)
+    t0 = time.perf_counter()
+    O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
+    t_sigma = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.dgamma(P, w.loops, w.Lam, a.buf, da, EVAL, gtol=GAMMA_TOL)
+    t_probe = time.perf_counter() - t0
+    full_est = t_probe * stride
+    stride = int(max(1, min(64, np.ceil(full_est / max(target_s, 1e-3)))))
+    P = O.Problem(r, m, num_threads=threads, task_stride=stride)
+    da = np.zeros_like(a.buf)
+    O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
+    t0 = time.perf_counter()
+    st = O.dgamma(P, w.loops, w.Lam, a.buf, da, EVAL, gtol=GAMMA_TOL)
+    t_gamma = time.perf_counter() - t0
+    per_rhs = t_sigma + stride * t_gamma
+    return 1.0 / per_rhs, threads, stride, t_sigma + t_gamma, st
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    entry.load_package()
+    import pffrg_gb300.workloads as wl
+
+    O = entry.load_oracle()
+    w = wl.WORKLOADS[args.workload]
+    lat, r, m, a = wl.build_state(w)
+    threads = os.cpu_count() or 1
+    # one step = the oracle's right-hand side on a strided sample of the channel tasks,
+    # sized so that warm-up + timed steps end within a few minutes
+    per_step_target = max(2.0, 150.0 / max(1, args.steps + args.warmup))
+    rate, threads, stride, _, _ = cpu_rhs_rate(O, r, m, a, w, per_step_target)
+    P = O.Problem(r, m, num_threads=threads, task_stride=stride)
+    times = []
+    for k in range(args.warmup + args.steps):
+        da = np.zeros_like(a.buf)
+        t0 = time.perf_counter()
+        O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
+        ts = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.dgamma(P, w.loops, w.Lam, a.buf, da, EVAL, gtol=GAMMA_TOL)
+        tg = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(ts + stride * tg)
+    per = float(np.mean(times))
+    value = 1.0 / per
+    sample = (f"every {stride}-th channel task of each dΓ pass (dΣ in full), pass time scaled by {stride}; "
+              "CPU restatement of the reference algorithm (Julia is not installed)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(args, w), "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                                                        "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def ours(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    pkg = entry.load_package()
+    import pffrg_gb300._capi as C
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = wl.WORKLOADS[args.workload]
+    lat, r, m, a = wl.build_state(w)
+    lay = a.layout
+    action_bytes = lay.size * 8
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+
+    ctx = FlowContext(r, m, precision="mixed", device=local)
+    ctx.upload(C.SLOT_A, a)
+
+    def rhs():
+        ctx.rhs(w.Lam, EVAL, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
+
+    # warm-up
+    for _ in range(args.warmup):
+        rhs()
+    ctx.set_timing(True)
+    ctx.read_stats(reset=True)
+    barrier()
+    with ClockSampler(local) as clocks:
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            rhs()
+        barrier()
+        t_wall = time.perf_counter() - t_wall0
+    st = ctx.read_stats(reset=True)
+    ctx.set_timing(False)
+    ms_step = st["rhs_ms"] / args.steps
+    pass_ms_step = st["pass_ms"] / args.steps
+    launches_step = st["launches"] / args.steps
+    pass_launches_step = st["pass_launches"] / args.steps
+    evals_step = st["integrand_evals"]
+    alg_bytes_step = st["algorithmic_values"] * 4  # FP32 vertex values on the mixed path
+    t_max = ms_step
+    if dist:
+        tt = torch.tensor([ms_step], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * 1e3 / t_max
+
+    # mixed result for the error report
+    da_mixed = pkg.action.Action.empty_like(a)
+    ctx.download(C.SLOT_DA, da_mixed)
+
+    # FP64 comparator on the same state
+    ctx.set_precision("fp64")
+    rhs()
+    ctx.set_timing(True)
+    ctx.read_stats(reset=True)
+    for _ in range(args.fp64_steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        rhs()
+    st64 = ctx.read_stats(reset=True)
+    ctx.set_timing(False)
+    fp64_ms = st64["rhs_ms"] / max(1, args.fp64_steps)
+    da64 = pkg.action.Action.empty_like(a)
+    ctx.download(C.SLOT_DA, da64)
+    err_mixed = float(np.max(np.abs(da_mixed.buf - da64.buf)) / np.max(np.abs(da64.buf)))
+    ctx.set_precision("mixed")
+
+    # end to end through the reference-facing calls with host (pinned) buffers
+    lib = C.load()
+    nbytes = action_bytes
+    pa = lib.pffrg_host_alloc(nbytes)
+    pd = lib.pffrg_host_alloc(nbytes)
+    import ctypes
+
+    ha = np.frombuffer((ctypes.c_double * lay.size).from_address(pa), dtype=np.float64)
+    hd = np.frombuffer((ctypes.c_double * lay.size).from_address(pd), dtype=np.float64)
+    A_host = pkg.action.Action(a.symmetry, lay.num_sites, lay.num_sigma, lay.num_omega, lay.num_nu, a.S, ha)
+    D_host = pkg.action.Action(a.symmetry, lay.num_sites, lay.num_sigma, lay.num_omega, lay.num_nu, a.S, hd)
+    A_host.buf[:] = a.buf
+    for _ in range(1):
+        D_host.buf[:] = 0.0
+        ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
+        ctx.compute_dgamma(w.Lam, A_host, D_host, EVAL, GAMMA_TOL, loops=w.loops)
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        D_host.buf[:] = 0.0
+        t0 = time.perf_counter()
+        ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
+        ctx.compute_dgamma(w.Lam, A_host, D_host, EVAL, GAMMA_TOL, loops=w.loops)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_times))
+    if dist:
+        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e_value = world / e2e_s
+    h2d = 4 * action_bytes  # a and da uploaded by each of the two calls
+    d2h = 2 * action_bytes  # da returned by each call
+    lib.pffrg_host_free(pa)
+    lib.pffrg_host_free(pd)
+    ctx.close()
+
+    clk = clocks.summary()
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes_step / (pass_ms_step * 1e-3) / 1e9 if pass_ms_step > 0 else None
+    traffic = None
+    tr = ncu_traffic_per_launch()
+    if tr and tr.get("workload") == w.name and tr.get("precision") == "mixed":
+        traffic = tr.get("dram_bytes_per_launch")
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    # CPU baseline (oracle, all host cores, bounded strided sample), rank 0 at N=1 only
+    cpu = None
+    if world == 1:
+        O = entry.load_oracle()
+        rate, threads, stride, secs, _ = cpu_rhs_rate(O, r, m, a, w, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"every {stride}-th channel task of each dΓ pass (dΣ in full), pass time x{stride}; "
+                         f"{secs:.1f} s of CPU work; CPU restatement of the reference algorithm"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 integrand / f64 quadrature bookkeeping", "data": "synthetic",
+        "config": config(args, w, {"precision": "mixed", "wall_ms_per_step": t_wall * 1e3 / args.steps}),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(round(launches_step * args.steps)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "pass_kernel (channel tasks)", "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_step": alg_bytes_step, "kernel_ms_per_step": pass_ms_step,
+                     "launches_per_step": pass_launches_step},
+        "cpu_baseline": cpu,
+        "fp64": {"value": 1e3 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
+                 "mixed_speedup": fp64_ms / ms_step},
+        "mixed_vs_fp64_rel_err": err_mixed,
+        "integrand_evals_per_step": evals_step,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

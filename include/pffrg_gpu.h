@@ -149,6 +149,19 @@ int pffrg_accept(pffrg_ctx* ctx);
  * for throughput and algorithmic-byte accounting. */
 int64_t pffrg_last_integrand_evals(const pffrg_ctx* ctx);
 
+/* Work counters and optional CUDA-event timing (recorded on the context's stream). */
+typedef struct pffrg_stats {
+    int64_t integrand_evals;    /* bubble integrand evaluations of the last RHS / dΓ call */
+    int64_t algorithmic_values; /* vertex values those evaluations read (corners x sites x components,
+                                   bare and output values, t-channel overlap operands) */
+    double pass_ms;             /* summed duration of the channel-task kernels since the last reset */
+    double rhs_ms;              /* summed duration of pffrg_rhs calls since the last reset */
+    int64_t pass_launches;      /* channel-task kernel launches since the last reset */
+    int64_t launches;           /* all kernel launches since the last reset */
+} pffrg_stats;
+int pffrg_set_timing(pffrg_ctx* ctx, int on);
+int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset);
+
 /* Pinned host memory for fast copies (cudaHostAlloc); NULL on failure. */
 void* pffrg_host_alloc(int64_t bytes);
 void pffrg_host_free(void* p);

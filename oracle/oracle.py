@@ -38,6 +38,7 @@ class _Problem(ctypes.Structure):
         ("symmetry", ctypes.c_int32),
         ("S", ctypes.c_double),
         ("num_threads", ctypes.c_int32),
+        ("task_stride", ctypes.c_int32),
     ]
 
 
@@ -48,6 +49,7 @@ class Stats(ctypes.Structure):
         ("overlap_terms", ctypes.c_int64),
         ("sigma_evals", ctypes.c_int64),
         ("reevals", ctypes.c_int64),
+        ("level_hist", ctypes.c_int64 * 24),
     ]
 
 
@@ -114,7 +116,7 @@ def _opt(x):
 class Problem:
     """Lattice tables + meshes + model, kept alive for the oracle calls."""
 
-    def __init__(self, r, m, symmetry: str = "su2", S: float = 0.5, num_threads: int = 0):
+    def __init__(self, r, m, symmetry: str = "su2", S: float = 0.5, num_threads: int = 0, task_stride: int = 1):
         offs, rows = r.overlap_csr()
         self._keep = dict(
             exchange=np.ascontiguousarray(r.exchange, dtype=np.int64),
@@ -132,7 +134,7 @@ class Problem:
         self.s = _Problem(r.num_sites, ip(k["exchange"]), ip(k["mult"]), ip(k["offs"]), ip(k["rows"]),
                           m.num_sigma, m.num_omega, m.num_nu, _f(k["sigma"]), _f(k["omega_s"]),
                           _f(k["nu_s"]), _f(k["omega_t"]), _f(k["nu_t"]), 0 if symmetry == "su2" else 1,
-                          float(S), int(num_threads))
+                          float(S), int(num_threads), int(task_stride))
         self.ref = ctypes.byref(self.s)
 
     @property
@@ -143,7 +145,9 @@ class Problem:
 def stats() -> dict:
     st = Stats()
     lib().oracle_last_stats(ctypes.byref(st))
-    return {k: int(getattr(st, k)) for k, _ in Stats._fields_}
+    out = {k: int(getattr(st, k)) for k, _ in Stats._fields_ if k != "level_hist"}
+    out["level_hist"] = [int(x) for x in st.level_hist]
+    return out
 
 
 def _check(rc: int, what: str):

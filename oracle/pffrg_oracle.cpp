@@ -598,6 +598,9 @@ void simps(F& f, double* b1, double* b2, int len, double a, double b, double ato
         double rdiff = adiff / std::max(n1, n2);
         if (adiff < atol || rdiff < rtol || n > (int64_t(1) << 20)) {
             for (int i = 0; i < len; ++i) b1[i] += b2[i];
+            int lv = 0;
+            while ((int64_t(2) << lv) < n) ++lv;
+            g_stats.level_hist[lv < 23 ? lv : 23] += 1;
             break;
         }
         for (int i = 0; i < len; ++i) b1[i] = b2[i];
@@ -864,15 +867,17 @@ void run_pass(const Prob& P, const PassDesc base[3], double L, bool full, const 
     const oracle_stats saved = g_stats;
 #pragma omp parallel num_threads(nthreads(P))
     {
-        g_stats = oracle_stats{0, 0, 0, 0, 0};
+        g_stats = oracle_stats{};
         ThreadScratch ts;
         const int len = d.C * d.Ns;
         ts.tb1.resize(len);
         ts.tb2.resize(len);
         ts.tb3.resize(len);
         ts.temp.resize(2 * len);
+        const int64_t stride = P.p->task_stride > 1 ? P.p->task_stride : 1;
 #pragma omp for schedule(dynamic, 1)
         for (int64_t j = 0; j < nt; ++j) {
+            if (j % stride) continue;
             const Task& t = tasks[j / 3];
             run_task(P, base[j % 3], L, t, corrs, eval, atol, rtol, out, ts);
         }
@@ -882,6 +887,7 @@ void run_pass(const Prob& P, const PassDesc base[3], double L, bool full, const 
             total.gathered_values += g_stats.gathered_values;
             total.overlap_terms += g_stats.overlap_terms;
             total.reevals += g_stats.reevals;
+            for (int k = 0; k < 24; ++k) total.level_hist[k] += g_stats.level_hist[k];
         }
     }
     g_stats = saved;
@@ -889,6 +895,7 @@ void run_pass(const Prob& P, const PassDesc base[3], double L, bool full, const 
     g_stats.gathered_values += total.gathered_values;
     g_stats.overlap_terms += total.overlap_terms;
     g_stats.reevals += total.reevals;
+    for (int k = 0; k < 24; ++k) g_stats.level_hist[k] += total.level_hist[k];
 }
 
 // symmetrize! (action_su2.jl:141-173)
@@ -1083,7 +1090,7 @@ void sigma_integrals(const Prob& P, SigmaKind kind, double L, const double* a, c
     g_stats.sigma_evals += evals;
 }
 
-void reset_stats() { g_stats = oracle_stats{0, 0, 0, 0, 0}; }
+void reset_stats() { g_stats = oracle_stats{}; }
 
 }  // namespace
 

@@ -44,6 +44,7 @@ typedef struct oracle_problem {
     int32_t symmetry; /* 0 = su2 */
     double S;
     int32_t num_threads; /* <= 0: all available */
+    int32_t task_stride; /* > 1: run only every task_stride-th channel task of a pass (timing samples) */
 } oracle_problem;
 
 /* statistics of the last call on this thread */
@@ -53,6 +54,7 @@ typedef struct oracle_stats {
     int64_t overlap_terms;    /* t-channel overlap products */
     int64_t sigma_evals;      /* self-energy kernel evaluations */
     int64_t reevals;          /* integrand evaluations of residual! at nodes evaluated before */
+    int64_t level_hist[24];   /* Simpson subdomains by final refinement level (n = 2^level new nodes) */
 } oracle_stats;
 
 int64_t oracle_action_size(const oracle_problem* p);

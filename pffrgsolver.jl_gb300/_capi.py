@@ -26,8 +26,14 @@ EXPORTED = [
     "pffrg_create", "pffrg_destroy", "pffrg_last_error", "pffrg_set_mesh", "pffrg_set_precision",
     "pffrg_dsigma", "pffrg_dgamma", "pffrg_sde", "pffrg_bse", "pffrg_action_size", "pffrg_upload",
     "pffrg_download", "pffrg_rhs", "pffrg_bs_step", "pffrg_accept", "pffrg_last_integrand_evals",
-    "pffrg_host_alloc", "pffrg_host_free",
+    "pffrg_host_alloc", "pffrg_host_free", "pffrg_set_timing", "pffrg_read_stats",
 ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("integrand_evals", ctypes.c_int64), ("algorithmic_values", ctypes.c_int64),
+                ("pass_ms", ctypes.c_double), ("rhs_ms", ctypes.c_double), ("pass_launches", ctypes.c_int64),
+                ("launches", ctypes.c_int64)]
 
 
 class LatticeView(ctypes.Structure):
@@ -89,6 +95,8 @@ def load():
     L.pffrg_host_alloc.argtypes = [ctypes.c_int64]
     L.pffrg_host_alloc.restype = vp
     L.pffrg_host_free.argtypes = [vp]
+    L.pffrg_set_timing.argtypes = [vp, ctypes.c_int]
+    L.pffrg_read_stats.argtypes = [vp, ctypes.POINTER(Stats), ctypes.c_int]
     _lib = L
     return L
 

@@ -53,6 +53,14 @@ struct pffrg_ctx {
     int4* tasks_red = nullptr;
     int n_sym = 0, n_full = 0, n_red = 0;
     int64_t last_evals = 0;
+    int64_t last_alg_values = 0;
+    // optional CUDA-event timing of the pass kernels and of whole right-hand sides
+    int timing = 0;
+    std::vector<cudaEvent_t> ev;  // pairs (start, stop) of the pass launches since the last reset
+    int ev_used = 0;
+    cudaEvent_t rhs_ev[2] = {nullptr, nullptr};
+    double pass_ms = 0.0, rhs_ms = 0.0;
+    int64_t pass_launches = 0, launches = 0;
     std::string err;
 
     int fail(int code, const char* fmt, ...) {
@@ -189,6 +197,38 @@ int copy_view(pffrg_ctx* ctx, double* dev, const pffrg_action_view* v, bool to_d
     return 0;
 }
 
+// pass launch, bracketed by CUDA events on the context's stream when timing is on
+template <typename R>
+cudaError_t run_pass(pffrg_ctx* ctx, const PassArgs<R>& p) {
+    ++ctx->launches;
+    ++ctx->pass_launches;
+    if (!ctx->timing) return launch_pass<R>(p, ctx->st);
+    while ((int)ctx->ev.size() < 2 * (ctx->ev_used + 1)) {
+        cudaEvent_t e;
+        cudaError_t er = cudaEventCreate(&e);
+        if (er != cudaSuccess) return er;
+        ctx->ev.push_back(e);
+    }
+    cudaEvent_t e0 = ctx->ev[2 * ctx->ev_used], e1 = ctx->ev[2 * ctx->ev_used + 1];
+    ++ctx->ev_used;
+    cudaError_t er = cudaEventRecord(e0, ctx->st);
+    if (er != cudaSuccess) return er;
+    er = launch_pass<R>(p, ctx->st);
+    if (er != cudaSuccess) return er;
+    return cudaEventRecord(e1, ctx->st);
+}
+
+// accumulate the recorded pass durations (stream already synchronised)
+int collect_pass_times(pffrg_ctx* ctx) {
+    for (int k = 0; k < ctx->ev_used; ++k) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->ev[2 * k], ctx->ev[2 * k + 1]));
+        ctx->pass_ms += ms;
+    }
+    ctx->ev_used = 0;
+    return 0;
+}
+
 template <typename R>
 PassArgs<R> base_pass(pffrg_ctx* ctx, double Lam, int eval, double atol, double rtol) {
     PassArgs<R> p;
@@ -274,6 +314,7 @@ int corrs_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* da, dou
     c.rtol = rtol;
     c.corrs = out;
     c.status = ctx->status;
+    ++ctx->launches;
     CK(launch_corrs<R>(c, ctx->st));
     return 0;
 }
@@ -295,11 +336,13 @@ int sigma_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* aux, do
     s.rtol = rtol;
     s.twoS = 2.0 * ctx->S;
     s.status = ctx->status;
+    ++ctx->launches;
     CK(launch_sigma<R>(s, ctx->st));
     return 0;
 }
 
 int to_f(pffrg_ctx* ctx, const double* x, float* y) {
+    ++ctx->launches;
     CK(launch_to_float(x, y, ctx->L.total, ctx->st));
     return 0;
 }
@@ -347,7 +390,7 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
         s.dal = (const R*)ctx->f_dal;
         s.dtemp = (const R*)ctx->f_dtemp;
     }
-    CK(cudaMemsetAsync(ctx->counter, 0, sizeof(unsigned long long), ctx->st));
+    CK(cudaMemsetAsync(ctx->counter, 0, 2 * sizeof(unsigned long long), ctx->st));
     if (int rc = upload_log_bounds(ctx, Lam, eval)) return rc;
     // 1 loop (compute.jl:57-112)
     if (int rc = corrs_run<R>(ctx, PROP_KAT, Lam, s.a, s.da, gatol, grtol, ctx->corrs)) return rc;
@@ -359,8 +402,8 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
         p.prop_a = s.a;
         p.prop_da = s.da;
         p.out = da;
-        CK(launch_pass<R>(p, ctx->st));
-        CK(launch_symmetrize(L, ctx->lat.exch, da, ctx->st));
+        CK(run_pass<R>(ctx, p));
+        CK((++ctx->launches, launch_symmetrize)(L, ctx->lat.exch, da, ctx->st));
     }
     if (loops >= 2) {
         // 2 loop (compute.jl:115-174)
@@ -375,14 +418,14 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
         p.prop_a = s.a;
         p.prop_da = s.a;
         p.out = ctx->da_l;
-        CK(launch_pass<R>(p, ctx->st));
-        CK(launch_symmetrize_add_to(L, ctx->lat.exch, ctx->da_l, da, ctx->st));
+        CK(run_pass<R>(ctx, p));
+        CK((++ctx->launches, launch_symmetrize_add_to)(L, ctx->lat.exch, ctx->da_l, da, ctx->st));
     }
     if (loops >= 3) {
         // multiloop (compute.jl:177-287)
-        CK(launch_axpby(L, 0.0, nullptr, 0.0, ctx->da_temp, false, true, ctx->st));
-        CK(launch_axpby(L, 0.0, nullptr, 0.0, ctx->da_sig, false, true, ctx->st));
-        CK(launch_symmetrize_add_to(L, ctx->lat.exch, ctx->da_l, ctx->da_temp, ctx->st));
+        CK((++ctx->launches, launch_axpby)(L, 0.0, nullptr, 0.0, ctx->da_temp, false, true, ctx->st));
+        CK((++ctx->launches, launch_axpby)(L, 0.0, nullptr, 0.0, ctx->da_sig, false, true, ctx->st));
+        CK((++ctx->launches, launch_symmetrize_add_to)(L, ctx->lat.exch, ctx->da_l, ctx->da_temp, ctx->st));
         for (int loop = 3; loop <= loops; ++loop) {
             if constexpr (sizeof(R) == 4) {
                 if (int rc = to_f(ctx, ctx->da_l, ctx->f_dal)) return rc;
@@ -397,7 +440,7 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
                 p.prop_da = s.a;
                 p.out = ctx->da_c;
                 set_slots<R>(p, s.a, s.dal, s.a, s.dal, kMaskCentral);
-                CK(launch_pass<R>(p, ctx->st));
+                CK(run_pass<R>(ctx, p));
             }
             {
                 PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
@@ -407,13 +450,13 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
                 p.prop_da = s.a;
                 p.out = ctx->da_l;
                 set_slots<R>(p, s.dtemp, s.a, s.dtemp, s.a, kMaskLeft);
-                CK(launch_pass<R>(p, ctx->st));
+                CK(run_pass<R>(ctx, p));
             }
-            CK(launch_symmetrize(L, ctx->lat.exch, ctx->da_c, ctx->st));
+            CK((++ctx->launches, launch_symmetrize)(L, ctx->lat.exch, ctx->da_c, ctx->st));
             CK(cudaMemcpyAsync(ctx->da_temp, ctx->da_c, sizeof(double) * L.total, cudaMemcpyDeviceToDevice, ctx->st));
-            CK(launch_symmetrize_add_to(L, ctx->lat.exch, ctx->da_l, ctx->da_temp, ctx->st));
-            CK(launch_axpby(L, 1.0, ctx->da_c, 1.0, ctx->da_sig, false, true, ctx->st));
-            CK(launch_axpby(L, 1.0, ctx->da_temp, 1.0, da, false, true, ctx->st));
+            CK((++ctx->launches, launch_symmetrize_add_to)(L, ctx->lat.exch, ctx->da_l, ctx->da_temp, ctx->st));
+            CK((++ctx->launches, launch_axpby)(L, 1.0, ctx->da_c, 1.0, ctx->da_sig, false, true, ctx->st));
+            CK((++ctx->launches, launch_axpby)(L, 1.0, ctx->da_temp, 1.0, da, false, true, ctx->st));
         }
         if (sigma_corr) {
             // compute_dΣ_corr! (flow_self.jl:23-51)
@@ -431,8 +474,8 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
             CK(cudaMemsetAsync(ctx->sig_tmp, 0, sizeof(double) * L.Nsig, ctx->st));
             if (int rc = sigma_run<R>(ctx, SIG_CORR2, Lam, s.a, sig_src, ctx->sig_tmp, satol, srtol)) return rc;
             // da.Σ += da_Σ.Σ + corr2 (index 0 included: both are zero there)
-            CK(launch_axpby(L, 1.0, ctx->da_sig, 1.0, da, true, false, ctx->st));
-            CK(launch_axpby(L, 1.0, ctx->sig_tmp, 1.0, da, true, false, ctx->st));
+            CK((++ctx->launches, launch_axpby)(L, 1.0, ctx->da_sig, 1.0, da, true, false, ctx->st));
+            CK((++ctx->launches, launch_axpby)(L, 1.0, ctx->sig_tmp, 1.0, da, true, false, ctx->st));
         }
     }
     return 0;
@@ -452,14 +495,16 @@ int rhs_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* da, 
 }
 
 int read_evals(pffrg_ctx* ctx) {
-    unsigned long long h = 0;
-    CK(cudaMemcpyAsync(&h, ctx->counter, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
+    unsigned long long h[2] = {0, 0};
+    CK(cudaMemcpyAsync(h, ctx->counter, sizeof(h), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
-    ctx->last_evals = (int64_t)h;
-    return 0;
+    ctx->last_evals = (int64_t)h[0];
+    ctx->last_alg_values = (int64_t)h[1];
+    return collect_pass_times(ctx);
 }
 
 int absmax(pffrg_ctx* ctx, const double* a, double* dst) {
+    ctx->launches += 2;
     CK(launch_absmax_q3(ctx->L, a, ctx->partial, kPartials, dst, ctx->st));
     return 0;
 }
@@ -474,6 +519,27 @@ int64_t pffrg_action_size(const pffrg_ctx* ctx) { return ctx ? ctx->L.total : 0;
 
 int64_t pffrg_last_integrand_evals(const pffrg_ctx* ctx) { return ctx ? ctx->last_evals : 0; }
 
+int pffrg_set_timing(pffrg_ctx* ctx, int on) {
+    if (!ctx) return PFFRG_E_ARGS;
+    ctx->timing = on ? 1 : 0;
+    return 0;
+}
+
+int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset) {
+    if (!ctx || !out) return PFFRG_E_ARGS;
+    out->integrand_evals = ctx->last_evals;
+    out->algorithmic_values = ctx->last_alg_values;
+    out->pass_ms = ctx->pass_ms;
+    out->rhs_ms = ctx->rhs_ms;
+    out->pass_launches = ctx->pass_launches;
+    out->launches = ctx->launches;
+    if (reset) {
+        ctx->pass_ms = ctx->rhs_ms = 0.0;
+        ctx->pass_launches = ctx->launches = 0;
+    }
+    return 0;
+}
+
 void pffrg_destroy(pffrg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
@@ -487,6 +553,9 @@ void pffrg_destroy(pffrg_ctx* ctx) {
     for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
         if (ctx->slot[k]) cudaFree(ctx->slot[k]);
     if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
+    for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->rhs_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
 }
@@ -574,7 +643,7 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
          dalloc((void**)&ctx->corrs_sde, sizeof(double) * 6 * L.NO) &&
          dalloc((void**)&ctx->partial, sizeof(double) * kPartials) &&
          dalloc((void**)&ctx->scalars, sizeof(double) * 4) && dalloc((void**)&ctx->status, sizeof(int)) &&
-         dalloc((void**)&ctx->counter, sizeof(unsigned long long));
+         dalloc((void**)&ctx->counter, 2 * sizeof(unsigned long long));
     if (!ok) return bail("device allocation failed");
     if (cudaHostAlloc((void**)&ctx->h_scalars, sizeof(double) * 4, cudaHostAllocDefault) != cudaSuccess)
         return bail("pinned allocation failed");
@@ -682,11 +751,23 @@ int pffrg_rhs(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, in
         return ctx->fail(PFFRG_E_ARGS, "bad slots");
     if (loops < 1 || eval < 1) return ctx->fail(PFFRG_E_ARGS, "loops and eval must be positive");
     CK(cudaSetDevice(ctx->device));
+    if (ctx->timing) {
+        for (auto& e : ctx->rhs_ev)
+            if (!e) CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(ctx->rhs_ev[0], ctx->st));
+    }
     int rc = rhs_dev(ctx, loops, Lam, ctx->slot[a_slot], ctx->slot[da_slot], eval, gatol, grtol, satol, srtol,
                      sigma_corr);
     if (rc) return rc;
+    if (ctx->timing) CK(cudaEventRecord(ctx->rhs_ev[1], ctx->st));
     if ((rc = check_status(ctx))) return rc;
-    return read_evals(ctx);
+    if ((rc = read_evals(ctx))) return rc;
+    if (ctx->timing) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->rhs_ev[0], ctx->rhs_ev[1]));
+        ctx->rhs_ms += ms;
+    }
+    return 0;
 }
 
 int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
@@ -723,7 +804,7 @@ int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
         p.prop_a = r1;
         p.prop_da = r1;
         p.out = d2;
-        CK(launch_pass<R>(p, ctx->st));
+        CK(run_pass<R>(ctx, p));
         if constexpr (sizeof(R) == 4) {
             if (int rc = to_f(ctx, d2, ctx->f_da)) return rc;
         }
@@ -764,8 +845,8 @@ int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
         p.prop_da = r1;
         p.out = d2;
         set_slots<R>(p, r1, r1, r1, r1, kMaskLeft);
-        CK(launch_pass<R>(p, ctx->st));
-        CK(launch_symmetrize(ctx->L, ctx->lat.exch, d2, ctx->st));
+        CK(run_pass<R>(ctx, p));
+        CK((++ctx->launches, launch_symmetrize)(ctx->L, ctx->lat.exch, d2, ctx->st));
         return 0;
     };
     int rc = ctx->precision == PFFRG_FP64 ? run(double{}) : run(float{});
@@ -797,29 +878,29 @@ int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, 
     if (int rc = rhs(Lam, A)) return rc;
     if (int rc = read_evals(ctx)) return rc;
     evals += ctx->last_evals;
-    CK(launch_axpby(L, 1.0, K, -2.0 * dLam / 9.0, N, true, true, ctx->st));
-    CK(launch_axpby(L, 1.0, K, -7.0 * dLam / 24.0, E, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -2.0 * dLam / 9.0, N, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -7.0 * dLam / 24.0, E, true, true, ctx->st));
     CK(cudaMemcpyAsync(I, A, bytes, cudaMemcpyDeviceToDevice, ctx->st));
-    CK(launch_axpby(L, 1.0, K, -0.5 * dLam, I, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -0.5 * dLam, I, true, true, ctx->st));
     if (int rc = rhs(Lam - 0.5 * dLam, I)) return rc;
     if (int rc = read_evals(ctx)) return rc;
     evals += ctx->last_evals;
-    CK(launch_axpby(L, 1.0, K, -1.0 * dLam / 3.0, N, true, true, ctx->st));
-    CK(launch_axpby(L, 1.0, K, -1.0 * dLam / 4.0, E, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -1.0 * dLam / 3.0, N, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -1.0 * dLam / 4.0, E, true, true, ctx->st));
     CK(cudaMemcpyAsync(I, A, bytes, cudaMemcpyDeviceToDevice, ctx->st));
-    CK(launch_axpby(L, 1.0, K, -0.75 * dLam, I, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -0.75 * dLam, I, true, true, ctx->st));
     if (int rc = rhs(Lam - 0.75 * dLam, I)) return rc;
     if (int rc = read_evals(ctx)) return rc;
     evals += ctx->last_evals;
-    CK(launch_axpby(L, 1.0, K, -4.0 * dLam / 9.0, N, true, true, ctx->st));
-    CK(launch_axpby(L, 1.0, K, -1.0 * dLam / 3.0, E, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -4.0 * dLam / 9.0, N, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -1.0 * dLam / 3.0, E, true, true, ctx->st));
     CK(cudaMemcpyAsync(I, N, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     if (int rc = rhs(Lam - dLam, I)) return rc;
     if (int rc = read_evals(ctx)) return rc;
     evals += ctx->last_evals;
-    CK(launch_axpby(L, 1.0, K, -1.0 * dLam / 8.0, E, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, K, -1.0 * dLam / 8.0, E, true, true, ctx->st));
     // subtract_from!(a_inter, a_err) and the error ratio (launcher_1l.jl:112-116)
-    CK(launch_axpby(L, 1.0, I, -1.0, E, true, true, ctx->st));
+    CK((++ctx->launches, launch_axpby)(L, 1.0, I, -1.0, E, true, true, ctx->st));
     if (int rc = absmax(ctx, E, ctx->scalars + 0)) return rc;
     if (int rc = absmax(ctx, I, ctx->scalars + 1)) return rc;
     if (int rc = absmax(ctx, A, ctx->scalars + 2)) return rc;

@@ -154,6 +154,7 @@ struct Warp {
     R W, V, VP;
     int nprop;
     unsigned long long nodes;  // integrand evaluations of this team
+    unsigned long long alg;    // algorithmic vertex values of these evaluations (lane 0 of the team)
 
     // Evaluate the integrand at node x for this team's sites: g[c][k] = Γ_c(site tl + k*T).
     // Team-collective; inactive teams take part in the warp syncs only.
@@ -183,6 +184,16 @@ struct Warp {
             }
         }
         __syncwarp();
+        if (A.node_counter && active && tl == 0) {
+            // corner reads of the two site slots on all sites and of the t-channel local
+            // slots at one site, bare (2 Ns) and output (Ns) values, t-channel overlap operands
+            unsigned long long cs = 0, c1 = 0;
+            for (int s = 0; s < nslots; ++s)
+                for (int ch = 0; ch < 3; ++ch) (s < 2 ? cs : c1) += corners_of(ts.plan[s][ch].kernel);
+            unsigned long long v = cs * Ns + c1 + 3ull * Ns;
+            if (X == 1) v += 2ull * ldg(A.ov_off + Ns);
+            alg += v * kC;
+        }
         R p = (R)0;
         if (active) p = (nprop == 2) ? ts.p_half[0] + ts.p_half[1] : ts.p_half[0];
         if (X != 1) {
@@ -280,7 +291,7 @@ __global__ void __launch_bounds__(kWarps * 32) pass_kernel(PassArgs<R> A) {
     const R VP = (kernel == 3 || kernel == 4) ? nu[task.w] : inf;
 
     Warp<R, T, SPL> wp{A, M, teams[warp * NPW + team], tmp_all + (size_t)(warp * NPW + team) * 4 * Ns, X, tl, W, V,
-                       VP, A.prop_kind == PROP_KAT ? 2 : 1, 0};
+                       VP, A.prop_kind == PROP_KAT ? 2 : 1, 0, 0};
 
     // integration ranges (flow_s.jl:29-38): ref = Λ + w/2, val = Ω[end] + ν[end], computed in FP64
     const double W64 = Om64[task.y];
@@ -436,7 +447,10 @@ __global__ void __launch_bounds__(kWarps * 32) pass_kernel(PassArgs<R> A) {
         }
     }
 
-    if (A.node_counter && tl == 0 && wp.nodes) atomicAdd(A.node_counter, wp.nodes);
+    if (A.node_counter && tl == 0 && wp.nodes) {
+        atomicAdd(A.node_counter, wp.nodes);
+        atomicAdd(A.node_counter + 1, wp.alg);
+    }
     // every team holds the full per-site sums: team 0 hands them to the CTA reduction
     if (team == 0) {
 #pragma unroll

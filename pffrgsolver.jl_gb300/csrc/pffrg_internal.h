@@ -47,7 +47,7 @@ struct PassArgs {
     double Lam, atol, rtol;
     int eval;
     double twoS;
-    unsigned long long* node_counter;  // optional: integrand evaluations
+    unsigned long long* node_counter;  // optional: [0] integrand evaluations, [1] algorithmic values read
 };
 
 template <typename R>

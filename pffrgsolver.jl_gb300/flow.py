@@ -78,6 +78,14 @@ class FlowContext:
     def last_integrand_evals(self) -> int:
         return int(self.lib.pffrg_last_integrand_evals(self.h))
 
+    def set_timing(self, on: bool) -> None:
+        self._check(self.lib.pffrg_set_timing(self.h, int(on)), "set_timing")
+
+    def read_stats(self, reset: bool = False) -> dict:
+        st = _capi.Stats()
+        self._check(self.lib.pffrg_read_stats(self.h, ctypes.byref(st), int(reset)), "read_stats")
+        return {k: getattr(st, k) for k, _ in _capi.Stats._fields_}
+
     # ---- reference-facing calls (host arrays in, host arrays out) ----
     def compute_dsigma(self, Lam: float, a: Action, da: Action, sigma_tol=(1e-8, 1e-4)) -> None:
         av, dv = _capi.action_view(a), _capi.action_view(da)
