@@ -48,6 +48,12 @@ struct pffrg_ctx {
     double* h_scalars = nullptr;   // pinned [4]
     int* status = nullptr;
     unsigned long long* counter = nullptr;
+    // wave workspace of the passes (device scratch) and its host-visible counters
+    void* wave_mem = nullptr;
+    size_t wave_bytes = 0;
+    long long wave_nsub = 0, wave_qcap = 0;
+    int* h_wave_counters = nullptr;  // pinned [8]
+    int queue_overflow = 0;
     int4* tasks_sym = nullptr;
     int4* tasks_full = nullptr;
     int4* tasks_red = nullptr;
@@ -73,6 +79,19 @@ struct pffrg_ctx {
         return code;
     }
 };
+
+#define CK_PASS(call)                                                                                     \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) {                                                                          \
+            if (ctx->queue_overflow) {                                                                    \
+                ctx->queue_overflow = 0;                                                                  \
+                return ctx->fail(PFFRG_E_LIMIT, "quadrature chunk queue capacity exceeded");              \
+            }                                                                                             \
+            return ctx->fail(PFFRG_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                             __LINE__);                                                                   \
+        }                                                                                                 \
+    } while (0)
 
 #define CK(call)                                                                                          \
     do {                                                                                                  \
@@ -197,12 +216,44 @@ int copy_view(pffrg_ctx* ctx, double* dev, const pffrg_action_view* v, bool to_d
     return 0;
 }
 
+// make sure the wave workspace holds a pass of ntasks x nchan tasks at this eval
+cudaError_t ensure_wave_space(pffrg_ctx* ctx, long long nsub) {
+    const long long qcap = 8 * nsub + 65536;
+    if (nsub <= ctx->wave_nsub && ctx->wave_mem) return cudaSuccess;
+    if (ctx->wave_mem) {
+        cudaError_t e = cudaFree(ctx->wave_mem);
+        if (e != cudaSuccess) return e;
+        ctx->wave_mem = nullptr;
+    }
+    const size_t bytes = wave_space_bytes(nsub, ctx->L.Ns, qcap);
+    cudaError_t e = cudaMalloc(&ctx->wave_mem, bytes);
+    if (e != cudaSuccess) return e;
+    ctx->wave_bytes = bytes;
+    ctx->wave_nsub = nsub;
+    ctx->wave_qcap = qcap;
+    return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t launch_waves(pffrg_ctx* ctx, const PassArgs<R>& p) {
+    const long long nsub = (long long)p.ntasks * p.nchan * (4 * p.eval + 1);
+    cudaError_t e = ensure_wave_space(ctx, nsub);
+    if (e != cudaSuccess) return e;
+    WaveSpace W;
+    wave_space_carve(W, ctx->wave_mem, nsub, ctx->L.Ns, ctx->wave_qcap);
+    // this pass uses its own subdomain count; the queues keep the allocated capacity
+    W.nsub = (int)nsub;
+    e = launch_pass<R>(p, W, ctx->h_wave_counters, ctx->st);
+    if (e == cudaErrorLaunchOutOfResources && ctx->h_wave_counters[4]) ctx->queue_overflow = 1;
+    return e;
+}
+
 // pass launch, bracketed by CUDA events on the context's stream when timing is on
 template <typename R>
 cudaError_t run_pass(pffrg_ctx* ctx, const PassArgs<R>& p) {
     ++ctx->launches;
     ++ctx->pass_launches;
-    if (!ctx->timing) return launch_pass<R>(p, ctx->st);
+    if (!ctx->timing) return launch_waves<R>(ctx, p);
     while ((int)ctx->ev.size() < 2 * (ctx->ev_used + 1)) {
         cudaEvent_t e;
         cudaError_t er = cudaEventCreate(&e);
@@ -213,7 +264,7 @@ cudaError_t run_pass(pffrg_ctx* ctx, const PassArgs<R>& p) {
     ++ctx->ev_used;
     cudaError_t er = cudaEventRecord(e0, ctx->st);
     if (er != cudaSuccess) return er;
-    er = launch_pass<R>(p, ctx->st);
+    er = launch_waves<R>(ctx, p);
     if (er != cudaSuccess) return er;
     return cudaEventRecord(e1, ctx->st);
 }
@@ -236,9 +287,9 @@ PassArgs<R> base_pass(pffrg_ctx* ctx, double Lam, int eval, double atol, double 
     p.L = ctx->L;
     p.exch = ctx->lat.exch;
     p.ov_off = ctx->lat.ov_off;
-    p.ov_ab = ctx->lat.ov_ab;
-    if constexpr (sizeof(R) == 8) p.ov_m = (const R*)ctx->lat.ov_m;
-    else p.ov_m = (const R*)ctx->lat.ov_mf;
+    p.ov_rows = ctx->lat.ov_rows;
+    p.rows_total = ctx->lat.rows;
+    p.rows_in_smem = 0;
     p.mesh = ctx->mesh;
     p.log_bounds = ctx->log_bounds;
     p.corrs = ctx->corrs;
@@ -402,7 +453,7 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
         p.prop_a = s.a;
         p.prop_da = s.da;
         p.out = da;
-        CK(run_pass<R>(ctx, p));
+        CK_PASS(run_pass<R>(ctx, p));
         CK((++ctx->launches, launch_symmetrize)(L, ctx->lat.exch, da, ctx->st));
     }
     if (loops >= 2) {
@@ -418,7 +469,7 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
         p.prop_a = s.a;
         p.prop_da = s.a;
         p.out = ctx->da_l;
-        CK(run_pass<R>(ctx, p));
+        CK_PASS(run_pass<R>(ctx, p));
         CK((++ctx->launches, launch_symmetrize_add_to)(L, ctx->lat.exch, ctx->da_l, da, ctx->st));
     }
     if (loops >= 3) {
@@ -440,7 +491,7 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
                 p.prop_da = s.a;
                 p.out = ctx->da_c;
                 set_slots<R>(p, s.a, s.dal, s.a, s.dal, kMaskCentral);
-                CK(run_pass<R>(ctx, p));
+                CK_PASS(run_pass<R>(ctx, p));
             }
             {
                 PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
@@ -450,7 +501,7 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
                 p.prop_da = s.a;
                 p.out = ctx->da_l;
                 set_slots<R>(p, s.dtemp, s.a, s.dtemp, s.a, kMaskLeft);
-                CK(run_pass<R>(ctx, p));
+                CK_PASS(run_pass<R>(ctx, p));
             }
             CK((++ctx->launches, launch_symmetrize)(L, ctx->lat.exch, ctx->da_c, ctx->st));
             CK(cudaMemcpyAsync(ctx->da_temp, ctx->da_c, sizeof(double) * L.total, cudaMemcpyDeviceToDevice, ctx->st));
@@ -544,7 +595,7 @@ void pffrg_destroy(pffrg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
-    void* ptrs[] = {ctx->lat.exch, ctx->lat.mult, ctx->lat.ov_off, ctx->lat.ov_ab, ctx->lat.ov_m, ctx->lat.ov_mf,
+    void* ptrs[] = {ctx->lat.exch, ctx->lat.mult, ctx->lat.ov_off, ctx->lat.ov_rows, ctx->wave_mem,
                     ctx->mesh, ctx->log_bounds, ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig, ctx->sig_tmp, ctx->f_a, ctx->f_da,
                     ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
                     ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red};
@@ -553,6 +604,7 @@ void pffrg_destroy(pffrg_ctx* ctx) {
     for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
         if (ctx->slot[k]) cudaFree(ctx->slot[k]);
     if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
+    if (ctx->h_wave_counters) cudaFreeHost(ctx->h_wave_counters);
     for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->rhs_ev)
         if (e) cudaEventDestroy(e);
@@ -611,24 +663,22 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
     }
     for (int i = 0; i <= Ns; ++i) off[i] = (int)lat->overlap_offsets[i];
     const int64_t R = off[Ns];
-    std::vector<int> ab(R > 0 ? R : 1);
-    std::vector<double> m64(R > 0 ? R : 1);
-    std::vector<float> m32(R > 0 ? R : 1);
+    std::vector<unsigned> rows(R > 0 ? R : 1);
     for (int64_t j = 0; j < R; ++j) {
-        const int a = (int)lat->overlap_rows[3 * j] - 1, b = (int)lat->overlap_rows[3 * j + 1] - 1;
+        const int64_t a = lat->overlap_rows[3 * j] - 1, b = lat->overlap_rows[3 * j + 1] - 1;
+        const int64_t mm = lat->overlap_rows[3 * j + 2];
         if (a < 0 || a >= Ns || b < 0 || b >= Ns) return bail("overlap table out of range");
-        ab[j] = a | (b << 16);
-        m64[j] = (double)lat->overlap_rows[3 * j + 2];
-        m32[j] = (float)m64[j];
+        if (mm < 0 || mm >= 65536) return bail("overlap multiplicity out of range");
+        rows[j] = (unsigned)a | ((unsigned)b << 8) | ((unsigned)mm << 16);
     }
+    for (int i = 0; i < Ns; ++i)
+        if (off[i] > off[i + 1] || off[i] < 0) return bail("overlap offsets not increasing");
     ctx->lat.Ns = Ns;
     ctx->lat.rows = R;
     auto dalloc = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes > 0 ? bytes : 8) == cudaSuccess; };
     bool ok = dalloc((void**)&ctx->lat.exch, sizeof(int) * Ns) && dalloc((void**)&ctx->lat.mult, sizeof(int) * Ns) &&
               dalloc((void**)&ctx->lat.ov_off, sizeof(int) * (Ns + 1)) &&
-              dalloc((void**)&ctx->lat.ov_ab, sizeof(int) * ab.size()) &&
-              dalloc((void**)&ctx->lat.ov_m, sizeof(double) * m64.size()) &&
-              dalloc((void**)&ctx->lat.ov_mf, sizeof(float) * m32.size()) &&
+              dalloc((void**)&ctx->lat.ov_rows, sizeof(unsigned) * rows.size()) &&
               dalloc((void**)&ctx->mesh, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn));
     for (int k = 0; k < PFFRG_NUM_SLOTS && ok; ++k) ok = dalloc((void**)&ctx->slot[k], sizeof(double) * L.total);
     ok = ok && dalloc((void**)&ctx->da_l, sizeof(double) * L.total) &&
@@ -645,7 +695,8 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
          dalloc((void**)&ctx->scalars, sizeof(double) * 4) && dalloc((void**)&ctx->status, sizeof(int)) &&
          dalloc((void**)&ctx->counter, 2 * sizeof(unsigned long long));
     if (!ok) return bail("device allocation failed");
-    if (cudaHostAlloc((void**)&ctx->h_scalars, sizeof(double) * 4, cudaHostAllocDefault) != cudaSuccess)
+    if (cudaHostAlloc((void**)&ctx->h_scalars, sizeof(double) * 4, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc((void**)&ctx->h_wave_counters, sizeof(int) * 8, cudaHostAllocDefault) != cudaSuccess)
         return bail("pinned allocation failed");
     std::vector<int4> ts = make_tasks(L.NO, L.Nn, 0), tf = make_tasks(L.NO, L.Nn, 1), tr = make_tasks(L.NO, L.Nn, 2);
     ctx->n_sym = (int)ts.size();
@@ -659,9 +710,7 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
     bool cp = cudaMemcpyAsync(ctx->lat.exch, exch.data(), sizeof(int) * Ns, cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemcpyAsync(ctx->lat.mult, mult.data(), sizeof(int) * Ns, cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemcpyAsync(ctx->lat.ov_off, off.data(), sizeof(int) * (Ns + 1), cudaMemcpyHostToDevice, st) == cudaSuccess &&
-              cudaMemcpyAsync(ctx->lat.ov_ab, ab.data(), sizeof(int) * ab.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
-              cudaMemcpyAsync(ctx->lat.ov_m, m64.data(), sizeof(double) * m64.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
-              cudaMemcpyAsync(ctx->lat.ov_mf, m32.data(), sizeof(float) * m32.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemcpyAsync(ctx->lat.ov_rows, rows.data(), sizeof(unsigned) * rows.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemcpyAsync(ctx->tasks_sym, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemcpyAsync(ctx->tasks_full, tf.data(), sizeof(int4) * tf.size(), cudaMemcpyHostToDevice, st) == cudaSuccess &&
               cudaMemcpyAsync(ctx->tasks_red, tr.data(), sizeof(int4) * tr.size(), cudaMemcpyHostToDevice, st) == cudaSuccess;
@@ -804,7 +853,7 @@ int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
         p.prop_a = r1;
         p.prop_da = r1;
         p.out = d2;
-        CK(run_pass<R>(ctx, p));
+        CK_PASS(run_pass<R>(ctx, p));
         if constexpr (sizeof(R) == 4) {
             if (int rc = to_f(ctx, d2, ctx->f_da)) return rc;
         }
@@ -845,7 +894,7 @@ int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
         p.prop_da = r1;
         p.out = d2;
         set_slots<R>(p, r1, r1, r1, r1, kMaskLeft);
-        CK(run_pass<R>(ctx, p));
+        CK_PASS(run_pass<R>(ctx, p));
         CK((++ctx->launches, launch_symmetrize)(ctx->L, ctx->lat.exch, d2, ctx->st));
         return 0;
     };

@@ -1,26 +1,39 @@
-// Channel-task kernel of the flow right-hand side (sm_103a).
+// Channel-task passes of the flow right-hand side (sm_103a): level-synchronous
+// adaptive quadrature.
 //
-// One CTA integrates one channel task (channel X, kernel, w1, w2, w3) of a
-// pass, i.e. one call of compute_channel_X_{kat,left,central,BSE}!
-// (src/Flow/flow_s.jl:2-173, flow_t.jl, flow_u.jl, BSE_*.jl, SDE.jl:2-56):
+// A pass is the set of channel tasks (channel X, kernel, w1, w2, w3) that one
+// call of compute_dΓ_{1l,2l,ml}!/compute_Γ!/compute_Σ! fans out
+// (src/Flow/compute.jl, SDE.jl).  Each task integrates its bubble over the
+// 4*eval subdomains of integrate_log!/integrate_lin! (src/Flow/quadrature.jl:
+// 84-139) plus two boundary nodes (src/Flow/flow_s.jl:37-38), and every
+// subdomain runs the adaptive Simpson rule with Richardson extrapolation of
+// simps! (quadrature.jl:27-81), whose depth varies by orders of magnitude
+// between subdomains.  Instead of one CTA per task (whose slowest member sets
+// the pass time), the subdomains of all tasks advance level by level:
 //
-//   * the 4*eval Simpson subdomains of integrate_log!/integrate_lin!
-//     (src/Flow/quadrature.jl:84-139) plus the two boundary nodes are spread
-//     over the CTA's warps; every warp runs the adaptive Simpson rule with
-//     Richardson extrapolation of simps! (quadrature.jl:27-81) on its
-//     subdomains.  The reweighted nodes of residual! (quadrature.jl:2-24) are
-//     the previous level's new nodes, so instead of re-evaluating the
-//     integrand there the warp keeps their running sum: one third fewer
-//     integrand evaluations, identical arithmetic up to rounding order.
-//   * inside a warp, a team of T lanes evaluates one node: the lanes split the
-//     per-node scalar work (the two propagator halves and the 6 or 12
-//     interpolation plans, bubbles.jl and buffer.jl) and then each lane
-//     gathers and combines the vertex on its sites (flow_su2_{s,t,u}.jl); the
-//     t channel stages both vertex slots in shared memory for the overlap sum
-//     (flow_su2_t.jl:66-75).  32/T nodes are evaluated per warp at once.
-//   * the per-level convergence test (Frobenius norms over all components and
-//     sites) and the stage bookkeeping are FP64; the integrand runs in R
-//     (double, or float with compensated summation of the node sums).
+//   wave 0   every subdomain evaluates its first five nodes (the 3-point and
+//            the 5-point Simpson sums) and takes the first convergence test;
+//   wave k   the 2^(k+1) new nodes of every subdomain still refining are cut
+//            into chunks of at most kChunk nodes; eval_kernel spreads the
+//            chunks over the whole GPU and writes one partial node sum per
+//            chunk; decide_kernel sums a subdomain's partials in node order,
+//            forms the next Simpson sum and the Richardson value, takes the
+//            reference's test (||R - S|| < atol or relative < rtol, or
+//            n > 2^20) and either stores the result or queues the next level;
+//   reduce   sums each task's subdomain results in a fixed order and writes
+//            the output slice (flow_s.jl:41-51).
+//
+// The reweighted nodes of residual! (quadrature.jl:2-24) are the previous
+// level's new nodes, so their sum is carried from the last level instead of
+// re-evaluating the integrand there.  Results are deterministic (fixed
+// summation order) and agree with the reference's arithmetic up to rounding.
+//
+// Node evaluation: a team of T lanes evaluates a batch of up to kBatch nodes.
+// The lanes first split the batch's scalar work (propagator halves,
+// bubbles.jl; 6 or 12 interpolation plans, buffer.jl + channel.jl), then each
+// lane gathers and combines the vertex on its sites (flow_su2_{s,t,u}.jl); the
+// t channel stages both slots in shared memory for the overlap sum
+// (flow_su2_t.jl:66-75) whose rows sit packed in shared memory.
 #pragma once
 
 #include "pffrg_internal.h"
@@ -30,12 +43,24 @@ namespace pffrg {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarps = 4;
 constexpr int kC = 2;  // SU(2): spin and density components
+constexpr int kBatch = 8;
 
 template <typename R>
-struct TeamScratch {
+struct NodeScratch {
     R p_half[2];
     R loc[4];  // t channel: v3s, v3d, v4s, v4d
     Plan<R> plan[4][3];
+};
+
+// nodes per team batch: 8 per warp in total
+template <int T>
+struct BatchOf {
+    static constexpr int NB = kBatch * T / 32;
+};
+
+template <typename R, int T>
+struct TeamScratch {
+    NodeScratch<R> node[BatchOf<T>::NB];
 };
 
 // per-node argument triple (w, v, v') of buffer (slot, ch) for channel X
@@ -92,15 +117,15 @@ __device__ __forceinline__ void slot_arg(int X, int slot, int ch, R v, R W, R V,
     }
 }
 
-// vertex component c of one slot at site i (get_Γ_comp_avx!, Action.jl:110-167)
+// vertex component c of one slot at one site (single value), for the t-channel local vertices
 template <typename R>
-__device__ __forceinline__ R gather(const PassArgs<R>& A, const TeamScratch<R>& ts, int slot, int c, int i,
-                                    int exch_i) {
+__device__ __forceinline__ R gather_one(const PassArgs<R>& A, const NodeScratch<R>& ns, int slot, int c, int i,
+                                        int exch_i) {
     const R* __restrict__ src = A.src[slot];
     R val = ldg(src + A.L.bare(c) + i);
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
-        const Plan<R>& P = ts.plan[slot][ch];
+        const Plan<R>& P = ns.plan[slot][ch];
         if (P.kernel) {
             const R* q = src + A.L.qbase(c, P.src_ch, P.kernel - 1);
             R acc = plan_read(P, q, P.exch ? exch_i : i);
@@ -108,6 +133,60 @@ __device__ __forceinline__ R gather(const PassArgs<R>& A, const TeamScratch<R>& 
         }
     }
     return val;
+}
+
+// both components of one slot on this lane's sites: v[c][k] = Γ_c(site tl + k T)
+template <typename R, int T, int SPL>
+__device__ __forceinline__ void gather_slot(const PassArgs<R>& A, const NodeScratch<R>& ns, int slot, int tl,
+                                            const int* site_ex, R v[kC][SPL]) {
+    const R* __restrict__ src = A.src[slot];
+    const int Ns = A.L.Ns;
+#pragma unroll
+    for (int k = 0; k < SPL; ++k) {
+        const int i = tl + k * T;
+        v[0][k] = (R)0;
+        v[1][k] = (R)0;
+        if (i < Ns) {
+            v[0][k] = ldg(src + A.L.bare(0) + i);
+            v[1][k] = ldg(src + A.L.bare(1) + i);
+        }
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        const int kern = ns.plan[slot][ch].kernel;
+        if (!kern) continue;
+        // the plan in registers once per node, reused for both components and all sites
+        const int src_ch = ns.plan[slot][ch].src_ch;
+        const int ex = ns.plan[slot][ch].exch;
+        const R sgn_d = ns.plan[slot][ch].sgn_d;
+        const int nc = corners_of(kern);
+        R w[8];
+        int off[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            w[q] = q < nc ? ns.plan[slot][ch].w[q] : (R)0;
+            off[q] = q < nc ? ns.plan[slot][ch].off[q] : 0;
+        }
+        const R* q0 = src + A.L.qbase(0, src_ch, kern - 1);
+        const R* q1 = src + A.L.qbase(1, src_ch, kern - 1);
+#pragma unroll
+        for (int k = 0; k < SPL; ++k) {
+            const int i = tl + k * T;
+            if (i >= Ns) continue;
+            const int s = ex ? site_ex[k] : i;
+            R a0 = w[0] * ldg(q0 + off[0] + s);
+            R a1 = w[0] * ldg(q1 + off[0] + s);
+#pragma unroll
+            for (int q = 1; q < 8; ++q) {
+                if (q < nc) {
+                    a0 += w[q] * ldg(q0 + off[q] + s);
+                    a1 += w[q] * ldg(q1 + off[q] + s);
+                }
+            }
+            v[0][k] += a0;
+            v[1][k] += sgn_d * a1;
+        }
+    }
 }
 
 template <typename R>
@@ -129,13 +208,6 @@ __device__ __forceinline__ void acc_add<float>(Acc<float>& a, float x) {
     a.s = t;
 }
 
-template <typename R, int T>
-__device__ __forceinline__ double cross_team_sum(double v) {
-#pragma unroll
-    for (int o = T; o < 32; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
-    return v;
-}
-
 template <int T>
 __device__ __forceinline__ double in_team_sum(double v) {
 #pragma unroll
@@ -143,366 +215,628 @@ __device__ __forceinline__ double in_team_sum(double v) {
     return v;
 }
 
+// Task of a subdomain record and its frequencies (get_kernel_args, mesh.jl:30-83)
+struct TaskInfo {
+    int X, kernel, w1, w2, w3;
+};
+
+template <typename R>
+__device__ __forceinline__ TaskInfo task_of(const PassArgs<R>& A, int sub, int jobs) {
+    const int ct = sub / jobs;  // channel-task index = y * ntasks + task
+    const int y = ct / A.ntasks;
+    const int4 t = A.tasks[ct - y * A.ntasks];
+    return TaskInfo{A.chan_of_y[y], t.x, t.y, t.z, t.w};
+}
+
 template <typename R, int T, int SPL>
-struct Warp {
+struct Team {
     const PassArgs<R>& A;
     const SMesh<R>& M;
-    TeamScratch<R>& ts;
-    R* tmp;  // t channel: [2][kC][Ns] slot values of this team's node
-    int X;   // channel
-    int tl;  // lane in team
-    R W, V, VP;
-    int nprop;
-    unsigned long long nodes;  // integrand evaluations of this team
-    unsigned long long alg;    // algorithmic vertex values of these evaluations (lane 0 of the team)
+    TeamScratch<R, T>& ts;
+    R* tmp;                 // t channel: [4][Ns] slot values of the current node
+    const unsigned* rows;   // packed overlap rows (shared or global)
+    const int* row_off;     // [Ns+1]
+    int tl;                 // lane in team
+    int site_ex[SPL];       // exchange[site] of this lane's sites
+    unsigned long long nodes, alg;
 
-    // Evaluate the integrand at node x for this team's sites: g[c][k] = Γ_c(site tl + k*T).
-    // Team-collective; inactive teams take part in the warp syncs only.
-    __device__ __noinline__ void eval(double x, bool active, R g[kC][SPL]) {
-        const R v = (R)x;
+    // Evaluate the integrand of channel X at up to NB nodes x[0..count) of one task:
+    // g[j][c][k] = Γ_c(site tl + k T; x_j).  Team-collective: all lanes of the warp call it
+    // together (inactive teams with count = 0).
+    __device__ void eval(const TaskInfo& ti, R W, R V, R VP, const double* x, int count, R g[BatchOf<T>::NB][kC][SPL]) {
+        const int X = ti.X;
         const int Ns = A.L.Ns;
         const int nslots = (X == 1) ? 4 : 2;
-        if (active) ++nodes;
+        const int nprop = A.prop_kind == PROP_KAT ? 2 : 1;
         const int nitems = nprop + 3 * nslots;
-        if (active) {
-            for (int item = tl; item < nitems; item += T) {
-                if (item < nprop) {
-                    ts.p_half[item] = prop_half<R>(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a, A.prop_da,
-                                                   (R)A.Lam, v, W);
+        nodes += count;
+        // teams of one warp may hold different channels and batch lengths: every lane runs
+        // the same sequence of warp syncs, bounded by the warp's longest batch
+        int mx = count;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+        // phase A: scalar work of all nodes of the batch, split over the team's lanes
+        for (int it = tl; it < count * nitems; it += T) {
+            const int j = it / nitems, item = it - j * nitems;
+            NodeScratch<R>& ns = ts.node[j];
+            const R v = (R)x[j];
+            if (item < nprop) {
+                ns.p_half[item] = prop_half<R>(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a, A.prop_da, (R)A.Lam, v, W);
+            } else {
+                const int k = item - nprop;
+                const int slot = k / 3, ch = k - 3 * slot;
+                Plan<R>& P = ns.plan[slot][ch];
+                if (A.mask[X][slot] & (1 << ch)) {
+                    R a0, a1, a2;
+                    slot_arg<R>(X, slot, ch, v, W, V, VP, a0, a1, a2);
+                    make_plan<R>(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
                 } else {
-                    const int k = item - nprop;
-                    const int slot = k / 3, ch = k % 3;
-                    Plan<R>& P = ts.plan[slot][ch];
-                    if (A.mask[X][slot] & (1 << ch)) {
-                        R a0, a1, a2;
-                        slot_arg<R>(X, slot, ch, v, W, V, VP, a0, a1, a2);
-                        make_plan<R>(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
-                    } else {
-                        P.kernel = 0;
+                    P.kernel = 0;
+                }
+            }
+        }
+        __syncwarp();
+        if (X == 1) {
+            // local vertices at site 1 (flow_su2_t.jl:46-48)
+            const int e0 = ldg(A.exch);
+            for (int it = tl; it < count * 4; it += T) {
+                const int j = it >> 2, q = it & 3;
+                ts.node[j].loc[q] = gather_one(A, ts.node[j], 2 + (q >> 1), q & 1, 0, e0);
+            }
+        }
+        __syncwarp();
+        if (A.node_counter && tl == 0) {
+            for (int j = 0; j < count; ++j) {
+                unsigned long long cs = 0, c1 = 0;
+                for (int s = 0; s < nslots; ++s)
+                    for (int ch = 0; ch < 3; ++ch) (s < 2 ? cs : c1) += corners_of(ts.node[j].plan[s][ch].kernel);
+                unsigned long long v = cs * Ns + c1 + 3ull * Ns;
+                if (X == 1) v += 2ull * row_off[Ns];
+                alg += v * kC;
+            }
+        }
+        // phase B: gathers and per-site combination, node by node
+        for (int j = 0; j < mx; ++j) {
+            const bool act = j < count;
+            const NodeScratch<R>& ns = ts.node[act ? j : 0];
+            R p = (R)0;
+            R v1[kC][SPL], v2[kC][SPL];
+            if (act) {
+                p = (nprop == 2) ? ns.p_half[0] + ns.p_half[1] : ns.p_half[0];
+                gather_slot<R, T, SPL>(A, ns, 0, tl, site_ex, v1);
+                gather_slot<R, T, SPL>(A, ns, 1, tl, site_ex, v2);
+            }
+            if (act && X != 1) {
+                const R two = (X == 0) ? (R)-2 : (R)2;
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) {
+                    g[j][0][k] = -p * (two * v1[0][k] * v2[0][k] + v1[0][k] * v2[1][k] + v1[1][k] * v2[0][k]);
+                    g[j][1][k] = -p * ((R)3 * v1[0][k] * v2[0][k] + v1[1][k] * v2[1][k]);
+                }
+            }
+            const bool tch = act && X == 1;
+            if (tch) {
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) {
+                    const int i = tl + k * T;
+                    if (i < Ns) {
+                        tmp[i] = v1[0][k];
+                        tmp[Ns + i] = v1[1][k];
+                        tmp[2 * Ns + i] = v2[0][k];
+                        tmp[3 * Ns + i] = v2[1][k];
                     }
                 }
             }
-        }
-        __syncwarp();
-        if (A.node_counter && active && tl == 0) {
-            // corner reads of the two site slots on all sites and of the t-channel local
-            // slots at one site, bare (2 Ns) and output (Ns) values, t-channel overlap operands
-            unsigned long long cs = 0, c1 = 0;
-            for (int s = 0; s < nslots; ++s)
-                for (int ch = 0; ch < 3; ++ch) (s < 2 ? cs : c1) += corners_of(ts.plan[s][ch].kernel);
-            unsigned long long v = cs * Ns + c1 + 3ull * Ns;
-            if (X == 1) v += 2ull * ldg(A.ov_off + Ns);
-            alg += v * kC;
-        }
-        R p = (R)0;
-        if (active) p = (nprop == 2) ? ts.p_half[0] + ts.p_half[1] : ts.p_half[0];
-        if (X != 1) {
-            const R two = (X == 0) ? (R)-2 : (R)2;
+            __syncwarp();
+            if (tch) {
+                const R v3s = ns.loc[0], v3d = ns.loc[1], v4s = ns.loc[2], v4d = ns.loc[3];
+                const R coef = -p * (R)-2;
+                const R twoS = (R)A.twoS;
 #pragma unroll
-            for (int k = 0; k < SPL; ++k) {
-                const int i = tl + k * T;
-                g[0][k] = (R)0;
-                g[1][k] = (R)0;
-                if (active && i < Ns) {
-                    const int ei = ldg(A.exch + i);
-                    const R v1s = gather(A, ts, 0, 0, i, ei), v1d = gather(A, ts, 0, 1, i, ei);
-                    const R v2s = gather(A, ts, 1, 0, i, ei), v2d = gather(A, ts, 1, 1, i, ei);
-                    g[0][k] = -p * (two * v1s * v2s + v1s * v2d + v1d * v2s);
-                    g[1][k] = -p * ((R)3 * v1s * v2s + v1d * v2d);
+                for (int k = 0; k < SPL; ++k) {
+                    const int i = tl + k * T;
+                    const R v1s = v1[0][k], v1d = v1[1][k], v2s = v2[0][k], v2d = v2[1][k];
+                    R Gs = -p * ((R)-1 * v1s * v4s + v1s * v4d - (R)1 * v3s * v2s + v3d * v2s);
+                    R Gd = -p * ((R)3 * v1d * v4s + v1d * v4d + (R)3 * v3s * v2d + v3d * v2d);
+                    if (i < Ns) {
+                        const int j0 = row_off[i], j1 = row_off[i + 1];
+                        for (int r = j0; r < j1; ++r) {
+                            const unsigned row = rows[r];
+                            const int ia = row & 0xff, ib = (row >> 8) & 0xff;
+                            const R mm = coef * (R)(row >> 16) * twoS;
+                            Gs += mm * tmp[ia] * tmp[2 * Ns + ib];
+                            Gd += mm * tmp[Ns + ia] * tmp[3 * Ns + ib];
+                        }
+                    }
+                    g[j][0][k] = Gs;
+                    g[j][1][k] = Gd;
                 }
             }
             __syncwarp();
-            return;
         }
-        // t channel: local vertices at site 1 (flow_su2_t.jl:46-48)
-        if (active && tl < 4) {
-            const int slot = 2 + (tl >> 1), c = tl & 1;
-            ts.loc[tl] = gather(A, ts, slot, c, 0, ldg(A.exch));
-        }
-        // both slots on all sites into shared memory
-#pragma unroll
-        for (int k = 0; k < SPL; ++k) {
-            const int i = tl + k * T;
-            if (active && i < Ns) {
-                const int ei = ldg(A.exch + i);
-                tmp[i] = gather(A, ts, 0, 0, i, ei);
-                tmp[Ns + i] = gather(A, ts, 0, 1, i, ei);
-                tmp[2 * Ns + i] = gather(A, ts, 1, 0, i, ei);
-                tmp[3 * Ns + i] = gather(A, ts, 1, 1, i, ei);
-            }
-        }
-        __syncwarp();
-        const R v3s = ts.loc[0], v3d = ts.loc[1], v4s = ts.loc[2], v4d = ts.loc[3];
-        const R fac = -p * (R)-2;
-        const R twoS = (R)A.twoS;
-#pragma unroll
-        for (int k = 0; k < SPL; ++k) {
-            const int i = tl + k * T;
-            g[0][k] = (R)0;
-            g[1][k] = (R)0;
-            if (active && i < Ns) {
-                const R v1s = tmp[i], v1d = tmp[Ns + i], v2s = tmp[2 * Ns + i], v2d = tmp[3 * Ns + i];
-                R Gs = -p * ((R)-1 * v1s * v4s + v1s * v4d - (R)1 * v3s * v2s + v3d * v2s);
-                R Gd = -p * ((R)3 * v1d * v4s + v1d * v4d + (R)3 * v3s * v2d + v3d * v2d);
-                const int j0 = ldg(A.ov_off + i), j1 = ldg(A.ov_off + i + 1);
-                for (int j = j0; j < j1; ++j) {
-                    const int ab = ldg(A.ov_ab + j);
-                    const int ia = ab & 0xffff, ib = ab >> 16;
-                    const R mm = fac * ldg(A.ov_m + j) * twoS;
-                    Gs += mm * tmp[ia] * tmp[2 * Ns + ib];
-                    Gd += mm * tmp[Ns + ia] * tmp[3 * Ns + ib];
-                }
-                g[0][k] = Gs;
-                g[1][k] = Gd;
-            }
-        }
-        __syncwarp();
+    }
+};
+
+// ---------------------------------------------------------------------------
+// wave workspace (device scratch of a pass; one block carved into arrays)
+// ---------------------------------------------------------------------------
+constexpr int kChunk = 32;      // nodes per chunk
+constexpr int kMaxChunks = 64;  // chunks per subdomain and level (bigger levels use bigger chunks)
+
+// Queue the next level (n new nodes) of subdomain sub into wave parity `par`.
+__device__ __forceinline__ void enqueue(WaveSpace& Wsp, int par, int sub, long long n) {
+    long long nch = (n + kChunk - 1) / kChunk;
+    if (nch > kMaxChunks) nch = kMaxChunks;
+    const long long per = (n + nch - 1) / nch;
+    nch = (n + per - 1) / per;
+    const int base = atomicAdd(&Wsp.counters[par], (int)nch);
+    if (base + nch > Wsp.qcap) {
+        atomicOr(&Wsp.counters[4], 1);
+        Wsp.subs[sub].n = 0;
+        return;
+    }
+    for (int k = 0; k < nch; ++k) {
+        const long long f = k * per;
+        const long long c = (f + per <= n) ? per : n - f;
+        Wsp.queue[par][base + k] = make_int4(sub, (int)f, (int)c, 0);
+    }
+    Wsp.subs[sub].chunk0 = base;
+    Wsp.subs[sub].nchunk = (int)nch;
+    Wsp.subs[sub].n = n;
+    const int a = atomicAdd(&Wsp.counters[2 + par], 1);
+    Wsp.active[par][a] = sub;
+}
+
+template <typename R>
+__device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const SMesh<R>& M, const TaskInfo& ti, R& W, R& V,
+                                           R& VP) {
+    const R* Om = (ti.X == 1) ? M.Ot : M.Os;
+    const R* nu = (ti.X == 1) ? M.nt : M.ns;
+    const R inf = (R)INFINITY;
+    W = Om[ti.w1];
+    V = (ti.kernel == 2 || ti.kernel == 4) ? nu[ti.w2] : inf;
+    VP = (ti.kernel == 3 || ti.kernel == 4) ? nu[ti.w3] : inf;
+}
+
+// shared-memory layout common to the wave kernels
+template <typename R, int T>
+struct SmemLayout {
+    static constexpr int NPW = 32 / T;
+    size_t mesh, teams, tmp, rows, total;
+    __host__ __device__ SmemLayout(int Ns, long long R_rows, bool rows_in_smem) {
+        mesh = 0;
+        teams = mesh + sizeof(SMesh<R>);
+        tmp = teams + sizeof(TeamScratch<R, T>) * kWarps * NPW;
+        rows = tmp + ((sizeof(R) * (size_t)kWarps * NPW * 4 * Ns + 15) & ~(size_t)15);
+        total = rows + (rows_in_smem ? sizeof(unsigned) * (size_t)(R_rows + Ns + 1) : 0);
     }
 };
 
 template <typename R, int T, int SPL>
-__global__ void __launch_bounds__(kWarps * 32) pass_kernel(PassArgs<R> A) {
+__device__ __forceinline__ Team<R, T, SPL> make_team(const PassArgs<R>& A, unsigned char* smem, const SMesh<R>& M,
+                                                     int warp, int team, int tl) {
     constexpr int NPW = 32 / T;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    SMesh<R>& M = *reinterpret_cast<SMesh<R>*>(smem_raw);
-    TeamScratch<R>* teams = reinterpret_cast<TeamScratch<R>*>(smem_raw + sizeof(SMesh<R>));
     const int Ns = A.L.Ns;
-    R* tmp_all = reinterpret_cast<R*>(smem_raw + sizeof(SMesh<R>) + sizeof(TeamScratch<R>) * kWarps * NPW);
-    double* red = reinterpret_cast<double*>(tmp_all + (size_t)kWarps * NPW * 4 * Ns);
+    SmemLayout<R, T> lay(Ns, A.rows_total, A.rows_in_smem);
+    TeamScratch<R, T>* teams = reinterpret_cast<TeamScratch<R, T>*>(smem + lay.teams);
+    R* tmp = reinterpret_cast<R*>(smem + lay.tmp) + (size_t)(warp * NPW + team) * 4 * Ns;
+    const unsigned* rows;
+    const int* roff;
+    if (A.rows_in_smem) {
+        rows = reinterpret_cast<const unsigned*>(smem + lay.rows);
+        roff = reinterpret_cast<const int*>(rows + A.rows_total);
+    } else {
+        rows = A.ov_rows;
+        roff = A.ov_off;
+    }
+    Team<R, T, SPL> t{A, M, teams[warp * NPW + team], tmp, rows, roff, tl, {}, 0, 0};
+#pragma unroll
+    for (int k = 0; k < SPL; ++k) {
+        const int i = tl + k * T;
+        t.site_ex[k] = i < Ns ? ldg(A.exch + i) : 0;
+    }
+    return t;
+}
 
+template <typename R, int T>
+__device__ __forceinline__ void load_common(const PassArgs<R>& A, unsigned char* smem) {
+    SMesh<R>& M = *reinterpret_cast<SMesh<R>*>(smem);
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+    if (A.rows_in_smem) {
+        SmemLayout<R, T> lay(A.L.Ns, A.rows_total, true);
+        unsigned* rows = reinterpret_cast<unsigned*>(smem + lay.rows);
+        for (long long k = threadIdx.x; k < A.rows_total; k += blockDim.x) rows[k] = ldg(A.ov_rows + k);
+        int* roff = reinterpret_cast<int*>(rows + A.rows_total);
+        for (int k = threadIdx.x; k <= A.L.Ns; k += blockDim.x) roff[k] = ldg(A.ov_off + k);
+    }
     __syncthreads();
+}
 
-    const int X = A.chan_of_y[blockIdx.y];
-    const int4 task = A.tasks[blockIdx.x];
-    const int kernel = task.x;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int team = lane / T, tl = lane % T;
-
-    // get_kernel_args (mesh.jl:30-83)
-    const R* Om = (X == 1) ? M.Ot : M.Os;
-    const R* nu = (X == 1) ? M.nt : M.ns;
+// subdomain range of job `job` of a task (flow_s.jl:29-36; quadrature.jl:84-139); false if empty
+template <typename R>
+__device__ __forceinline__ bool sub_range(const PassArgs<R>& A, const TaskInfo& ti, int job, double& lo, double& hi,
+                                          double& sgn) {
     const double* mesh = A.mesh;
-    const double* Om64 = mesh + A.L.Nsig + (X == 1 ? A.L.NO + A.L.Nn : 0);
+    const double* Om64 = mesh + A.L.Nsig + (ti.X == 1 ? A.L.NO + A.L.Nn : 0);
     const double* nu64 = Om64 + A.L.NO;
-    const R inf = (R)INFINITY;
-    const R W = Om[task.y];
-    const R V = (kernel == 2 || kernel == 4) ? nu[task.z] : inf;
-    const R VP = (kernel == 3 || kernel == 4) ? nu[task.w] : inf;
-
-    Warp<R, T, SPL> wp{A, M, teams[warp * NPW + team], tmp_all + (size_t)(warp * NPW + team) * 4 * Ns, X, tl, W, V,
-                       VP, A.prop_kind == PROP_KAT ? 2 : 1, 0, 0};
-
-    // integration ranges (flow_s.jl:29-38): ref = Λ + w/2, val = Ω[end] + ν[end], computed in FP64
-    const double W64 = Om64[task.y];
-    const double ref = A.Lam + 0.5 * W64;
+    const double ref = A.Lam + 0.5 * Om64[ti.w1];
     const double val = Om64[A.L.NO - 1] + nu64[A.L.Nn - 1];
     const int eval = A.eval;
-    // subdomain end points of integrate_log! (ξ^k a, computed on the host with libm's pow
-    // exactly as the reference): an end point at v = ±val sits on the jump of the vertex
-    // read-out at Ω[end] + ν[end], so it must round exactly like the reference's
-    const double* lb = A.log_bounds + (size_t)((X == 1 ? A.L.NO : 0) + task.y) * (eval + 1);
+    const int range = job / eval, sub = job % eval + 1;
+    sgn = 1.0;
+    if (range == 0 || range == 3) {
+        const double a = 2.0 * ref, b = 1.0 * val;
+        if (!(b > a)) return false;
+        // ξ^k a with libm's pow, computed on the host: an end point at ±val sits on the jump
+        // of the vertex read-out at Ω[end] + ν[end] and must round exactly like the reference
+        const double* lb = A.log_bounds + (size_t)((ti.X == 1 ? A.L.NO : 0) + ti.w1) * (eval + 1);
+        lo = lb[sub - 1];
+        hi = lb[sub];
+        sgn = range == 0 ? -1.0 : 1.0;
+    } else {
+        const double a = range == 1 ? -2.0 * ref : 0.0 * ref;
+        const double b = range == 1 ? 0.0 * ref : 2.0 * ref;
+        if (!(b > a)) return false;
+        const double h = (b - a) / eval;
+        lo = __dadd_rn(a, __dmul_rn((double)(sub - 1), h));
+        hi = __dadd_rn(a, __dmul_rn((double)sub, h));
+    }
+    return true;
+}
 
-    double tacc[kC][SPL];
+// the reference's convergence test of simps! on one team's sites; returns 1 when done
+template <int T, int SPL>
+__device__ __forceinline__ int simps_test(const double s_old[kC][SPL], const double s_new[kC][SPL], long long n,
+                                          double atol, double rtol, int team, bool in_team0_only) {
+    double ss_r = 0.0, ss_n = 0.0, ss_d = 0.0;
 #pragma unroll
     for (int c = 0; c < kC; ++c)
 #pragma unroll
-        for (int k = 0; k < SPL; ++k) tacc[c][k] = 0.0;
+        for (int k = 0; k < SPL; ++k) {
+            const double rich = s_old[c][k] * (-1.0 / 15.0) + (16.0 / 15.0) * s_new[c][k];
+            const double dd = rich - s_new[c][k];
+            ss_r += rich * rich;
+            ss_n += s_new[c][k] * s_new[c][k];
+            ss_d += dd * dd;
+        }
+    (void)team;
+    (void)in_team0_only;
+    ss_r = in_team_sum<T>(ss_r);
+    ss_n = in_team_sum<T>(ss_n);
+    ss_d = in_team_sum<T>(ss_d);
+    const double adiff = sqrt(ss_d);
+    const double rdiff = adiff / fmax(sqrt(ss_r), sqrt(ss_n));
+    return (adiff < atol || rdiff < rtol || 2 * n > (1ll << 20)) ? 1 : 0;
+}
 
-    R g[kC][SPL];
-    const int njobs = 4 * eval + 1;
-    for (int job = warp; job < njobs; job += kWarps) {
-        if (job == 4 * eval) {
-            // boundary corrections (flow_s.jl:37-38): two single nodes weighted by corrs
-            const double c0 = A.corrs[0 + 2 * (X + 3 * task.y)];
-            const double c1 = A.corrs[1 + 2 * (X + 3 * task.y)];
-            double bacc[kC][SPL];
-#pragma unroll
-            for (int c = 0; c < kC; ++c)
-#pragma unroll
-                for (int k = 0; k < SPL; ++k) bacc[c][k] = 0.0;
-            for (int r = 0; r < 2; r += NPW) {
-                const int nd = r + team;
-                wp.eval(nd == 0 ? -val : val, nd < 2, g);
-                if (nd < 2) {
-                    const double wgt = nd == 0 ? c0 : c1;
-#pragma unroll
-                    for (int c = 0; c < kC; ++c)
-#pragma unroll
-                        for (int k = 0; k < SPL; ++k) bacc[c][k] += wgt * (double)g[c][k];
-                }
+// ---- wave 0: first five nodes of every subdomain, boundary nodes, first test ----
+template <typename R, int T, int SPL>
+__global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveSpace Wsp) {
+    constexpr int NPW = 32 / T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    load_common<R, T>(A, smem);
+    const SMesh<R>& M = *reinterpret_cast<const SMesh<R>*>(smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int team = lane / T, tl = lane % T;
+    Team<R, T, SPL> tm = make_team<R, T, SPL>(A, smem, M, warp, team, tl);
+    const int Ns = A.L.Ns;
+    const int jobs = 4 * A.eval + 1;
+    const long long nwarps = (long long)gridDim.x * kWarps;
+    constexpr int NB = BatchOf<T>::NB;
+    for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < Wsp.nsub; base += nwarps * NPW) {
+        const int sub = (int)(base + team);
+        const bool valid = sub < Wsp.nsub;
+        TaskInfo ti{0, 1, 0, 0, 0};
+        int job = 0, cnt = 0;
+        double x[8], lo = 0, hi = 0, sgn = 1;
+        double c0 = 0, c1 = 0;
+        bool boundary = false;
+        if (valid) {
+            ti = task_of(A, sub, jobs);
+            job = sub % jobs;
+            if (job == 4 * A.eval) {
+                const double* Om64 = A.mesh + A.L.Nsig + (ti.X == 1 ? A.L.NO + A.L.Nn : 0);
+                const double val = Om64[A.L.NO - 1] + Om64[A.L.NO + A.L.Nn - 1];
+                x[0] = -val;
+                x[1] = val;
+                c0 = A.corrs[0 + 2 * (ti.X + 3 * ti.w1)];
+                c1 = A.corrs[1 + 2 * (ti.X + 3 * ti.w1)];
+                cnt = 2;
+                boundary = true;
+            } else if (sub_range(A, ti, job, lo, hi, sgn)) {
+                const double mid = 0.5 * (lo + hi);
+                const double h = 0.5 * (hi - lo) / 2.0;
+                x[0] = sgn * lo;
+                x[1] = sgn * __dadd_rn(lo, __dmul_rn(1.0, h));
+                x[2] = sgn * mid;
+                x[3] = sgn * __dadd_rn(lo, __dmul_rn(3.0, h));
+                x[4] = sgn * hi;
+                cnt = 5;
             }
-#pragma unroll
-            for (int c = 0; c < kC; ++c)
-#pragma unroll
-                for (int k = 0; k < SPL; ++k) tacc[c][k] += cross_team_sum<R, T>(bacc[c][k]);
-            continue;
         }
-        const int range = job / eval, sub = job % eval + 1;
-        double lo, hi, sgn = 1.0;
-        if (range == 0 || range == 3) {
-            const double a = 2.0 * ref, b = 1.0 * val;
-            if (!(b > a)) continue;
-            lo = lb[sub - 1];
-            hi = lb[sub];
-            sgn = range == 0 ? -1.0 : 1.0;
-        } else {
-            // integrate_lin!: a + (i-1) h and a + i h, rounded like the reference (no FMA)
-            const double a = range == 1 ? -2.0 * ref : 0.0 * ref;
-            const double b = range == 1 ? 0.0 * ref : 2.0 * ref;
-            if (!(b > a)) continue;
-            const double h = (b - a) / eval;
-            lo = __dadd_rn(a, __dmul_rn((double)(sub - 1), h));
-            hi = __dadd_rn(a, __dmul_rn((double)sub, h));
-        }
-
-        // ---- simps! on [lo, hi] ----
-        double s_old[kC][SPL], s_new[kC][SPL], f_prev[kC][SPL];
-#pragma unroll
-        for (int c = 0; c < kC; ++c)
-#pragma unroll
-            for (int k = 0; k < SPL; ++k) s_old[c][k] = f_prev[c][k] = 0.0;
-        const double mid = 0.5 * (lo + hi);
-        const double w_end = 1.0 * (hi - lo) / 6.0, w_mid = 2.0 * (hi - lo) / 3.0;
-        for (int r = 0; r < 3; r += NPW) {
-            const int nd = r + team;
-            const double x = nd == 0 ? lo : (nd == 1 ? mid : hi);
-            wp.eval(sgn * x, nd < 3, g);
-            if (nd < 3) {
-                const double wgt = nd == 1 ? w_mid : w_end;
+        R W = 0, V = 0, VP = 0;
+        if (valid) task_freqs(A, M, ti, W, V, VP);
+        // all teams of the warp evaluate together (cnt = 0 for idle teams), NB nodes at a time
+        R g[5][kC][SPL];
+        for (int b = 0; b < 5; b += NB) {
+            R gb[NB][kC][SPL];
+            const int nb = max(0, min(NB, cnt - b));
+            tm.eval(ti, W, V, VP, x + b, nb, gb);
+            for (int j = 0; j < NB && b + j < 5; ++j)
 #pragma unroll
                 for (int c = 0; c < kC; ++c)
 #pragma unroll
-                    for (int k = 0; k < SPL; ++k) {
-                        s_old[c][k] += wgt * (double)g[c][k];
-                        if (nd == 1) f_prev[c][k] += (double)g[c][k];
-                    }
-            }
+                    for (int k = 0; k < SPL; ++k) g[b + j][c][k] = gb[j][c][k];
         }
+        const bool simpson = valid && !boundary && cnt == 5;
+        // simps!: 3-point sum, 5-point sum via residual! with n = 2, Richardson test
+        const double we = 1.0 * (hi - lo) / 6.0, wm = 2.0 * (hi - lo) / 3.0;
+        const double h = 0.5 * (hi - lo) / 2.0;
+        const double wn = 4.0 * h / 3.0, wo = -2.0 * h / 3.0;
+        double s_old[kC][SPL], s_new[kC][SPL], f_new[kC][SPL];
 #pragma unroll
         for (int c = 0; c < kC; ++c)
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
-                s_old[c][k] = cross_team_sum<R, T>(s_old[c][k]);
-                f_prev[c][k] = cross_team_sum<R, T>(f_prev[c][k]);
+                s_old[c][k] = s_new[c][k] = f_new[c][k] = 0.0;
+                if (!simpson) continue;
+                s_old[c][k] = we * (double)g[0][c][k];
+                s_old[c][k] += wm * (double)g[2][c][k];
+                s_old[c][k] += we * (double)g[4][c][k];
+                f_new[c][k] = (double)g[1][c][k] + (double)g[3][c][k];
+                s_new[c][k] = 0.5 * s_old[c][k] + wn * f_new[c][k] + wo * (double)g[2][c][k];
             }
-        long long n = 2;
-        while (true) {
-            const double h = 0.5 * (hi - lo) / (double)n;
-            Acc<R> fn[kC][SPL];
-#pragma unroll
-            for (int c = 0; c < kC; ++c)
-#pragma unroll
-                for (int k = 0; k < SPL; ++k) fn[c][k] = Acc<R>{(R)0, (R)0};
-            for (long long r = 0; r < n; r += NPW) {
-                const long long nd = r + team;
-                const double x = __dadd_rn(lo, __dmul_rn(2.0 * (double)(nd + 1) - 1.0, h));
-                wp.eval(sgn * x, nd < n, g);
-                if (nd < n) {
-#pragma unroll
-                    for (int c = 0; c < kC; ++c)
-#pragma unroll
-                        for (int k = 0; k < SPL; ++k) acc_add(fn[c][k], g[c][k]);
-                }
-            }
-            double ss_r = 0.0, ss_n = 0.0, ss_d = 0.0;
-            const double wn = 4.0 * h / 3.0, wo = -2.0 * h / 3.0;
+        // every lane takes part in the test's team reductions
+        const int done = simps_test<T, SPL>(s_old, s_new, 2, A.atol, A.rtol, team, false);
+        if (!valid) continue;
+        double* sA = Wsp.stA + (size_t)sub * kC * Ns;
+        double* sB = Wsp.stB + (size_t)sub * kC * Ns;
+        if (!simpson) {
+            // boundary corrections (two nodes weighted by corrs) or an empty range
 #pragma unroll
             for (int c = 0; c < kC; ++c)
 #pragma unroll
                 for (int k = 0; k < SPL; ++k) {
-                    const double fsum = cross_team_sum<R, T>((double)fn[c][k].s + (double)fn[c][k].c);
-                    s_new[c][k] = 0.5 * s_old[c][k] + wn * fsum + wo * f_prev[c][k];
-                    f_prev[c][k] = fsum;
-                    const double rich = s_old[c][k] * (-1.0 / 15.0) + (16.0 / 15.0) * s_new[c][k];
-                    const double dd = rich - s_new[c][k];
-                    // a team holds a full copy: count each site once
-                    if (team == 0) {
-                        ss_r += rich * rich;
-                        ss_n += s_new[c][k] * s_new[c][k];
-                        ss_d += dd * dd;
-                    }
+                    const int i = tl + k * T;
+                    if (i < Ns) sA[c * Ns + i] = boundary ? c0 * (double)g[0][c][k] + c1 * (double)g[1][c][k] : 0.0;
                 }
-            ss_r = in_team_sum<T>(ss_r);
-            ss_n = in_team_sum<T>(ss_n);
-            ss_d = in_team_sum<T>(ss_d);
-            const double adiff = sqrt(ss_d);
-            const double rdiff = adiff / fmax(sqrt(ss_r), sqrt(ss_n));
-            int done = (adiff < A.atol || rdiff < A.rtol || 2 * n > (1ll << 20)) ? 1 : 0;
-            done = __shfl_sync(kFull, done, 0);
-            if (done) {
-#pragma unroll
-                for (int c = 0; c < kC; ++c)
-#pragma unroll
-                    for (int k = 0; k < SPL; ++k)
-                        tacc[c][k] += (s_old[c][k] * (-1.0 / 15.0) + (16.0 / 15.0) * s_new[c][k] - s_new[c][k]) +
-                                      s_new[c][k];
-                break;
-            }
-#pragma unroll
-            for (int c = 0; c < kC; ++c)
-#pragma unroll
-                for (int k = 0; k < SPL; ++k) s_old[c][k] = s_new[c][k];
-            n *= 2;
+            if (tl == 0) Wsp.subs[sub].n = 0;
+            continue;
         }
-    }
-
-    if (A.node_counter && tl == 0 && wp.nodes) {
-        atomicAdd(A.node_counter, wp.nodes);
-        atomicAdd(A.node_counter + 1, wp.alg);
-    }
-    // every team holds the full per-site sums: team 0 hands them to the CTA reduction
-    if (team == 0) {
 #pragma unroll
         for (int c = 0; c < kC; ++c)
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 const int i = tl + k * T;
-                if (i < Ns) red[(warp * kC + c) * Ns + i] = tacc[c][k];
+                if (i >= Ns) continue;
+                if (done) {
+                    sA[c * Ns + i] = (s_old[c][k] * (-1.0 / 15.0) + (16.0 / 15.0) * s_new[c][k] - s_new[c][k]) + s_new[c][k];
+                } else {
+                    sA[c * Ns + i] = s_new[c][k];
+                    sB[c * Ns + i] = f_new[c][k];
+                }
+            }
+        if (tl == 0) {
+            SubRec& S = Wsp.subs[sub];
+            S.lo = lo;
+            S.hi = hi;
+            S.sgn = sgn;
+            if (done) S.n = 0;
+            else enqueue(Wsp, 1, sub, 4);
+        }
+    }
+    if (A.node_counter && tl == 0) {
+        atomicAdd(A.node_counter, tm.nodes);
+        atomicAdd(A.node_counter + 1, tm.alg);
+    }
+}
+
+// ---- wave k >= 1: evaluate queued chunks, one partial node sum per chunk ----
+template <typename R, int T, int SPL>
+__global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
+    constexpr int NPW = 32 / T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    load_common<R, T>(A, smem);
+    const SMesh<R>& M = *reinterpret_cast<const SMesh<R>*>(smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int team = lane / T, tl = lane % T;
+    Team<R, T, SPL> tm = make_team<R, T, SPL>(A, smem, M, warp, team, tl);
+    const int Ns = A.L.Ns;
+    const int jobs = 4 * A.eval + 1;
+    const int nchunks = Wsp.counters[par];
+    const long long nwarps = (long long)gridDim.x * kWarps;
+    constexpr int NB = BatchOf<T>::NB;
+    R g[NB][kC][SPL];
+    for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < nchunks; base += nwarps * NPW) {
+        const int chunk = (int)(base + team);
+        const bool valid = chunk < nchunks;
+        int4 cr = make_int4(0, 0, 0, 0);
+        TaskInfo ti{0, 1, 0, 0, 0};
+        double lo = 0, h = 0, sgn = 1;
+        R W = 0, V = 0, VP = 0;
+        if (valid) {
+            cr = Wsp.queue[par][chunk];
+            const SubRec S = Wsp.subs[cr.x];
+            ti = task_of(A, cr.x, jobs);
+            task_freqs(A, M, ti, W, V, VP);
+            lo = S.lo;
+            sgn = S.sgn;
+            h = 0.5 * (S.hi - S.lo) / (double)S.n;
+        }
+        // the longest chunk of the warp's teams bounds the batch loop
+        int cnt = valid ? cr.z : 0;
+        int mx = cnt;
+#pragma unroll
+        for (int o = T; o < 32; o <<= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+        Acc<R> acc[kC][SPL];
+#pragma unroll
+        for (int c = 0; c < kC; ++c)
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) acc[c][k] = Acc<R>{(R)0, (R)0};
+        for (int b = 0; b < mx; b += NB) {
+            double x[NB];
+            const int nb = max(0, min(NB, cnt - b));
+            for (int j = 0; j < nb; ++j) {
+                const long long nd = (long long)cr.y + b + j;  // 0-based new node of the level
+                x[j] = sgn * __dadd_rn(lo, __dmul_rn(2.0 * (double)(nd + 1) - 1.0, h));
+            }
+            tm.eval(ti, W, V, VP, x, nb, g);
+            for (int j = 0; j < nb; ++j)
+#pragma unroll
+                for (int c = 0; c < kC; ++c)
+#pragma unroll
+                    for (int k = 0; k < SPL; ++k) acc_add(acc[c][k], g[j][c][k]);
+        }
+        if (!valid) continue;
+        double* P = Wsp.part + (size_t)chunk * kC * Ns;
+#pragma unroll
+        for (int c = 0; c < kC; ++c)
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int i = tl + k * T;
+                if (i < Ns) P[c * Ns + i] = (double)acc[c][k].s + (double)acc[c][k].c;
             }
     }
-    __syncthreads();
-    // output slice (flow_s.jl:41-51)
+    if (A.node_counter && tl == 0) {
+        atomicAdd(A.node_counter, tm.nodes);
+        atomicAdd(A.node_counter + 1, tm.alg);
+    }
+}
+
+// ---- wave k >= 1: per subdomain, next Simpson sum, test, result or next level ----
+template <int T, int SPL>
+__global__ void __launch_bounds__(kWarps * 32) decide_kernel(WaveSpace Wsp, int Ns, double atol, double rtol, int par) {
+    constexpr int NPW = 32 / T;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int team = lane / T, tl = lane % T;
+    const int nact = Wsp.counters[2 + par];
+    const long long nwarps = (long long)gridDim.x * kWarps;
+    for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < nact; base += nwarps * NPW) {
+        const int a = (int)(base + team);
+        const bool valid = a < nact;
+        const int sub = valid ? Wsp.active[par][a] : 0;
+        SubRec S;
+        if (valid) S = Wsp.subs[sub];
+        else S.n = 1, S.nchunk = 0, S.chunk0 = 0, S.lo = 0, S.hi = 0;
+        double* sA = Wsp.stA + (size_t)sub * kC * Ns;
+        double* sB = Wsp.stB + (size_t)sub * kC * Ns;
+        double s_old[kC][SPL], s_new[kC][SPL], f_new[kC][SPL];
+        const double h = 0.5 * (S.hi - S.lo) / (double)S.n;
+        const double wn = 4.0 * h / 3.0, wo = -2.0 * h / 3.0;
+#pragma unroll
+        for (int c = 0; c < kC; ++c)
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int i = tl + k * T;
+                s_old[c][k] = s_new[c][k] = f_new[c][k] = 0.0;
+                if (!valid || i >= Ns) continue;
+                double f = 0.0;
+                for (int q = 0; q < S.nchunk; ++q) f += Wsp.part[(size_t)(S.chunk0 + q) * kC * Ns + c * Ns + i];
+                f_new[c][k] = f;
+                s_old[c][k] = sA[c * Ns + i];
+                s_new[c][k] = 0.5 * s_old[c][k] + wn * f + wo * sB[c * Ns + i];
+            }
+        const int done = simps_test<T, SPL>(s_old, s_new, S.n, atol, rtol, team, false);
+        if (!valid) continue;
+#pragma unroll
+        for (int c = 0; c < kC; ++c)
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int i = tl + k * T;
+                if (i >= Ns) continue;
+                if (done) {
+                    sA[c * Ns + i] = (s_old[c][k] * (-1.0 / 15.0) + (16.0 / 15.0) * s_new[c][k] - s_new[c][k]) + s_new[c][k];
+                } else {
+                    sA[c * Ns + i] = s_new[c][k];
+                    sB[c * Ns + i] = f_new[c][k];
+                }
+            }
+        if (tl == 0) {
+            if (done) Wsp.subs[sub].n = 0;
+            else enqueue(Wsp, par ^ 1, sub, 2 * S.n);
+        }
+    }
+}
+
+// ---- sum each task's subdomain results (range order, boundary last) into the output ----
+template <typename R>
+__global__ void reduce_kernel(PassArgs<R> A, WaveSpace Wsp) {
+    const int ct = blockIdx.x;  // channel task
+    const int jobs = 4 * A.eval + 1;
+    const int Ns = A.L.Ns;
+    const TaskInfo ti = task_of(A, ct * jobs, jobs);
     const Layout& L = A.L;
     int64_t off;
-    switch (kernel) {
-        case 1: off = (int64_t)Ns * task.y; break;
-        case 2: off = (int64_t)Ns * (task.y + (int64_t)L.NO * task.z); break;
-        case 3: off = (int64_t)Ns * (task.y + (int64_t)L.NO * task.w); break;
-        default: off = (int64_t)Ns * (task.y + (int64_t)L.NO * (task.z + (int64_t)L.Nn * task.w)); break;
+    switch (ti.kernel) {
+        case 1: off = (int64_t)Ns * ti.w1; break;
+        case 2: off = (int64_t)Ns * (ti.w1 + (int64_t)L.NO * ti.w2); break;
+        case 3: off = (int64_t)Ns * (ti.w1 + (int64_t)L.NO * ti.w3); break;
+        default: off = (int64_t)Ns * (ti.w1 + (int64_t)L.NO * (ti.w2 + (int64_t)L.Nn * ti.w3)); break;
     }
     for (int e = threadIdx.x; e < kC * Ns; e += blockDim.x) {
         const int c = e / Ns, i = e % Ns;
         double s = 0.0;
-        for (int w = 0; w < kWarps; ++w) s += red[(w * kC + c) * Ns + i];
-        A.out[L.qbase(c, X, kernel - 1) + off + i] = s;
+        for (int j = 0; j < jobs; ++j) s += Wsp.stA[((size_t)ct * jobs + j) * kC * Ns + c * Ns + i];
+        A.out[L.qbase(c, ti.X, ti.kernel - 1) + off + i] = s;
     }
 }
 
-template <typename R, int T, int SPL>
-static cudaError_t launch_t(const PassArgs<R>& a, cudaStream_t st) {
-    constexpr int NPW = 32 / T;
-    const size_t smem = sizeof(SMesh<R>) + sizeof(TeamScratch<R>) * kWarps * NPW +
-                        sizeof(R) * (size_t)kWarps * NPW * 4 * a.L.Ns + sizeof(double) * kWarps * kC * a.L.Ns;
-    auto kfn = pass_kernel<R, T, SPL>;
-    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    dim3 grid(a.ntasks, a.nchan);
-    kfn<<<grid, kWarps * 32, smem, st>>>(a);
-    return cudaGetLastError();
-}
-
-// team width T = lanes per node, SPL = sites per lane
+// team width T = lanes per node batch, SPL = sites per lane
 template <typename R>
-cudaError_t launch_pass_impl(const PassArgs<R>& a, cudaStream_t st) {
+struct PassLauncher {
+    template <int T, int SPL>
+    static cudaError_t run(const PassArgs<R>& a0, WaveSpace& Wsp, int* h_counters, cudaStream_t st, int grid_cap) {
+        // overlap rows in shared memory when they fit next to the rest
+        PassArgs<R> a = a0;
+        a.rows_in_smem = SmemLayout<R, T>(a.L.Ns, a.rows_total, true).total <= (size_t)160 * 1024;
+        SmemLayout<R, T> lay(a.L.Ns, a.rows_total, a.rows_in_smem);
+        const size_t smem = lay.total;
+        cudaError_t e;
+        if ((e = cudaFuncSetAttribute(wave0_kernel<R, T, SPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        if ((e = cudaFuncSetAttribute(eval_kernel<R, T, SPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        constexpr int NPW = 32 / T;
+        const int teams_per_block = kWarps * NPW;
+        if ((e = cudaMemsetAsync(Wsp.counters, 0, sizeof(int) * 5, st))) return e;
+        int g0 = (Wsp.nsub + teams_per_block - 1) / teams_per_block;
+        wave0_kernel<R, T, SPL><<<g0 < grid_cap ? g0 : grid_cap, kWarps * 32, smem, st>>>(a, Wsp);
+        if ((e = cudaGetLastError())) return e;
+        int par = 1;
+        for (int wave = 1; wave <= 21; ++wave) {
+            if ((e = cudaMemcpyAsync(h_counters, Wsp.counters, sizeof(int) * 5, cudaMemcpyDeviceToHost, st))) return e;
+            if ((e = cudaStreamSynchronize(st))) return e;
+            if (h_counters[4]) return cudaErrorLaunchOutOfResources;  // chunk queue overflow
+            const int nchunks = h_counters[par], nact = h_counters[2 + par];
+            if (nact == 0) break;
+            // reset the other parity's counters for the next wave's queue
+            if ((e = cudaMemsetAsync(Wsp.counters + (par ^ 1), 0, sizeof(int), st))) return e;
+            if ((e = cudaMemsetAsync(Wsp.counters + 2 + (par ^ 1), 0, sizeof(int), st))) return e;
+            int ge = (nchunks + teams_per_block - 1) / teams_per_block;
+            eval_kernel<R, T, SPL><<<ge < grid_cap ? ge : grid_cap, kWarps * 32, smem, st>>>(a, Wsp, par);
+            if ((e = cudaGetLastError())) return e;
+            int gd = (nact + teams_per_block - 1) / teams_per_block;
+            decide_kernel<T, SPL><<<gd < grid_cap ? gd : grid_cap, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol,
+                                                                                           par);
+            if ((e = cudaGetLastError())) return e;
+            par ^= 1;
+        }
+        reduce_kernel<R><<<a.ntasks * a.nchan, 128, 0, st>>>(a, Wsp);
+        return cudaGetLastError();
+    }
+};
+
+template <typename R>
+cudaError_t launch_pass_impl(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st) {
     const int Ns = a.L.Ns;
     if (a.ntasks == 0) return cudaSuccess;
-    if (Ns <= 8) return launch_t<R, 8, 1>(a, st);
-    if (Ns <= 16) return launch_t<R, 16, 1>(a, st);
-    if (Ns <= 32) return launch_t<R, 32, 1>(a, st);
-    if (Ns <= 64) return launch_t<R, 32, 2>(a, st);
-    if (Ns <= 128) return launch_t<R, 32, 4>(a, st);
-    if (Ns <= 256) return launch_t<R, 32, 8>(a, st);
+    const int cap = 152 * 32;
+    if (Ns <= 8) return PassLauncher<R>::template run<8, 1>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 16) return PassLauncher<R>::template run<16, 1>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 32) return PassLauncher<R>::template run<32, 1>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 64) return PassLauncher<R>::template run<32, 2>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 128) return PassLauncher<R>::template run<32, 4>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 256) return PassLauncher<R>::template run<32, 8>(a, Wsp, h_counters, st, cap);
     return cudaErrorInvalidValue;
 }
 

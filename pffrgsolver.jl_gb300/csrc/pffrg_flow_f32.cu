@@ -4,8 +4,8 @@
 namespace pffrg {
 
 template <>
-cudaError_t launch_pass<float>(const PassArgs<float>& a, cudaStream_t st) {
-    return launch_pass_impl<float>(a, st);
+cudaError_t launch_pass<float>(const PassArgs<float>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st) {
+    return launch_pass_impl<float>(a, Wsp, h_counters, st);
 }
 
 }  // namespace pffrg

@@ -4,8 +4,8 @@
 namespace pffrg {
 
 template <>
-cudaError_t launch_pass<double>(const PassArgs<double>& a, cudaStream_t st) {
-    return launch_pass_impl<double>(a, st);
+cudaError_t launch_pass<double>(const PassArgs<double>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st) {
+    return launch_pass_impl<double>(a, Wsp, h_counters, st);
 }
 
 }  // namespace pffrg

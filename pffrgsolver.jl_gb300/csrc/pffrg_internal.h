@@ -18,9 +18,7 @@ struct DevLattice {
     int* exch = nullptr;     // [Ns]
     int* mult = nullptr;     // [Ns]
     int* ov_off = nullptr;   // [Ns+1]
-    int* ov_ab = nullptr;    // [R] site a | (site b << 16)
-    double* ov_m = nullptr;  // [R] multiplicity
-    float* ov_mf = nullptr;  // [R] multiplicity (FP32 path)
+    unsigned* ov_rows = nullptr;  // [R] site a | site b << 8 | multiplicity << 16
 };
 
 // One pass of channel tasks (Katanin / left / central / BSE / reduced-s).
@@ -34,9 +32,10 @@ struct PassArgs {
     const R* prop_da;  // dΣ of the Katanin propagator
     double* out;       // FP64 output action
     const int* exch;
-    const int* ov_off;
-    const int* ov_ab;
-    const R* ov_m;
+    const int* ov_off;       // [Ns+1]
+    const unsigned* ov_rows; // [R] site a | site b << 8 | multiplicity << 16
+    long long rows_total;
+    int rows_in_smem;        // stage the rows in shared memory
     const double* mesh;
     const double* corrs;  // [2,3,NO]
     const double* log_bounds;  // [mesh s/u = 0, t = 1][w1][k = 0..eval]: ξ^k a of integrate_log!
@@ -50,8 +49,62 @@ struct PassArgs {
     unsigned long long* node_counter;  // optional: [0] integrand evaluations, [1] algorithmic values read
 };
 
+// Scratch of one pass of the level-synchronous quadrature: one record and two state
+// vectors per Simpson subdomain, the chunk queues of the current and next level, and one
+// partial node sum per chunk.  Carved out of one device block.
+struct SubRec {
+    double lo, hi, sgn;
+    long long n;  // new nodes of the pending level (0: finished)
+    int chunk0;   // first chunk of the pending level in the wave queue
+    int nchunk;
+};
+
+struct WaveSpace {
+    SubRec* subs;    // [nsub]
+    double* stA;     // [nsub][2 Ns]: Simpson sum of the last level, then the result
+    double* stB;     // [nsub][2 Ns]: node sum of the last level's new nodes
+    int4* queue[2];  // chunk records (sub, first node, count, -) of the current / next level
+    int* active[2];  // subdomains with chunks in the current / next level
+    double* part;    // [qcap][2 Ns] chunk partial node sums
+    int* counters;   // [0..1] chunks, [2..3] active subdomains per parity, [4] queue overflow
+    int nsub, qcap;
+};
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// bytes of the wave workspace for nsub subdomains, Ns sites and qcap chunks
+inline size_t wave_space_bytes(long long nsub, int Ns, long long qcap) {
+    const size_t vec = sizeof(double) * 2 * (size_t)Ns;
+    return align256(sizeof(SubRec) * nsub) + 2 * align256(vec * nsub) + 2 * align256(sizeof(int4) * qcap) +
+           2 * align256(sizeof(int) * nsub) + align256(vec * qcap) + align256(sizeof(int) * 8);
+}
+
+inline void wave_space_carve(WaveSpace& W, void* base, long long nsub, int Ns, long long qcap) {
+    char* p = static_cast<char*>(base);
+    const size_t vec = sizeof(double) * 2 * (size_t)Ns;
+    W.subs = reinterpret_cast<SubRec*>(p);
+    p += align256(sizeof(SubRec) * nsub);
+    W.stA = reinterpret_cast<double*>(p);
+    p += align256(vec * nsub);
+    W.stB = reinterpret_cast<double*>(p);
+    p += align256(vec * nsub);
+    for (int k = 0; k < 2; ++k) {
+        W.queue[k] = reinterpret_cast<int4*>(p);
+        p += align256(sizeof(int4) * qcap);
+    }
+    for (int k = 0; k < 2; ++k) {
+        W.active[k] = reinterpret_cast<int*>(p);
+        p += align256(sizeof(int) * nsub);
+    }
+    W.part = reinterpret_cast<double*>(p);
+    p += align256(vec * qcap);
+    W.counters = reinterpret_cast<int*>(p);
+    W.nsub = (int)nsub;
+    W.qcap = (int)qcap;
+}
+
 template <typename R>
-cudaError_t launch_pass(const PassArgs<R>& a, cudaStream_t st);
+cudaError_t launch_pass(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st);
 
 // GK integrals of the self energy / corrections (QuadGK-equivalent)
 enum SigmaKind { SIG_FLOW = 0, SIG_CORR1 = 1, SIG_CORR2 = 2, SIG_SDE = 3 };
