@@ -38,7 +38,6 @@ UNIT = "dΓ evals/s"
 WORKLOAD = "pyrochlore-L6-2l"
 GAMMA_TOL = (1e-8, 1e-4)
 SIGMA_TOL = (1e-8, 1e-4)
-EVAL = 10  # eval at Λ = 1 with min_eval = 10 (launcher_1l.jl:78)
 
 
 def parse():
@@ -50,13 +49,15 @@ def parse():
     p.add_argument("--workload", default=WORKLOAD)
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     return p.parse_args()
 
 
 def config(args, w, extra=None):
     c = {"workload": w.name, "lattice": w.lattice, "L": w.size, "model": w.model, "J": w.J, "symmetry": w.symmetry,
          "loops": w.loops, "Lambda": w.Lam, "num_sigma": w.num_sigma, "num_omega": w.num_omega, "num_nu": w.num_nu,
-         "eval": EVAL, "gamma_tol": list(GAMMA_TOL), "sigma_tol": list(SIGMA_TOL), "noise": w.noise, "seed": w.seed,
+         "eval": w.eval, "gamma_tol": list(GAMMA_TOL), "sigma_tol": list(SIGMA_TOL), "noise": w.noise, "seed": w.seed,
          "l2": "flushed between timed steps (256 MiB write); the vertex (5.3 MB) is L2-resident within a step",
          "parallelism": f"replicas x{args.gpus}"}
     if extra:
@@ -148,7 +149,7 @@ def cpu_rhs_rate(O, r, m, a, w, target_s: float):
     O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
     t_sigma = time.perf_counter() - t0
     t0 = time.perf_counter()
-    O.dgamma(P, w.loops, w.Lam, a.buf, da, EVAL, gtol=GAMMA_TOL)
+    O.dgamma(P, w.loops, w.Lam, a.buf, da, w.eval, gtol=GAMMA_TOL)
     t_probe = time.perf_counter() - t0
     full_est = t_probe * stride
     stride = int(max(1, min(64, np.ceil(full_est / max(target_s, 1e-3)))))
@@ -156,7 +157,7 @@ def cpu_rhs_rate(O, r, m, a, w, target_s: float):
     da = np.zeros_like(a.buf)
     O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
     t0 = time.perf_counter()
-    st = O.dgamma(P, w.loops, w.Lam, a.buf, da, EVAL, gtol=GAMMA_TOL)
+    st = O.dgamma(P, w.loops, w.Lam, a.buf, da, w.eval, gtol=GAMMA_TOL)
     t_gamma = time.perf_counter() - t0
     per_rhs = t_sigma + stride * t_gamma
     return 1.0 / per_rhs, threads, stride, t_sigma + t_gamma, st
@@ -185,7 +186,7 @@ def reference_arm(args):
         O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
         ts = time.perf_counter() - t0
         t0 = time.perf_counter()
-        O.dgamma(P, w.loops, w.Lam, a.buf, da, EVAL, gtol=GAMMA_TOL)
+        O.dgamma(P, w.loops, w.Lam, a.buf, da, w.eval, gtol=GAMMA_TOL)
         tg = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(ts + stride * tg)
@@ -242,7 +243,7 @@ def ours(args):
     ctx.upload(C.SLOT_A, a)
 
     def rhs():
-        ctx.rhs(w.Lam, EVAL, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
+        ctx.rhs(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
 
     # warm-up
     for _ in range(args.warmup):
@@ -278,57 +279,14 @@ def ours(args):
     ctx.download(C.SLOT_DA, da_mixed)
 
     # FP64 comparator on the same state
-    ctx.set_precision("fp64")
-    rhs()
-    ctx.set_timing(True)
-    ctx.read_stats(reset=True)
-    for _ in range(args.fp64_steps):
-        flush.zero_()
-        torch.cuda.synchronize(dev)
-        rhs()
-    st64 = ctx.read_stats(reset=True)
-    ctx.set_timing(False)
-    fp64_ms = st64["rhs_ms"] / max(1, args.fp64_steps)
-    da64 = pkg.action.Action.empty_like(a)
-    ctx.download(C.SLOT_DA, da64)
-    err_mixed = float(np.max(np.abs(da_mixed.buf - da64.buf)) / np.max(np.abs(da64.buf)))
-    ctx.set_precision("mixed")
+    fp64_ms, err_mixed = None, None
+    if args.fp64_steps > 0:
+        fp64_ms, err_mixed = fp64_leg(args, ctx, pkg, C, a, rhs, flush, dev, da_mixed)
 
     # end to end through the reference-facing calls with host (pinned) buffers
-    lib = C.load()
-    nbytes = action_bytes
-    pa = lib.pffrg_host_alloc(nbytes)
-    pd = lib.pffrg_host_alloc(nbytes)
-    import ctypes
-
-    ha = np.frombuffer((ctypes.c_double * lay.size).from_address(pa), dtype=np.float64)
-    hd = np.frombuffer((ctypes.c_double * lay.size).from_address(pd), dtype=np.float64)
-    A_host = pkg.action.Action(a.symmetry, lay.num_sites, lay.num_sigma, lay.num_omega, lay.num_nu, a.S, ha)
-    D_host = pkg.action.Action(a.symmetry, lay.num_sites, lay.num_sigma, lay.num_omega, lay.num_nu, a.S, hd)
-    A_host.buf[:] = a.buf
-    for _ in range(1):
-        D_host.buf[:] = 0.0
-        ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
-        ctx.compute_dgamma(w.Lam, A_host, D_host, EVAL, GAMMA_TOL, loops=w.loops)
-    e2e_times = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize(dev)
-        D_host.buf[:] = 0.0
-        t0 = time.perf_counter()
-        ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
-        ctx.compute_dgamma(w.Lam, A_host, D_host, EVAL, GAMMA_TOL, loops=w.loops)
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_s = float(np.mean(e2e_times))
-    if dist:
-        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_value = world / e2e_s
-    h2d = 4 * action_bytes  # a and da uploaded by each of the two calls
-    d2h = 2 * action_bytes  # da returned by each call
-    lib.pffrg_host_free(pa)
-    lib.pffrg_host_free(pd)
+    e2e = None
+    if not args.no_e2e:
+        e2e = end_to_end(args, ctx, pkg, C, a, w, flush, dev, dist, world)
     ctx.close()
 
     clk = clocks.summary()
@@ -345,7 +303,7 @@ def ours(args):
         return 0
     # CPU baseline (oracle, all host cores, bounded strided sample), rank 0 at N=1 only
     cpu = None
-    if world == 1:
+    if world == 1 and not args.no_cpu:
         O = entry.load_oracle()
         rate, threads, stride, secs, _ = cpu_rhs_rate(O, r, m, a, w, args.cpu_seconds)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
@@ -356,16 +314,16 @@ def ours(args):
         "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 integrand / f64 quadrature bookkeeping", "data": "synthetic",
         "config": config(args, w, {"precision": "mixed", "wall_ms_per_step": t_wall * 1e3 / args.steps}),
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": e2e,
         "gpu_launches": int(round(launches_step * args.steps)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "pass_kernel (channel tasks)", "peak_kind": peak_kind,
+                     "kernel": "quadrature wave kernels of the dΓ passes", "peak_kind": peak_kind,
                      "algorithmic_bytes_per_step": alg_bytes_step, "kernel_ms_per_step": pass_ms_step,
                      "launches_per_step": pass_launches_step},
         "cpu_baseline": cpu,
         "fp64": {"value": 1e3 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
-                 "mixed_speedup": fp64_ms / ms_step},
+                 "mixed_speedup": fp64_ms / ms_step} if fp64_ms else None,
         "mixed_vs_fp64_rel_err": err_mixed,
         "integrand_evals_per_step": evals_step,
         "clocks": clk,
@@ -374,6 +332,71 @@ def ours(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def fp64_leg(args, ctx, pkg, C, a, rhs, flush, dev, da_mixed):
+    """FP64 right-hand sides on the same state: time per step and the mixed path's error."""
+    import torch
+
+    ctx.set_precision("fp64")
+    rhs()
+    ctx.set_timing(True)
+    ctx.read_stats(reset=True)
+    for _ in range(args.fp64_steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        rhs()
+    st64 = ctx.read_stats(reset=True)
+    ctx.set_timing(False)
+    fp64_ms = st64["rhs_ms"] / args.fp64_steps
+    da64 = pkg.action.Action.empty_like(a)
+    ctx.download(C.SLOT_DA, da64)
+    err = float(np.max(np.abs(da_mixed.buf - da64.buf)) / np.max(np.abs(da64.buf)))
+    ctx.set_precision("mixed")
+    return fp64_ms, err
+
+
+def end_to_end(args, ctx, pkg, C, a, w, flush, dev, dist, world):
+    """The same metric through pffrg_dsigma + pffrg_dgamma with host (pinned) buffers."""
+    import ctypes
+
+    import torch
+
+    lay = a.layout
+    action_bytes = lay.size * 8
+    lib = C.load()
+    nbytes = action_bytes
+    pa = lib.pffrg_host_alloc(nbytes)
+    pd = lib.pffrg_host_alloc(nbytes)
+    ha = np.frombuffer((ctypes.c_double * lay.size).from_address(pa), dtype=np.float64)
+    hd = np.frombuffer((ctypes.c_double * lay.size).from_address(pd), dtype=np.float64)
+    A_host = pkg.action.Action(a.symmetry, lay.num_sites, lay.num_sigma, lay.num_omega, lay.num_nu, a.S, ha)
+    D_host = pkg.action.Action(a.symmetry, lay.num_sites, lay.num_sigma, lay.num_omega, lay.num_nu, a.S, hd)
+    A_host.buf[:] = a.buf
+    for _ in range(1):
+        D_host.buf[:] = 0.0
+        ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
+        ctx.compute_dgamma(w.Lam, A_host, D_host, w.eval, GAMMA_TOL, loops=w.loops)
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        D_host.buf[:] = 0.0
+        t0 = time.perf_counter()
+        ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
+        ctx.compute_dgamma(w.Lam, A_host, D_host, w.eval, GAMMA_TOL, loops=w.loops)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_times))
+    if dist:
+        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e_value = world / e2e_s
+    h2d = 4 * action_bytes  # a and da uploaded by each of the two calls
+    d2h = 2 * action_bytes  # da returned by each call
+    lib.pffrg_host_free(pa)
+    lib.pffrg_host_free(pd)
+    return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
 
 def main():

@@ -35,6 +35,7 @@ class Workload:
     bare_on_t: bool = False
     symmetry: str = "su2"
     S: float = 0.5
+    eval: int = 10  # subdomains per integration range (launcher_1l.jl:78 gives 10 at Λ = 1)
 
 
 WORKLOADS = {
@@ -43,6 +44,9 @@ WORKLOADS = {
     # BASELINE configs[1]: pyrochlore L=6 Heisenberg, 2 loop, same meshes, N(0, 0.05) seed 1 + bare J on Ω=0 of ch_t spin
     "pyrochlore-L6-2l": Workload("pyrochlore-L6-2l", "pyrochlore", 6, "heisenberg", [[1.0]], 2, 1.0, 50, 15, 10,
                                  0.05, 1, bare_on_t=True),
+    # the same lattice and state on small meshes (11/4/3 positive frequencies, eval 2, 1 loop): profiling case
+    "pyrochlore-L6-reduced": Workload("pyrochlore-L6-reduced", "pyrochlore", 6, "heisenberg", [[1.0]], 1, 1.0, 11, 4,
+                                      3, 0.05, 1, bare_on_t=True, eval=2),
 }
 
 
