@@ -162,6 +162,35 @@ typedef struct pffrg_stats {
 int pffrg_set_timing(pffrg_ctx* ctx, int on);
 int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset);
 
+/* One-loop dΓ without any device allocation.  This entry point has no
+ * counterpart in the reference.  It is meant for callers that cannot call
+ * cudaMalloc: code running while a CUDA graph is captured (allocation is not
+ * capturable), hosts whose device memory is owned by another framework's pool,
+ * and embedders with a device-memory budget fixed at start-up.
+ *
+ * Computes what pffrg_dgamma(loops = 1) computes in FP64 -- compute_dΓ_1l!'s
+ * boundary corrections, the Katanin bubbles of all channel tasks and the
+ * symmetrisation -- on packed actions already in device memory: a_dev is the
+ * state a, da_dev holds dΣ in its Σ part on entry (from compute_dΣ!) and
+ * receives the vertex derivative (bare entries untouched).  lattice and mesh
+ * are host views as for pffrg_create.  stream: a cudaStream_t (NULL: legacy
+ * default stream); the call returns after the stream has drained.
+ *
+ * All scratch (tables, integration bounds, boundary corrections, adaptive
+ * quadrature workspace) lives in one static device array of
+ * pffrg_noalloc_scratch_bytes() = 128 MiB that every GPU loading this library
+ * holds until the process exits.  Problems needing more return PFFRG_E_LIMIT
+ * with the required size in pffrg_noalloc_last_error() (square L = 3 with the
+ * 50/15/10 default-size meshes at eval <= 10 fits).  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before capturing a stream.  Every call reuses the same
+ * array, so calls whose GPU work overlaps (other streams, other host threads)
+ * race and must be serialised by the caller. */
+int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lattice, const pffrg_mesh_view* mesh, double S, double Lam,
+                            const double* a_dev, double* da_dev, int eval, double atol, double rtol, void* stream);
+int64_t pffrg_noalloc_scratch_bytes(void);
+const char* pffrg_noalloc_last_error(void);
+
 /* Pinned host memory for fast copies (cudaHostAlloc); NULL on failure. */
 void* pffrg_host_alloc(int64_t bytes);
 void pffrg_host_free(void* p);
