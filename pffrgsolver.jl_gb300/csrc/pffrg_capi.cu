@@ -920,6 +920,9 @@ int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, 
     auto rhs = [&](double lam, const double* src) {
         return rhs_dev(ctx, loops, lam, src, K, eval, gatol, grtol, satol, srtol, sigma_corr);
     };
+    // the stage derivative has zero bare couplings, as the reference's a_stage (the 2-loop left
+    // kernels read them); the host-buffer entry points may have staged other values in this slot
+    for (int c = 0; c < L.C; ++c) CK(cudaMemsetAsync(K + L.bare(c), 0, sizeof(double) * L.Ns, ctx->st));
     // launcher_1l.jl:83-116
     CK(cudaMemcpyAsync(N, A, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     CK(cudaMemcpyAsync(E, A, bytes, cudaMemcpyDeviceToDevice, ctx->st));

@@ -1,0 +1,337 @@
+"""launch!: the FRG flow driver above the GPU right-hand side (host side).
+
+Restates src/Launcher/Launcher.jl:565-773 (launch!), the Bogacki-Shampine
+loop of src/Launcher/launcher_{1l,2l,ml}.jl (the four stages and the error
+ratio run on the device through ``pffrg_bs_step``), the parquet warm start of
+src/Launcher/parquet.jl:1-100, and the mesh scan/resampling between steps
+(src/Action/Action.jl:361-527, src/Action/channel.jl:416-471).  Observables
+are handed to ``measure`` callbacks; the HDF5 files of the reference are not
+written by this module.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import action as A
+from . import frequency as F
+from . import lattice as L
+from . import _capi
+from .flow import FlowContext, get_eval
+
+
+# ---------------------------------------------------------------------------
+# interpolation helpers on sorted meshes (param.jl:26-87), vectorised
+# ---------------------------------------------------------------------------
+def params(vals: np.ndarray, x: np.ndarray):
+    """Lower/upper indices and weights of get_param for every value in vals."""
+    vals = np.asarray(vals, dtype=np.float64)
+    n = len(x)
+    hi = np.searchsorted(x, vals, side="left")
+    top = vals >= x[-1]
+    hi = np.where(top, n - 1, hi)
+    hi = np.clip(hi, 0, n - 1)
+    lo = np.where(top, n - 1, np.where(vals < x[hi], hi - 1, hi))
+    lo = np.clip(lo, 0, n - 1)
+    wl = np.ones_like(vals)
+    wu = np.zeros_like(vals)
+    m = lo < hi
+    d = np.where(m, 1.0 / np.where(m, x[hi] - x[lo], 1.0), 0.0)
+    wl = np.where(m, d * (x[hi] - vals), 1.0)
+    wu = np.where(m, d * (vals - x[lo]), 0.0)
+    return lo, hi, wl, wu
+
+
+def get_sigma(w: float, sigma_mesh: np.ndarray, Sig: np.ndarray) -> float:
+    """get_Σ (Action.jl:8-26)."""
+    if abs(w) <= sigma_mesh[-1]:
+        lo, hi, wl, wu = params(np.array([abs(w)]), sigma_mesh)
+        return float(np.sign(w) * (wl[0] * Sig[lo[0]] + wu[0] * Sig[hi[0]]))
+    return float(sigma_mesh[-1] * Sig[-1] / w)
+
+
+# ---------------------------------------------------------------------------
+# mesh scanning (Action.jl:361-449) and resampling (Action.jl:451-527, channel.jl:416-471)
+# ---------------------------------------------------------------------------
+def scan(x, y, p0, p1, p2, p3, p4) -> float:
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    num_lin = int(math.ceil(p0 * (len(x) - 1)))
+    # a) first extremum at finite frequency, δa where the channel has decayed to 75 % of it
+    da = math.inf
+    idx = 0
+    slope = (y[1] - y[0]) / (x[1] - x[0])
+    for i in range(1, len(x) - 1):
+        s = (y[i + 1] - y[i]) / (x[i + 1] - x[i])
+        if np.sign(s) != np.sign(slope):
+            idx = i
+            break
+        slope = s
+    if idx > 0:
+        for i in range(idx + 1, len(x)):
+            if abs(y[i] / y[idx]) <= 0.75:
+                da = max(x[i], num_lin * x[idx] / math.ceil(0.5 * num_lin))
+                break
+    # b) finite value at the origin: p1 < Δ < p2
+    db = num_lin * x[1]
+    if abs(y[0]) / np.max(np.abs(y)) > 1e-2:
+        delta = abs(y[1] - y[0]) / max(abs(y[1]), abs(y[0]))
+        while not (p1 < delta < p2):
+            if delta >= p2:
+                db *= 0.98
+            elif delta <= p1:
+                db *= 1.02
+            if db >= x[-1]:
+                break
+            xp = F.get_mesh(db, x[-1], len(x) - 1, p0)
+            lo, hi, wl, wu = params(xp, x)
+            yp = wl * y[lo] + wu * y[hi]
+            delta = abs(yp[1] - yp[0]) / max(abs(yp[1]), abs(yp[0]))
+    # c) merge and bound
+    return min(max(num_lin * p3, min(da, db)), p4)
+
+
+def scan_channel(Lam, p_O, p_n, Om, nu, q3):
+    """(Ω_lin, ν_lin) of one channel from cuts through its maximum (Action.jl:452-480)."""
+    idx = np.unravel_index(int(np.argmax(np.abs(q3).reshape(-1, order="F"))), q3.shape, order="F")
+    s, w, v, vp = idx
+    cut_O = q3[s, :, v, vp]
+    cut_1 = np.array([q3[s, w, k, k] - q3[s, w, -1, -1] for k in range(len(nu))])
+    cut_2 = q3[s, w, :, vp] - q3[s, w, -1, vp]
+    cut_3 = q3[s, w, v, :] - q3[s, w, v, -1]
+    O_lin = scan(Om, cut_O, p_O[0], p_O[1], p_O[2], p_O[3] * Lam, p_O[4] * Lam)
+    n1 = scan(nu, cut_1, p_n[0], p_n[1], p_n[2], p_n[3] * Lam, p_n[4] * Lam)
+    n2 = scan(nu, cut_2, p_n[0], p_n[1], p_n[2], p_n[3] * Lam, p_n[4] * Lam)
+    n3 = scan(nu, cut_3, p_n[0], p_n[1], p_n[2], p_n[3] * Lam, p_n[4] * Lam)
+    return O_lin, min(n1, n2, n3)
+
+
+def _resample_channel(Om_old, nu_old, ch_old, Om_new, nu_new, ch_new):
+    """Trilinear resampling of one channel (channel.jl:416-471)."""
+    l1, h1, a1, b1 = params(Om_new, Om_old)
+    l2, h2, a2, b2 = params(nu_new, nu_old)
+    q1 = ch_old.q1
+    ch_new.q1[...] = a1[None, :] * q1[:, l1] + b1[None, :] * q1[:, h1]
+    for name in ("q2_1", "q2_2"):
+        q = getattr(ch_old, name)
+        out = (a1[None, :, None] * a2[None, None, :] * q[:, l1][:, :, l2]
+               + b1[None, :, None] * a2[None, None, :] * q[:, h1][:, :, l2]
+               + a1[None, :, None] * b2[None, None, :] * q[:, l1][:, :, h2]
+               + b1[None, :, None] * b2[None, None, :] * q[:, h1][:, :, h2])
+        getattr(ch_new, name)[...] = out
+    q3 = ch_old.q3
+    out = np.zeros_like(ch_new.q3)
+    W1 = (a1, b1)
+    I1 = (l1, h1)
+    W2 = (a2, b2)
+    I2 = (l2, h2)
+    for k3 in range(2):  # corner order of get_q3 (channel.jl:226-242)
+        for k2 in range(2):
+            for k1 in range(2):
+                w = W1[k1][:, None, None] * W2[k2][None, :, None] * W2[k3][None, None, :]
+                out += w[None] * q3[:, I1[k1]][:, :, I2[k2]][:, :, :, I2[k3]]
+    ch_new.q3[...] = out
+
+
+def resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m_old: F.Mesh, a_old: A.Action,
+                     a_new: A.Action, chi=None) -> F.Mesh:
+    """New meshes at cutoff Λ and the action resampled onto them (Action.jl:483-548)."""
+    s_lin = lins[1] * Lam
+    Os_lin = lins[2] * Lam
+    ns_lin = lins[3] * Lam
+    Ot_lin = lins[2] * Lam
+    nt_lin = lins[3] * Lam
+    c_lin = lins[4] * Lam
+    if Lam < lins[0]:
+        s_lin = p_sigma[1] * m_old.sigma[int(np.argmax(np.abs(a_old.Σ)))]
+        Os, ns, Ot, nt = [], [], [], []
+        for v in a_old.Γ:
+            o1, n1 = scan_channel(Lam, p_Os, p_ns, m_old.omega_s, m_old.nu_s, v.ch_s.q3)
+            o2, n2 = scan_channel(Lam, p_Os, p_ns, m_old.omega_s, m_old.nu_s, v.ch_u.q3)
+            Os.append(min(o1, o2))
+            ns.append(min(n1, n2))
+            o3, n3 = scan_channel(Lam, p_Ot, p_nt, m_old.omega_t, m_old.nu_t, v.ch_t.q3)
+            Ot.append(o3)
+            nt.append(n3)
+        Os_lin, ns_lin, Ot_lin, nt_lin = min(Os), min(ns), min(Ot), min(nt)
+        if chi is not None:
+            lst = []
+            for c in chi:
+                row = int(np.unravel_index(int(np.argmax(np.abs(c).reshape(-1, order="F"))), c.shape, order="F")[0])
+                lst.append(scan(m_old.chi, c[row, :], p_chi[0], p_chi[1], p_chi[2], p_chi[3] * Lam, p_chi[4] * Lam))
+            c_lin = min(lst)
+    b = max(Lam, bounds[0])
+    sigma = F.get_mesh(s_lin, bounds[1] * b, m_old.num_sigma - 1, p_sigma[0]) * p_sigma[2]
+    Os_m = F.get_mesh(Os_lin, bounds[2] * b, m_old.num_omega - 1, p_Os[0]) * p_Os[5]
+    ns_m = F.get_mesh(ns_lin, bounds[3] * b, m_old.num_nu - 1, p_ns[0]) * p_ns[5]
+    Ot_m = F.get_mesh(Ot_lin, bounds[2] * b, m_old.num_omega - 1, p_Ot[0]) * p_Ot[5]
+    nt_m = F.get_mesh(nt_lin, bounds[3] * b, m_old.num_nu - 1, p_nt[0]) * p_nt[5]
+    chi_m = F.get_mesh(c_lin, bounds[4] * b, m_old.num_chi - 1, p_chi[0]) * p_chi[5]
+    m_new = F.Mesh(m_old.num_sigma, m_old.num_omega, m_old.num_nu, m_old.num_chi, sigma, Os_m, ns_m, Ot_m, nt_m, chi_m)
+    for k, w in enumerate(m_new.sigma):
+        a_new.Σ[k] = get_sigma(w, m_old.sigma, a_old.Σ)
+    for vo, vn in zip(a_old.Γ, a_new.Γ):
+        _resample_channel(m_old.omega_s, m_old.nu_s, vo.ch_s, m_new.omega_s, m_new.nu_s, vn.ch_s)
+        _resample_channel(m_old.omega_t, m_old.nu_t, vo.ch_t, m_new.omega_t, m_new.nu_t, vn.ch_t)
+        _resample_channel(m_old.omega_s, m_old.nu_s, vo.ch_u, m_new.omega_s, m_new.nu_s, vn.ch_u)
+    return m_new
+
+
+# ---------------------------------------------------------------------------
+# launch!
+# ---------------------------------------------------------------------------
+@dataclass
+class FlowResult:
+    Lam: list = field(default_factory=list)       # accepted cutoffs
+    dLam: list = field(default_factory=list)
+    err: list = field(default_factory=list)
+    abs_max: list = field(default_factory=list)
+    rejected: int = 0
+    rhs_evals: int = 0
+    integrand_evals: int = 0
+    parquet_iterations: int = 0
+    seconds: float = 0.0
+    finished: bool = False
+    reason: str = ""
+    mesh: F.Mesh | None = None
+    action: A.Action | None = None
+
+
+def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep: float = 0.0, S: float = 0.5,
+           euclidean: bool = False, num_sigma: int = 25, num_omega: int = 15, num_nu: int = 10, num_chi: int = 10,
+           p_sigma=F.DEFAULT_P_SIGMA, p_Os=F.DEFAULT_P_OMEGA, p_ns=F.DEFAULT_P_NU, p_Ot=F.DEFAULT_P_OMEGA,
+           p_nt=F.DEFAULT_P_NU, p_chi=F.DEFAULT_P_CHI, lins=F.DEFAULT_LINS, bounds=F.DEFAULT_BOUNDS,
+           max_iter: int = 50, min_eval: int = 10, max_eval: int = 100, sigma_tol=(1e-8, 1e-4),
+           gamma_tol=(1e-8, 1e-4), chi_tol=(1e-8, 1e-4), parquet_tol=(1e-8, 1e-4), ode_tol=(1e-8, 1e-2),
+           loops: int = 1, parquet: bool = True, sigma_corr: bool = True, initial: float = 5.0,
+           final: float = 0.05, bmin: float = 1e-4, bmax: float = 0.1, cps=(), precision: str = "mixed",
+           device: int = 0, measure=None, verbose: bool = False) -> FlowResult:
+    """Run the FRG flow from ``initial`` to ``final`` (launch!, Launcher.jl:565-773).
+
+    ``measure(Λ, dΛ, m, a, ctx)`` is called after every accepted step with the
+    new state (the reference computes χ and writes observables there); it may
+    return False to stop the flow (the reference stops on non-monotone χ).
+    """
+    t0 = time.perf_counter()
+    if symmetry not in A.SYMMETRIES:
+        raise ValueError(f"Symmetry {symmetry} unknown. Valid arguments are su2 and u1-dm.")
+    flat = [float(x) for j in J for x in j] + [float(A_rep)]
+    nrm = math.sqrt(sum(x * x for x in flat))
+    Jn = [[float(x) / nrm for x in j] for j in J]
+    A_n = A_rep / nrm
+    lat = L.get_lattice(name, size, euclidean=euclidean)
+    r = L.get_reduced_lattice(model, Jn, lat)
+    m = F.initial_mesh(initial, num_sigma, num_omega, num_nu, num_chi, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi,
+                       lins, bounds)
+    a = A.get_action_empty(symmetry, r, m, S=S)
+    A.init_action(lat, r, a)
+    A.add_repulsion(A_n, a)
+    res = FlowResult()
+    ctx = FlowContext(r, m, symmetry=symmetry, S=S, precision=precision, device=device)
+    try:
+        if parquet:
+            res.parquet_iterations = launch_parquet(ctx, r, m, a, initial, max_iter, min_eval, max_eval, sigma_tol,
+                                                    gamma_tol, parquet_tol, verbose=verbose)
+        _flow(ctx, r, m, a, res, loops=loops, sigma_corr=sigma_corr and loops >= 3, Li=initial, Lf=final,
+              dLi=bmax * initial, bmin=bmin, bmax=bmax, min_eval=min_eval, max_eval=max_eval, sigma_tol=sigma_tol,
+              gamma_tol=gamma_tol, ode_tol=ode_tol, p=(p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds),
+              cps=list(cps), measure=measure, verbose=verbose)
+    finally:
+        ctx.close()
+    res.seconds = time.perf_counter() - t0
+    return res
+
+
+def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, Lf, dLi, bmin, bmax, min_eval,
+          max_eval, sigma_tol, gamma_tol, ode_tol, p, cps, measure, verbose):
+    """Bogacki-Shampine loop of launch_1l!/2l!/ml! (launcher_1l.jl:56-198) with device stages."""
+    p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds = p
+    Lam, dLam = Li, dLi
+    cps = sorted(set(list(cps) + [Li, Lf]), reverse=True)
+    for c in cps:
+        if c < Lam:
+            dLam = min(dLam, 0.85 * (Lam - c))
+            break
+    ctx.upload(_capi.SLOT_A, a)
+    a_next = A.Action.empty_like(a)
+    a_new = A.Action.empty_like(a)
+    while Lam > Lf:
+        eval_ = get_eval(Lam, min_eval, max_eval)
+        err, amax = ctx.bs_step(Lam, dLam, eval_, loops=loops, gamma_tol=gamma_tol, sigma_tol=sigma_tol,
+                                sigma_corr=sigma_corr, ode_tol=ode_tol)
+        res.rhs_evals += 4
+        res.integrand_evals += ctx.last_integrand_evals
+        if verbose:
+            print(f"Λ = {Lam:.6g}  dΛ = {dLam:.3g}  err = {err:.3g}  Γmax = {amax:.4g}", flush=True)
+        if err >= 10.0:
+            res.reason = "integration has become unstable"
+            break
+
+        def next_dlam(dl):
+            dl = max(bmin, min(bmax * Lam, 0.85 * (1.0 / err) ** (1.0 / 3.0) * dl))
+            lower = [c for c in cps if c - Lam < 0.0]
+            lam_cp = lower[0] if lower else 0.0
+            return min(dl, Lam - lam_cp)
+
+        if err <= 1.0 or dLam <= bmin:
+            Lam -= dLam
+            dLam = next_dlam(dLam)
+            res.Lam.append(Lam)
+            res.dLam.append(dLam)
+            res.err.append(err)
+            res.abs_max.append(amax)
+            ctx.download(_capi.SLOT_NEXT, a_next)
+            if amax >= 1000.0:
+                res.reason = "vertex has diverged"
+                if measure:
+                    measure(Lam, dLam, m, a_next, ctx)
+                break
+            if measure and measure(Lam, dLam, m, a_next, ctx) is False:
+                res.reason = "flowing correlations show non-monotonicity"
+                break
+            # new meshes and resampled state (launcher_1l.jl:177)
+            a_new.buf[:] = a_next.buf
+            m = resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m, a_next, a_new,
+                                 getattr(measure, "chi", None))
+            ctx.set_mesh(m)
+            ctx.upload(_capi.SLOT_A, a_new)
+        else:
+            dLam = next_dlam(dLam)
+            res.rejected += 1
+    else:
+        res.finished = True
+    res.mesh = m
+    res.action = a_new if res.Lam else a
+
+
+def launch_parquet(ctx: FlowContext, r, m, a: A.Action, Lam: float, max_iter: int, min_eval: int, max_eval: int,
+                   sigma_tol, gamma_tol, parquet_tol, beta=None, verbose: bool = False) -> int:
+    """Parquet fixed point of the SDE and the BSEs at cutoff Λ (parquet.jl:1-100); returns iterations."""
+    ap = A.Action.empty_like(a)
+    beta = min(Lam, 1.0) if beta is None else beta
+    eval_ = get_eval(Lam, min_eval, max_eval)
+    gm = a.gamma_mask()
+    q3 = a.q3_mask()
+    abs_err = rel_err = math.inf
+    count = 1
+    while abs_err >= parquet_tol[0] and rel_err >= parquet_tol[1] and count <= max_iter:
+        s_abs = s_rel = math.inf
+        s_count = 1
+        while s_abs >= parquet_tol[0] and s_rel >= parquet_tol[1] and s_count <= max_iter:
+            ctx.compute_sigma_sde(Lam, a, ap, eval_, gamma_tol, sigma_tol)
+            s_abs = float(np.max(np.abs(ap.Σ - a.Σ)))
+            s_rel = s_abs / max(float(np.max(np.abs(a.Σ))), float(np.max(np.abs(ap.Σ))))
+            a.Σ[:] = (1.0 - beta) * a.Σ + beta * ap.Σ
+            s_count += 1
+        ctx.compute_gamma_bse(Lam, a, ap, eval_, gamma_tol)
+        diff = ap.buf[q3] - a.buf[q3]
+        abs_err = float(np.max(np.abs(diff))) if diff.size else 0.0
+        rel_err = abs_err / max(a.abs_max(), ap.abs_max())
+        if verbose:
+            print(f"parquet iteration {count}: rel err {rel_err:.3e}", flush=True)
+        a.buf[gm] = (1.0 - beta) * a.buf[gm] + beta * ap.buf[gm]
+        count += 1
+    return count - 1

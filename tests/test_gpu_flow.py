@@ -1,0 +1,96 @@
+"""The device Bogacki-Shampine step and the launch! driver against the oracle.
+
+The reference step (launcher_1l.jl:83-116) is restated here in numpy on top
+of the oracle's right-hand side; the device step (pffrg_bs_step) must give the
+same 3rd-order solution and error ratio in FP64 (1e-10 relative).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_bs_step(O, P, a, Lam, dLam, loops, eval_, ode_tol=(1e-8, 1e-2)):
+    m = np.zeros(a.buf.size, dtype=bool)
+    m[: a.layout.num_sigma] = True
+    m |= a.gamma_mask()
+    q3 = a.q3_mask()
+
+    def rhs(state, lam):
+        out = np.zeros_like(state)
+        O.dsigma(P, lam, state, out)
+        O.dgamma(P, loops, lam, state, out, eval_, sigma_corr=loops >= 3)
+        return out
+
+    x = a.buf
+    da = x.copy()
+    aerr = x.copy()
+    k = rhs(x, Lam)
+    da[m] += -2.0 * dLam / 9.0 * k[m]
+    aerr[m] += -7.0 * dLam / 24.0 * k[m]
+    inter = x.copy()
+    inter[m] += -0.5 * dLam * k[m]
+    k = rhs(inter, Lam - 0.5 * dLam)
+    da[m] += -1.0 * dLam / 3.0 * k[m]
+    aerr[m] += -1.0 * dLam / 4.0 * k[m]
+    inter = x.copy()
+    inter[m] += -0.75 * dLam * k[m]
+    k = rhs(inter, Lam - 0.75 * dLam)
+    da[m] += -4.0 * dLam / 9.0 * k[m]
+    aerr[m] += -1.0 * dLam / 3.0 * k[m]
+    inter[m] = da[m]
+    k = rhs(inter, Lam - dLam)
+    aerr[m] += -1.0 * dLam / 8.0 * k[m]
+    aerr[m] -= inter[m]
+    delta = np.max(np.abs(aerr[q3]))
+    scale = ode_tol[0] + max(np.max(np.abs(inter[q3])), np.max(np.abs(x[q3]))) * ode_tol[1]
+    return inter, delta / scale
+
+
+@pytest.mark.parametrize("loops", [1, 2])
+def test_bs_step_matches_oracle(pkg, O, loops):
+    import pffrg_gb300._capi as C
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.action import Action
+    from pffrg_gb300.flow import FlowContext
+
+    w = wl.Workload("bs", "square", 3, "heisenberg", [[1.0]], loops, 2.0, 11, 4, 3, 0.05, 31)
+    lat, r, m, a = wl.build_state(w)
+    P = O.Problem(r, m)
+    ref_next, ref_err = oracle_bs_step(O, P, a, 2.0, 0.1, loops, 3)
+    with FlowContext(r, m, precision="fp64") as ctx:
+        ctx.upload(C.SLOT_A, a)
+        err, amax = ctx.bs_step(2.0, 0.1, 3, loops=loops)
+        nxt = Action.empty_like(a)
+        ctx.download(C.SLOT_NEXT, nxt)
+    mask = np.zeros(a.buf.size, dtype=bool)
+    mask[: m.num_sigma] = True
+    mask |= a.gamma_mask()
+    rel = np.max(np.abs(nxt.buf[mask] - ref_next[mask])) / np.max(np.abs(ref_next[mask]))
+    assert rel < 1e-10
+    assert err == pytest.approx(ref_err, rel=1e-9)
+    assert amax == pytest.approx(np.max(np.abs(ref_next[a.q3_mask()])), rel=1e-12)
+
+
+def test_launch_runs_to_final(pkg):
+    from pffrg_gb300.launcher import launch
+
+    seen = []
+
+    def measure(Lam, dLam, m, a, ctx):
+        seen.append(Lam)
+        return True
+
+    res = launch("t", "square", 3, "heisenberg", "su2", [[1.0]], num_sigma=10, num_omega=4, num_nu=3, num_chi=4,
+                 initial=5.0, final=3.0, parquet=False, precision="fp64", measure=measure)
+    assert res.finished and res.Lam[-1] <= 3.0 + 1e-12
+    assert seen == res.Lam and all(np.diff(res.Lam) < 0)
+    assert res.integrand_evals > 0
+
+
+def test_parquet_converges(pkg):
+    from pffrg_gb300.launcher import launch
+
+    res = launch("t", "square", 3, "heisenberg", "su2", [[1.0]], num_sigma=10, num_omega=4, num_nu=3, num_chi=4,
+                 initial=5.0, final=5.0, parquet=True, precision="fp64", parquet_tol=(1e-8, 1e-6))
+    assert 1 <= res.parquet_iterations < 50
