@@ -86,6 +86,8 @@ def lib():
                                  ctypes.c_double]
         L.oracle_sde.argtypes = [P, ctypes.c_double, _f64p, _f64p, _f64p, ctypes.c_int, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.oracle_chi.argtypes = [P, ctypes.c_double, _f64p, _f64p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                 _f64p]
         L.oracle_symmetrize.argtypes = [P, _f64p]
         L.oracle_symmetrize_add_to.argtypes = [P, _f64p, _f64p]
         L.oracle_buffer_kernel.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
@@ -99,6 +101,8 @@ def lib():
         L.oracle_test_quadgk.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double]
         L.oracle_test_quadgk.restype = ctypes.c_double
+        L.oracle_test_hcubature.argtypes = [ctypes.c_int] + [ctypes.c_double] * 6
+        L.oracle_test_hcubature.restype = ctypes.c_double
         L.oracle_last_stats.argtypes = [ctypes.POINTER(Stats)]
         _lib = L
     return _lib
@@ -188,6 +192,18 @@ def bse(P: Problem, Lam: float, a1: np.ndarray, a2: np.ndarray, corrs_buf: np.nd
     _check(lib().oracle_bse(P.ref, Lam, _f(a1), _f(a2), _f(corrs_buf), eval_, gtol[0], gtol[1]), "bse")
 
 
+def chi(P: Problem, Lam: float, a: np.ndarray, chi_mesh: np.ndarray, tol=(1e-8, 1e-4)):
+    """compute_χ!: χ[site, w] on the χ mesh (Fortran-ordered [Ns, num_chi]); for u1-dm the list
+    [χxx, χzz, χxy] of such arrays (correlation_u1_dm.jl:152-190)."""
+    cm = np.ascontiguousarray(chi_mesh, dtype=np.float64)
+    ncomp = 1 if int(P.s.symmetry) == 0 else 3
+    ns = int(P.s.num_sites)
+    out = np.zeros(ncomp * ns * len(cm))
+    _check(lib().oracle_chi(P.ref, Lam, _f(a), _f(cm), len(cm), tol[0], tol[1], _f(out)), "chi")
+    mats = [out[k * ns * len(cm):(k + 1) * ns * len(cm)].reshape((ns, len(cm)), order="F") for k in range(ncomp)]
+    return mats[0] if ncomp == 1 else mats
+
+
 def symmetrize(P: Problem, a: np.ndarray) -> None:
     _check(lib().oracle_symmetrize(P.ref, _f(a)), "symmetrize")
 
@@ -228,3 +244,7 @@ def test_quadgk(power: int, a: float, b: float, atol: float, rtol: float) -> flo
 
 def num_threads() -> int:
     return os.cpu_count() or 1
+
+
+def test_hcubature(which: int, x0: float, x1: float, y0: float, y1: float, atol: float, rtol: float) -> float:
+    return float(lib().oracle_test_hcubature(which, x0, x1, y0, y1, atol, rtol))

@@ -342,6 +342,30 @@ inline double flags_su2(const Buf& b, int comp) {
     return sgn;
 }
 
+// apply_flags_u1_dm (action_u1_dm.jl:80-118), 0-based components xx, zz, DM, dd, zd, dz:
+// the sign of the contribution and the component actually read
+inline double flags_u1dm(const Buf& b, int comp, int& src) {
+    double sgn = 1.0;
+    if ((comp == 4 || comp == 5) && b.sgn_mn) sgn = -sgn;
+    if ((comp == 3 || comp == 5) && b.sgn_m) sgn = -sgn;
+    if ((comp == 3 || comp == 4) && b.sgn_n) sgn = -sgn;
+    src = comp;
+    if (b.exch) {
+        if (comp == 2) sgn = -sgn;
+        else if (comp == 4) src = 5;
+        else if (comp == 5) src = 4;
+    }
+    return sgn;
+}
+
+inline double apply_flags(const Prob& P, const Buf& b, int comp, int& src) {
+    if (P.p->symmetry == 0) {
+        src = comp;
+        return flags_su2(b, comp);
+    }
+    return flags_u1dm(b, comp, src);
+}
+
 enum { CH_S = 1, CH_T = 2, CH_U = 4 };
 
 // get_Γ_comp_avx! for every component (action_su2.jl:115-134); temp[c*Ns + i]
@@ -351,17 +375,18 @@ inline void gather_slot(const Prob& P, const Act& A, const Buf& bs, const Buf& b
     for (int c = 0; c < d.C; ++c) {
         double* t = temp + (int64_t)c * d.Ns;
         for (int i = 0; i < nsites; ++i) t[i] = A.bare[c][i];
+        int src;
         if (mask & CH_S) {
-            double sg = flags_su2(bs, c);
-            interp_add(P, A.q[c][bs.map ? 2 : 0], bs, sg, t, nsites);
+            double sg = apply_flags(P, bs, c, src);
+            interp_add(P, A.q[src][bs.map ? 2 : 0], bs, sg, t, nsites);
         }
         if (mask & CH_T) {
-            double sg = flags_su2(bt, c);
-            interp_add(P, A.q[c][1], bt, sg, t, nsites);
+            double sg = apply_flags(P, bt, c, src);
+            interp_add(P, A.q[src][1], bt, sg, t, nsites);
         }
         if (mask & CH_U) {
-            double sg = flags_su2(bu, c);
-            interp_add(P, A.q[c][bu.map ? 0 : 2], bu, sg, t, nsites);
+            double sg = apply_flags(P, bu, c, src);
+            interp_add(P, A.q[src][bu.map ? 0 : 2], bu, sg, t, nsites);
         }
     }
 }
@@ -417,9 +442,19 @@ inline double gamma_comp_site(const Prob& P, const Act& A, int comp, int site, c
         }
         return sg * v;
     };
-    if (mask & CH_S) val += one(A.q[comp][bs.map ? 2 : 0], bs, flags_su2(bs, comp));
-    if (mask & CH_T) val += one(A.q[comp][1], bt, flags_su2(bt, comp));
-    if (mask & CH_U) val += one(A.q[comp][bu.map ? 0 : 2], bu, flags_su2(bu, comp));
+    int src;
+    if (mask & CH_S) {
+        const double sg = apply_flags(P, bs, comp, src);
+        val += one(A.q[src][bs.map ? 2 : 0], bs, sg);
+    }
+    if (mask & CH_T) {
+        const double sg = apply_flags(P, bt, comp, src);
+        val += one(A.q[src][1], bt, sg);
+    }
+    if (mask & CH_U) {
+        const double sg = apply_flags(P, bu, comp, src);
+        val += one(A.q[src][bu.map ? 0 : 2], bu, sg);
+    }
     return val;
 }
 
@@ -435,6 +470,7 @@ struct PassDesc {
     int mask[4];
     const double* a;   // propagator action
     const double* da;  // Katanin dΣ source
+    bool reduced = false;  // reduced s bubble of the SDE: u1-dm writes xx, zz, dd only (SDE_u1_dm.jl:2-56)
 };
 
 struct Ctx {
@@ -501,6 +537,67 @@ inline double node_prop(const Prob& P, const PassDesc& pd, double L, double v, d
     return -prop_plain(m, Sig, L, v - 0.5 * W, v + 0.5 * W);
 }
 
+// u1-dm vertex components at one site, in the reference's order xx, zz, DM, dd, zd, dz
+struct V6 {
+    double xx, zz, dm, dd, zd, dz;
+};
+
+inline V6 v6_at(const double* t, int Ns, int i) {
+    return V6{t[i], t[Ns + i], t[2 * Ns + i], t[3 * Ns + i], t[4 * Ns + i], t[5 * Ns + i]};
+}
+
+// s-channel bubble of two u1-dm vertices (flow_u1_dm_s.jl:53-58, the same in the left, central,
+// BSE and reduced kernels)
+inline void comb_s_u1dm(const V6& a, const V6& b, double g[6]) {
+    g[0] = a.dm * b.dz - a.dm * b.zd + a.xx * b.dd + a.dd * b.xx - a.xx * b.zz - a.dz * b.dm + a.zd * b.dm - a.zz * b.xx;
+    g[1] = a.zz * b.dd + a.dd * b.zz - a.dz * b.zd - 2.0 * a.xx * b.xx - 2.0 * a.dm * b.dm - a.zd * b.dz;
+    g[2] = a.dd * b.dm + a.dm * b.dd - a.zd * b.xx - a.xx * b.dz - a.zz * b.dm + a.xx * b.zd - a.dm * b.zz + a.dz * b.xx;
+    g[3] = -a.dz * b.dz + 2.0 * a.xx * b.xx + a.dd * b.dd + 2.0 * a.dm * b.dm - a.zd * b.zd + a.zz * b.zz;
+    g[4] = a.zd * b.dd + a.dd * b.zd - 2.0 * a.dm * b.xx + a.dz * b.zz + a.zz * b.dz + 2.0 * a.xx * b.dm;
+    g[5] = a.zd * b.zz + a.dd * b.dz + a.zz * b.zd + 2.0 * a.dm * b.xx + a.dz * b.dd - 2.0 * a.xx * b.dm;
+}
+
+// u-channel bubble (flow_u1_dm_u.jl:52-57)
+inline void comb_u_u1dm(const V6& a, const V6& b, double g[6]) {
+    g[0] = -a.dm * b.dz - a.dm * b.zd + a.xx * b.dd + a.dd * b.xx + a.xx * b.zz + a.dz * b.dm + a.zd * b.dm + a.zz * b.xx;
+    g[1] = a.zz * b.dd + a.dd * b.zz - a.dz * b.zd + 2.0 * a.xx * b.xx + 2.0 * a.dm * b.dm - a.zd * b.dz;
+    g[2] = a.dd * b.dm + a.dm * b.dd - a.zd * b.xx + a.xx * b.dz + a.zz * b.dm + a.xx * b.zd + a.dm * b.zz - a.dz * b.xx;
+    g[3] = -a.dz * b.dz + 2.0 * a.xx * b.xx + a.dd * b.dd + 2.0 * a.dm * b.dm - a.zd * b.zd + a.zz * b.zz;
+    g[4] = a.zd * b.dd + a.dd * b.zd - 2.0 * a.dm * b.xx + a.dz * b.zz + a.zz * b.dz + 2.0 * a.xx * b.dm;
+    g[5] = a.zd * b.zz + a.dd * b.dz + a.zz * b.zd - 2.0 * a.dm * b.xx + a.dz * b.dd + 2.0 * a.xx * b.dm;
+}
+
+// t-channel local part: non-local vertices v1 (left), v2 (right) at site i with the local
+// vertices v3 (left), v4 (right) at site 1 (flow_u1_dm_t.jl:68-84)
+inline void comb_t_u1dm(const V6& v1, const V6& v2, const V6& v3, const V6& v4, double g[6]) {
+    g[0] = v1.dm * v4.dz - v1.dm * v4.zd + v1.xx * v4.dd - v1.xx * v4.zz + v3.dd * v2.xx + v3.dz * v2.dm -
+           v3.zd * v2.dm - v3.zz * v2.xx;
+    g[1] = v1.zz * v4.dd + 2.0 * v1.zd * v4.dm - v1.zd * v4.zd + v1.zz * v4.zz - 2.0 * v1.zz * v4.xx - v1.zd * v4.dz -
+           2.0 * v3.dm * v2.dz - v3.dz * v2.dz + v3.dd * v2.zz - 2.0 * v3.xx * v2.zz + v3.zz * v2.zz - v3.zd * v2.dz;
+    g[2] = v1.dm * v4.dd - v1.xx * v4.dz + v1.xx * v4.zd - v1.dm * v4.zz - v3.dz * v2.xx + v3.dd * v2.dm +
+           v3.zd * v2.xx - v3.zz * v2.dm;
+    g[3] = -v1.dz * v4.dz + 2.0 * v1.dd * v4.xx + v1.dd * v4.zz - v1.dz * v4.zd - 2.0 * v1.dz * v4.dm + v1.dd * v4.dd +
+           2.0 * v3.dm * v2.zd + 2.0 * v3.xx * v2.dd + v3.zz * v2.dd - v3.dz * v2.zd + v3.dd * v2.dd - v3.zd * v2.zd;
+    g[4] = v1.zd * v4.zz + v1.zd * v4.dd + 2.0 * v1.zd * v4.xx + v1.zz * v4.zd + 2.0 * v1.zz * v4.dm + v1.zz * v4.dz +
+           v3.zd * v2.dd + 2.0 * v3.dm * v2.dd + v3.dd * v2.zd + v3.zz * v2.zd - 2.0 * v3.xx * v2.zd + v3.dz * v2.dd;
+    g[5] = -2.0 * v1.dd * v4.dm + v1.dd * v4.zd + v1.dd * v4.dz + v1.dz * v4.zz + v1.dz * v4.dd - 2.0 * v1.dz * v4.xx +
+           v3.zd * v2.zz + 2.0 * v3.xx * v2.dz + v3.dd * v2.dz + v3.dz * v2.zz - 2.0 * v3.dm * v2.zz + v3.zz * v2.dz;
+}
+
+// t-channel overlap term of one (a, b) row (flow_u1_dm_t.jl:104-109), without the factor -p (-2) m
+inline void comb_t_overlap_u1dm(const V6& v1, const V6& v2, double g[6]) {
+    g[0] = v1.xx * v2.xx - v1.dm * v2.dm;
+    g[1] = v1.zz * v2.zz - v1.zd * v2.dz;
+    g[2] = v1.dm * v2.xx + v1.xx * v2.dm;
+    g[3] = v1.dd * v2.dd - v1.dz * v2.zd;
+    g[4] = v1.zd * v2.dd + v1.zz * v2.zd;
+    g[5] = v1.dd * v2.dz + v1.dz * v2.zz;
+}
+
+struct Args3;
+void integrand_u1dm(const Ctx& cx, double p, const Args3 ar[4][3], const double* t1, const double* t2, double* buff,
+                    double dv);
+
 // buff layout: buff[c*Ns + i]; adds dv * Γ(v) for all sites
 void integrand(const Ctx& cx, double* buff, double v, double dv) {
     const Prob& P = *cx.P;
@@ -520,6 +617,10 @@ void integrand(const Ctx& cx, double* buff, double v, double dv) {
         Buf bt = buffer_t(m, ar[slot][1].w, ar[slot][1].v, ar[slot][1].vp);
         Buf bu = buffer_u(m, ar[slot][2].w, ar[slot][2].v, ar[slot][2].vp);
         gather_slot(P, cx.A[slot], bs, bt, bu, pd.mask[slot], slot == 0 ? t1 : t2, Ns);
+    }
+    if (P.p->symmetry == 1) {
+        integrand_u1dm(cx, p, ar, t1, t2, buff, dv);
+        return;
     }
     if (pd.ch == 0 || pd.ch == 2) {
         const double two = (pd.ch == 0) ? -2.0 : 2.0;
@@ -558,6 +659,52 @@ void integrand(const Ctx& cx, double* buff, double v, double dv) {
         g_stats.overlap_terms += P.ov_off[i + 1] - P.ov_off[i];
         buff[i] += dv * Gs;
         buff[Ns + i] += dv * Gd;
+    }
+}
+
+// the u1-dm bubbles (flow_u1_dm_{s,t,u}.jl, BSE_u1_dm_*.jl, SDE_u1_dm.jl:2-56)
+void integrand_u1dm(const Ctx& cx, double p, const Args3 ar[4][3], const double* t1, const double* t2, double* buff,
+                    double dv) {
+    const Prob& P = *cx.P;
+    const PassDesc& pd = *cx.pd;
+    const oracle_problem* m = P.p;
+    const int Ns = P.d.Ns;
+    double g[6];
+    if (pd.ch == 0 || pd.ch == 2) {
+        for (int i = 0; i < Ns; ++i) {
+            const V6 a = v6_at(t1, Ns, i), b = v6_at(t2, Ns, i);
+            if (pd.ch == 0) comb_s_u1dm(a, b, g);
+            else comb_u_u1dm(a, b, g);
+            for (int c = 0; c < 6; ++c) {
+                if (pd.reduced && (c == 2 || c == 4 || c == 5)) continue;
+                buff[c * Ns + i] += dv * (-p * g[c]);
+            }
+        }
+        return;
+    }
+    double v34[2][6];
+    for (int slot = 2; slot < 4; ++slot) {
+        Buf bs = buffer_s(m, ar[slot][0].w, ar[slot][0].v, ar[slot][0].vp);
+        Buf bt = buffer_t(m, ar[slot][1].w, ar[slot][1].v, ar[slot][1].vp);
+        Buf bu = buffer_u(m, ar[slot][2].w, ar[slot][2].v, ar[slot][2].vp);
+        for (int c = 0; c < 6; ++c) v34[slot - 2][c] = gamma_comp_site(P, cx.A[slot], c, 0, bs, bt, bu, pd.mask[slot]);
+    }
+    const V6 v3{v34[0][0], v34[0][1], v34[0][2], v34[0][3], v34[0][4], v34[0][5]};
+    const V6 v4{v34[1][0], v34[1][1], v34[1][2], v34[1][3], v34[1][4], v34[1][5]};
+    for (int i = 0; i < Ns; ++i) {
+        const V6 v1 = v6_at(t1, Ns, i), v2 = v6_at(t2, Ns, i);
+        comb_t_u1dm(v1, v2, v3, v4, g);
+        double G[6];
+        for (int c = 0; c < 6; ++c) G[c] = -p * g[c];
+        for (int64_t j = P.ov_off[i]; j < P.ov_off[i + 1]; ++j) {
+            const V6 a = v6_at(t1, Ns, P.ov_a[j]), b = v6_at(t2, Ns, P.ov_b[j]);
+            double h[6];
+            comb_t_overlap_u1dm(a, b, h);
+            const double mm = -p * (-2.0) * P.ov_m[j];
+            for (int c = 0; c < 6; ++c) G[c] += mm * h[c];
+        }
+        g_stats.overlap_terms += P.ov_off[i + 1] - P.ov_off[i];
+        for (int c = 0; c < 6; ++c) buff[c * Ns + i] += dv * G[c];
     }
 }
 
@@ -898,40 +1045,68 @@ void run_pass(const Prob& P, const PassDesc base[3], double L, bool full, const 
     for (int k = 0; k < 24; ++k) g_stats.level_hist[k] += total.level_hist[k];
 }
 
-// symmetrize! (action_su2.jl:141-173)
+// image of (comp, channel) under v <-> v' exchange: the component it is read from and the sign
+// (su2: action_su2.jl:141-251, the same component with sign +; u1-dm: action_u1_dm.jl:170-339,
+// s and t: DM -> -DM, zd -> -dz, dz -> -zd; u: zd -> -zd, dz -> -dz)
+inline void swap_image(const Prob& P, int c, int ch, int& src, double& sgn) {
+    src = c;
+    sgn = 1.0;
+    if (P.p->symmetry == 0) return;
+    if (ch == 2) {
+        if (c == 4 || c == 5) sgn = -1.0;
+        return;
+    }
+    if (c == 2) sgn = -1.0;
+    else if (c == 4) { src = 5; sgn = -1.0; }
+    else if (c == 5) { src = 4; sgn = -1.0; }
+}
+
+// symmetrize! (action_su2.jl:141-173, action_u1_dm.jl:170-214)
 void symmetrize(const Prob& P, double* a) {
     const Dims& d = P.d;
     const int Ns = d.Ns, NO = d.NO, Nn = d.Nn;
+    // the reference writes component by component in place; for u1-dm, zd and dz of the s and t
+    // channels read each other's lower triangle, which neither write touches
     for (int c = 0; c < d.C; ++c) {
         for (int ch = 0; ch < 3; ++ch) {
+            int sc;
+            double sg;
+            swap_image(P, c, ch, sc, sg);
             double* q3 = a + d.Nsig + c * d.comp + d.Ns + ch * d.chan + d.K1 + 2 * d.K2;
+            const double* s3 = a + d.Nsig + sc * d.comp + d.Ns + ch * d.chan + d.K1 + 2 * d.K2;
             for (int v = 0; v < Nn; ++v)
                 for (int vp = v + 1; vp < Nn; ++vp)
                     for (int w = 0; w < NO; ++w)
                         for (int i = 0; i < Ns; ++i) {
                             int src = (ch == 2) ? i : P.exch[i];
                             q3[i + (int64_t)Ns * (w + (int64_t)NO * (v + (int64_t)Nn * vp))] =
-                                q3[src + (int64_t)Ns * (w + (int64_t)NO * (vp + (int64_t)Nn * v))];
+                                sg * s3[src + (int64_t)Ns * (w + (int64_t)NO * (vp + (int64_t)Nn * v))];
                         }
         }
     }
 }
 
-// symmetrize_add_to! (action_su2.jl:176-251): a += a_l + (v <-> v') image of a_l
+// symmetrize_add_to! (action_su2.jl:176-251, action_u1_dm.jl:217-340): a += a_l + (v <-> v') image of a_l
 void symmetrize_add_to(const Prob& P, const double* al, double* a) {
     const Dims& d = P.d;
     const int Ns = d.Ns, NO = d.NO, Nn = d.Nn;
     for (int c = 0; c < d.C; ++c) {
         for (int ch = 0; ch < 3; ++ch) {
+            int sc;
+            double sg;
+            swap_image(P, c, ch, sc, sg);
             const int64_t off = d.Nsig + c * d.comp + d.Ns + ch * d.chan;
             const double* l1 = al + off;
+            const double* m1 = al + d.Nsig + sc * d.comp + d.Ns + ch * d.chan;  // the image's component
             double* o1 = a + off;
             auto ex = [&](int i) { return ch == 2 ? i : P.exch[i]; };
             for (int w = 0; w < NO; ++w)
                 for (int i = 0; i < Ns; ++i)
-                    o1[i + (int64_t)Ns * w] += l1[i + (int64_t)Ns * w] + l1[ex(i) + (int64_t)Ns * w];
+                    o1[i + (int64_t)Ns * w] += l1[i + (int64_t)Ns * w] + sg * m1[ex(i) + (int64_t)Ns * w];
             const double* l21 = l1 + d.K1;
             const double* l22 = l1 + d.K1 + d.K2;
+            const double* m21 = m1 + d.K1;
+            const double* m22 = m1 + d.K1 + d.K2;
             double* o21 = o1 + d.K1;
             double* o22 = o1 + d.K1 + d.K2;
             for (int v = 0; v < Nn; ++v)
@@ -939,10 +1114,11 @@ void symmetrize_add_to(const Prob& P, const double* al, double* a) {
                     for (int i = 0; i < Ns; ++i) {
                         int64_t k = i + (int64_t)Ns * (w + (int64_t)NO * v);
                         int64_t ke = ex(i) + (int64_t)Ns * (w + (int64_t)NO * v);
-                        o21[k] += l21[k] + l22[ke];
-                        o22[k] += l22[k] + l21[ke];
+                        o21[k] += l21[k] + sg * m22[ke];
+                        o22[k] += l22[k] + sg * m21[ke];
                     }
             const double* l3 = l1 + d.K1 + 2 * d.K2;
+            const double* m3 = m1 + d.K1 + 2 * d.K2;
             double* o3 = o1 + d.K1 + 2 * d.K2;
             for (int vp = 0; vp < Nn; ++vp)
                 for (int v = 0; v < Nn; ++v)
@@ -950,7 +1126,7 @@ void symmetrize_add_to(const Prob& P, const double* al, double* a) {
                         for (int i = 0; i < Ns; ++i) {
                             int64_t k = i + (int64_t)Ns * (w + (int64_t)NO * (v + (int64_t)Nn * vp));
                             int64_t ke = ex(i) + (int64_t)Ns * (w + (int64_t)NO * (vp + (int64_t)Nn * v));
-                            o3[k] += l3[k] + l3[ke];
+                            o3[k] += l3[k] + sg * m3[ke];
                         }
         }
     }
@@ -1055,9 +1231,18 @@ double sigma_kernel(const Prob& P, SigmaKind kind, double L, double w, double v,
         }
     }
     Act A = make_act(d, src);
-    double val = 3.0 * gamma_comp_site(P, A, 0, 0, b2s, b2t, b2u, m_loc) + gamma_comp_site(P, A, 1, 0, b2s, b2t, b2u, m_loc);
-    for (int j = 0; j < d.Ns; ++j)
-        val -= 2.0 * P.mult[j] * (2.0 * P.S) * gamma_comp_site(P, A, 1, j, b1s, b1t, b1u, m_non);
+    double val;
+    if (P.p->symmetry == 0) {
+        val = 3.0 * gamma_comp_site(P, A, 0, 0, b2s, b2t, b2u, m_loc) + gamma_comp_site(P, A, 1, 0, b2s, b2t, b2u, m_loc);
+        for (int j = 0; j < d.Ns; ++j)
+            val -= 2.0 * P.mult[j] * (2.0 * P.S) * gamma_comp_site(P, A, 1, j, b1s, b1t, b1u, m_non);
+    } else {
+        // flow_u1_dm_self.jl:2-33, SDE_u1_dm.jl:59-91: 2 Γxx + Γzz + Γdd on site 1, Γdd over the lattice
+        val = 2.0 * gamma_comp_site(P, A, 0, 0, b2s, b2t, b2u, m_loc) + gamma_comp_site(P, A, 1, 0, b2s, b2t, b2u, m_loc) +
+              gamma_comp_site(P, A, 3, 0, b2s, b2t, b2u, m_loc);
+        for (int j = 0; j < d.Ns; ++j)
+            val -= 2.0 * P.mult[j] * gamma_comp_site(P, A, 3, j, b1s, b1t, b1u, m_non);
+    }
     switch (kind) {
         case SIG_FLOW: val *= S_single(m, a, L, v) / (2.0 * kPi); break;
         case SIG_CORR1: val *= -G_full(m, a, L, v) / (2.0 * kPi); break;
@@ -1088,6 +1273,233 @@ void sigma_integrals(const Prob& P, SigmaKind kind, double L, const double* a, c
     }
     g_stats = saved;
     g_stats.sigma_evals += evals;
+}
+
+
+// ---------------------------------------------------------------------------
+// correlations χ (src/Observable/correlation_lib/correlation_lib.jl:2-30,
+// correlation_su2.jl:14-87).  The reference integrates with Cubature.jl
+// (compat 1.5, wrapping S. G. Johnson's "cubature" library, not part of the
+// reference tree): hcubature_v, h-adaptive, Genz-Malik degree-7/5 rule for
+// dim = 2, split along the dimension with the largest fourth difference, and
+// the vectorised ("parallel") refinement that bisects, per round, every
+// largest-error region needed to bring the remaining error under the bound.
+// ---------------------------------------------------------------------------
+struct Region2 {
+    double c[2], h[2], vol, val, err;
+    int split;
+    bool operator<(const Region2& o) const { return err < o.err; }
+};
+
+constexpr double kGML2 = 0.3585685828003180919906451539079374954541;  // sqrt(9/70)
+constexpr double kGML4 = 0.9486832980505137995996680633298155601160;  // sqrt(9/10)
+constexpr double kGML5 = 0.6882472016116852977216287342936235251269;  // sqrt(9/19)
+
+// the 17 Genz-Malik points of a 2-D region in the library's order
+inline void gm_points(const Region2& R, double pts[17][2]) {
+    int k = 0;
+    pts[k][0] = R.c[0];
+    pts[k][1] = R.c[1];
+    ++k;
+    for (int d = 0; d < 2; ++d) {
+        const double w2 = R.h[d] * kGML2, w4 = R.h[d] * kGML4;
+        const double off[4] = {-w2, w2, -w4, w4};
+        for (int q = 0; q < 4; ++q) {
+            pts[k][0] = R.c[0];
+            pts[k][1] = R.c[1];
+            pts[k][d] = R.c[d] + off[q];
+            ++k;
+        }
+    }
+    const double a = R.h[0] * kGML4, b = R.h[1] * kGML4;
+    const double rr[4][2] = {{-a, -b}, {a, -b}, {a, b}, {-a, b}};
+    for (int q = 0; q < 4; ++q) {
+        pts[k][0] = R.c[0] + rr[q][0];
+        pts[k][1] = R.c[1] + rr[q][1];
+        ++k;
+    }
+    const double a5 = R.h[0] * kGML5, b5 = R.h[1] * kGML5;
+    const double cs[4][2] = {{a5, b5}, {-a5, b5}, {-a5, -b5}, {a5, -b5}};
+    for (int q = 0; q < 4; ++q) {
+        pts[k][0] = R.c[0] + cs[q][0];
+        pts[k][1] = R.c[1] + cs[q][1];
+        ++k;
+    }
+}
+
+// rule75genzmalik_evalError for dim = 2
+inline void gm_eval(Region2& R, const double* v) {
+    const double n = 2.0;
+    const double w1 = (12824.0 - 9120.0 * n + 400.0 * n * n) / 19683.0;
+    const double w2 = 980.0 / 6561.0;
+    const double w3 = (1820.0 - 400.0 * n) / 19683.0;
+    const double w4 = 200.0 / 19683.0;
+    const double w5 = 6859.0 / 19683.0 / 4.0;
+    const double e1 = (729.0 - 950.0 * n + 50.0 * n * n) / 729.0;
+    const double e2 = 245.0 / 486.0;
+    const double e3 = (265.0 - 100.0 * n) / 1458.0;
+    const double e4 = 25.0 / 729.0;
+    const double ratio = (kGML2 * kGML2) / (kGML4 * kGML4);
+    const double val0 = v[0];
+    double sum2 = 0.0, sum3 = 0.0, diff[2];
+    for (int d = 0; d < 2; ++d) {
+        const double v0 = v[1 + 4 * d], v1 = v[2 + 4 * d], v2 = v[3 + 4 * d], v3 = v[4 + 4 * d];
+        sum2 += v0 + v1;
+        sum3 += v2 + v3;
+        diff[d] = std::fabs(v0 + v1 - 2 * val0 - ratio * (v2 + v3 - 2 * val0));
+    }
+    double sum4 = 0.0, sum5 = 0.0;
+    for (int q = 0; q < 4; ++q) sum4 += v[9 + q];
+    for (int q = 0; q < 4; ++q) sum5 += v[13 + q];
+    const double result = R.vol * (w1 * val0 + w2 * sum2 + w3 * sum3 + w4 * sum4 + w5 * sum5);
+    const double res5 = R.vol * (e1 * val0 + e2 * sum2 + e3 * sum3 + e4 * sum4);
+    R.val = result;
+    R.err = std::fabs(res5 - result);
+    R.split = diff[1] > diff[0] ? 1 : 0;
+}
+
+template <class F>
+double hcubature2(F& f, const double xmin[2], const double xmax[2], double abstol, double reltol,
+                  long long maxevals) {
+    auto eval = [&](Region2& R) {
+        double pts[17][2], v[17];
+        gm_points(R, pts);
+        for (int k = 0; k < 17; ++k) v[k] = f(pts[k][0], pts[k][1]);
+        gm_eval(R, v);
+    };
+    auto converged = [&](double err, double val) { return !(err > abstol && err > std::fabs(val) * reltol); };
+    Region2 R0;
+    for (int d = 0; d < 2; ++d) {
+        R0.c[d] = 0.5 * (xmin[d] + xmax[d]);
+        R0.h[d] = 0.5 * (xmax[d] - xmin[d]);
+    }
+    R0.vol = (2.0 * R0.h[0]) * (2.0 * R0.h[1]);
+    eval(R0);
+    std::priority_queue<Region2> heap;
+    heap.push(R0);
+    double tot_val = R0.val, tot_err = R0.err;
+    long long numeval = 17;
+    while (numeval < maxevals) {
+        if (converged(tot_err, tot_val)) break;
+        // the round's bound compares the remaining error with the total value at its start
+        double ee_err = tot_err;
+        const double ee_val = tot_val;
+        std::vector<Region2> Rs;
+        do {
+            Region2 R = heap.top();
+            heap.pop();
+            tot_val -= R.val;
+            tot_err -= R.err;
+            ee_err -= R.err;
+            // cut_region: halve along the split dimension
+            const int d = R.split;
+            Region2 R2 = R;
+            R.h[d] *= 0.5;
+            R.vol *= 0.5;
+            R2.h[d] = R.h[d];
+            R2.vol = (2.0 * R2.h[0]) * (2.0 * R2.h[1]);
+            R.c[d] -= R.h[d];
+            R2.c[d] += R.h[d];
+            Rs.push_back(R);
+            Rs.push_back(R2);
+            numeval += 34;
+            if (converged(ee_err, ee_val)) break;
+        } while (!heap.empty() && numeval < maxevals);
+        for (Region2& R : Rs) {
+            eval(R);
+            heap.push(R);
+            tot_val += R.val;
+            tot_err += R.err;
+        }
+    }
+    double I = 0.0;
+    while (!heap.empty()) {
+        I += heap.top().val;
+        heap.pop();
+    }
+    return I;
+}
+
+// integrate_χ_boxes (correlation_lib.jl:2-30): nine boxes of [0,1]^2 around the image of ±width
+template <class F>
+double chi_boxes(F& f, double width, double abstol, double reltol) {
+    const double wp = (width - 2.0 + std::sqrt(width * width + 4.0)) / (2.0 * width);
+    const double s = std::fabs(wp - 0.5);
+    const double lo[3] = {0.0, 0.5 - s, 0.5 + s}, hi[3] = {0.5 - s, 0.5 + s, 1.0};
+    // the reference's order: top line (y high), middle, bottom
+    const int rows[3] = {2, 1, 0};
+    double I = 0.0;
+    bool first = true;
+    for (int rr = 0; rr < 3; ++rr) {
+        for (int cc = 0; cc < 3; ++cc) {
+            const double xmin[2] = {lo[cc], lo[rows[rr]]}, xmax[2] = {hi[cc], hi[rows[rr]]};
+            const double v = hcubature2(f, xmin, xmax, abstol, reltol, 10000000LL);
+            if (first) { I = v; first = false; }
+            else I += v;
+        }
+    }
+    return I;
+}
+
+// compute_χ_kernel! (correlation_su2.jl:14-55) at (x, y) in [0,1]^2
+double chi_kernel(const Prob& P, const Act& A, const double* Sig, double L, int site, double w, double x, double y) {
+    const oracle_problem* m = P.p;
+    const double v = (2.0 * x - 1.0) / ((1.0 - x) * x);
+    const double vp = (2.0 * y - 1.0) / ((1.0 - y) * y);
+    const double dv = (2.0 * x * x - 2.0 * x + 1) / ((1.0 - x) * (1.0 - x) * x * x);
+    const double dvp = (2.0 * y * y - 2.0 * y + 1) / ((1.0 - y) * (1.0 - y) * y * y);
+    Buf bs1 = buffer_s(m, v + vp, 0.5 * (v - w - vp), 0.5 * (-v - w + vp));
+    Buf bt1 = buffer_t(m, w, v, vp);
+    Buf bu1 = buffer_u(m, v - vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp));
+    const double twoS = 2.0 * P.S;
+    const double tp2 = (2.0 * kPi) * (2.0 * kPi);
+    double val = -(twoS * twoS) * gamma_comp_site(P, A, 0, site, bs1, bt1, bu1, ALL) / tp2;
+    if (site == 0) {
+        Buf bs2 = buffer_s(m, v + vp, 0.5 * (v - w - vp), 0.5 * (v + w - vp));
+        Buf bt2 = buffer_t(m, -v + vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp));
+        Buf bu2 = buffer_u(m, -w, v, vp);
+        const double vs = gamma_comp_site(P, A, 0, site, bs2, bt2, bu2, ALL);
+        const double vd = gamma_comp_site(P, A, 1, site, bs2, bt2, bu2, ALL);
+        val -= twoS * (vs - vd) / (2.0 * tp2);
+    }
+    val *= G_full(m, Sig, L, v - 0.5 * w) * G_full(m, Sig, L, v + 0.5 * w) * dv;
+    val *= G_full(m, Sig, L, vp - 0.5 * w) * G_full(m, Sig, L, vp + 0.5 * w) * dvp;
+    return val;
+}
+
+// compute_χ_kernel_{xx,zz,xy}! (correlation_u1_dm.jl:14-149) at (x, y) in [0,1]^2; k = 0 xx, 1 zz, 2 xy
+double chi_kernel_u1dm(const Prob& P, const Act& A, const double* Sig, double L, int k, int site, double w, double x,
+                       double y) {
+    const oracle_problem* m = P.p;
+    const double v = (2.0 * x - 1.0) / ((1.0 - x) * x);
+    const double vp = (2.0 * y - 1.0) / ((1.0 - y) * y);
+    const double dv = (2.0 * x * x - 2.0 * x + 1) / ((1.0 - x) * (1.0 - x) * x * x);
+    const double dvp = (2.0 * y * y - 2.0 * y + 1) / ((1.0 - y) * (1.0 - y) * y * y);
+    Buf bs1 = buffer_s(m, v + vp, 0.5 * (v - w - vp), 0.5 * (-v - w + vp));
+    Buf bt1 = buffer_t(m, w, v, vp);
+    Buf bu1 = buffer_u(m, v - vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp));
+    const double tp2 = (2.0 * kPi) * (2.0 * kPi);
+    const int comp1[3] = {0, 1, 2};
+    double val = -gamma_comp_site(P, A, comp1[k], site, bs1, bt1, bu1, ALL) / tp2;
+    if (site == 0) {
+        Buf bs2 = buffer_s(m, v + vp, 0.5 * (v - w - vp), 0.5 * (v + w - vp));
+        Buf bt2 = buffer_t(m, -v + vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp));
+        Buf bu2 = buffer_u(m, -w, v, vp);
+        auto g = [&](int c) { return gamma_comp_site(P, A, c, 0, bs2, bt2, bu2, ALL); };
+        if (k == 0) {
+            const double vzz = g(1), vdd = g(3);
+            val -= (vzz - vdd) / (2.0 * tp2);
+        } else if (k == 1) {
+            const double vxx = g(0), vzz = g(1), vdd = g(3);
+            val -= (2.0 * vxx - vzz - vdd) / (2.0 * tp2);
+        } else {
+            const double vzd = g(4), vdz = g(5);
+            val -= (vzd - vdz) / (2.0 * tp2);
+        }
+    }
+    val *= G_full(m, Sig, L, v - 0.5 * w) * G_full(m, Sig, L, v + 0.5 * w) * dv;
+    val *= G_full(m, Sig, L, vp - 0.5 * w) * G_full(m, Sig, L, vp + 0.5 * w) * dvp;
+    return val;
 }
 
 void reset_stats() { g_stats = oracle_stats{}; }
@@ -1132,7 +1544,6 @@ int oracle_symmetrize_add_to(const oracle_problem* p, const double* a_l, double*
 int oracle_dgamma(const oracle_problem* p, int loops, double Lam, const double* a, double* da, double* da_l,
                   double* da_c, double* da_temp, double* da_sigma, int eval, double gatol, double grtol,
                   int sigma_corr, double satol, double srtol) {
-    if (p->symmetry != 0) return 2;
     Prob P = make_prob(p);
     const Dims& d = P.d;
     reset_stats();
@@ -1189,7 +1600,6 @@ int oracle_dgamma(const oracle_problem* p, int loops, double Lam, const double* 
 
 int oracle_bse(const oracle_problem* p, double Lam, const double* a1, double* a2, const double* corrs,
                int eval, double atol, double rtol) {
-    if (p->symmetry != 0) return 2;
     Prob P = make_prob(p);
     reset_stats();
     // compute_Γ! (compute.jl:2-54) has no corrs step of its own: it reuses the
@@ -1203,13 +1613,13 @@ int oracle_bse(const oracle_problem* p, double Lam, const double* a1, double* a2
 
 int oracle_sde(const oracle_problem* p, double Lam, const double* a1, double* a2, double* corrs, int eval,
                double gatol, double grtol, double satol, double srtol) {
-    if (p->symmetry != 0) return 2;
     Prob P = make_prob(p);
     const Dims& d = P.d;
     reset_stats();
     compute_corrs(P, 1, Lam, a1, nullptr, gatol, grtol, corrs);
     // reduced s bubble (SDE.jl:2-56): slot 1 is the bare vertex, kernels 1 and 3 only
     PassDesc pd = pass(0, PROP_PLAIN, a1, nullptr, a1, 0, a1, ALL);
+    pd.reduced = true;
     std::vector<Task> tasks;
     for (int w1 = 1; w1 <= d.NO; ++w1) {
         tasks.push_back({1, w1, -1, -1});
@@ -1228,6 +1638,58 @@ int oracle_sde(const oracle_problem* p, double Lam, const double* a1, double* a2
             run_task(P, pd, Lam, tasks[j], corrs, eval, gatol, grtol, a2, ts);
     }
     sigma_integrals(P, SIG_SDE, Lam, a1, a2, satol, srtol, a2);
+    return 0;
+}
+
+int oracle_chi(const oracle_problem* p, double Lam, const double* a, const double* chi_mesh, int num_chi,
+               double atol, double rtol, double* chi) {
+    Prob P = make_prob(p);
+    const Dims& d = P.d;
+    Act A = make_act(d, a);
+    const oracle_problem* m = p;
+    if (p->symmetry == 1) {
+        // compute_χ! (correlation_u1_dm.jl:152-190): χxx, χzz, χxy, each column-major [Ns, num_chi]
+        const int64_t plane = (int64_t)d.Ns * num_chi;
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads(P)) collapse(2)
+        for (int w = 0; w < num_chi; ++w) {
+            for (int i = 0; i < d.Ns; ++i) {
+                const double wv = chi_mesh[w];
+                const double ref = Lam + 0.5 * wv;
+                for (int k = 0; k < 3; ++k) {
+                    auto f = [&](double x, double y) { return chi_kernel_u1dm(P, A, a, Lam, k, i, wv, x, y); };
+                    chi[k * plane + i + (int64_t)d.Ns * w] = chi_boxes(f, 4.0 * ref, atol, rtol);
+                }
+                if (i == 0) {
+                    auto g = [&](double v) {
+                        return G_full(m, a, Lam, v - 0.5 * wv) * G_full(m, a, Lam, v + 0.5 * wv) / (4.0 * kPi);
+                    };
+                    const double inf = INFINITY;
+                    const double res = quadgk(g, {-inf, -2.0 * ref, 0.0, 2.0 * ref, inf}, atol, rtol);
+                    chi[0 * plane + (int64_t)d.Ns * w] += res;
+                    chi[1 * plane + (int64_t)d.Ns * w] += res;
+                }
+            }
+        }
+        return 0;
+    }
+    // compute_χ! (correlation_su2.jl:58-86): χ[i, w], column-major [Ns, num_chi]
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads(P)) collapse(2)
+    for (int w = 0; w < num_chi; ++w) {
+        for (int i = 0; i < d.Ns; ++i) {
+            const double wv = chi_mesh[w];
+            const double ref = Lam + 0.5 * wv;
+            auto f = [&](double x, double y) { return chi_kernel(P, A, a, Lam, i, wv, x, y); };
+            double c = chi_boxes(f, 4.0 * ref, atol, rtol);
+            if (i == 0) {
+                auto g = [&](double v) {
+                    return (2.0 * P.S) * G_full(m, a, Lam, v - 0.5 * wv) * G_full(m, a, Lam, v + 0.5 * wv) / (4.0 * kPi);
+                };
+                const double inf = INFINITY;
+                c += quadgk(g, {-inf, -2.0 * ref, 0.0, 2.0 * ref, inf}, atol, rtol);
+            }
+            chi[i + (int64_t)d.Ns * w] = c;
+        }
+    }
     return 0;
 }
 
@@ -1272,6 +1734,15 @@ int oracle_test_integrators(int n, double a, double b, int eval, double atol, do
     else integrate_lin(f, t1.data(), t2.data(), t3.data(), n, a, b, eval, atol, rtol);
     for (int i = 0; i < n; ++i) out[i] = t1[i];
     return 0;
+}
+
+double oracle_test_hcubature(int which, double x0, double x1, double y0, double y1, double atol, double rtol) {
+    auto f = [&](double x, double y) {
+        if (which == 0) return std::exp(-x * x - 2.0 * y * y) * std::cos(3.0 * x * y);
+        return 1.0 / std::sqrt(x * x + y * y + 1e-3);
+    };
+    const double xmin[2] = {x0, y0}, xmax[2] = {x1, y1};
+    return hcubature2(f, xmin, xmax, atol, rtol, 10000000LL);
 }
 
 double oracle_test_quadgk(int power, double a, double b, double atol, double rtol) {

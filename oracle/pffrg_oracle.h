@@ -84,6 +84,10 @@ int oracle_bse(const oracle_problem* p, double Lam, const double* a1, double* a2
 int oracle_sde(const oracle_problem* p, double Lam, const double* a1, double* a2, double* corrs,
                int eval, double gamma_atol, double gamma_rtol, double sigma_atol, double sigma_rtol);
 
+/* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86): χ[Ns, num_chi] column-major */
+int oracle_chi(const oracle_problem* p, double Lam, const double* a, const double* chi_mesh, int num_chi,
+               double atol, double rtol, double* chi);
+
 /* symmetrize! and symmetrize_add_to! (action_su2.jl:141-251) */
 int oracle_symmetrize(const oracle_problem* p, double* a);
 int oracle_symmetrize_add_to(const oracle_problem* p, const double* a_l, double* a);
@@ -104,6 +108,8 @@ double oracle_get_sigma(const oracle_problem* p, const double* a, double w);
  * b[i] += dx * x^i exp(-x^2) sin(2 pi x), i = 1..n (src/Flow/test.jl:1-13) */
 int oracle_test_integrators(int n, double a, double b, int eval, double atol, double rtol,
                             int log_mesh, double* out);
+/* the 2-D h-adaptive cubature on a test integrand: 0 = exp(-x^2-2y^2) cos(3xy), 1 = 1/sqrt(x^2+y^2+1e-3) */
+double oracle_test_hcubature(int which, double x0, double x1, double y0, double y1, double atol, double rtol);
 /* QuadGK-equivalent scalar integral of the same test function, i = power */
 double oracle_test_quadgk(int power, double a, double b, double atol, double rtol);
 

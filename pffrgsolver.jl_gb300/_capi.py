@@ -26,7 +26,7 @@ EXPORTED = [
     "pffrg_create", "pffrg_destroy", "pffrg_last_error", "pffrg_set_mesh", "pffrg_set_precision",
     "pffrg_dsigma", "pffrg_dgamma", "pffrg_sde", "pffrg_bse", "pffrg_action_size", "pffrg_upload",
     "pffrg_download", "pffrg_rhs", "pffrg_bs_step", "pffrg_accept", "pffrg_last_integrand_evals",
-    "pffrg_host_alloc", "pffrg_host_free", "pffrg_set_timing", "pffrg_read_stats",
+    "pffrg_host_alloc", "pffrg_host_free", "pffrg_set_timing", "pffrg_read_stats", "pffrg_chi", "pffrg_chi_slot",
 ]
 
 
@@ -90,6 +90,9 @@ def load():
     L.pffrg_bs_step.argtypes = [vp, ctypes.c_int, d, d, ctypes.c_int, d, d, d, d, ctypes.c_int, d, d,
                                 ctypes.POINTER(d), ctypes.POINTER(d)]
     L.pffrg_accept.argtypes = [vp]
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.pffrg_chi.argtypes = [vp, d, AV, dp, ctypes.c_int, d, d, dp]
+    L.pffrg_chi_slot.argtypes = [vp, d, ctypes.c_int, dp, ctypes.c_int, d, d, dp]
     L.pffrg_last_integrand_evals.argtypes = [vp]
     L.pffrg_last_integrand_evals.restype = ctypes.c_int64
     L.pffrg_host_alloc.argtypes = [ctypes.c_int64]

@@ -67,6 +67,15 @@ struct pffrg_ctx {
     cudaEvent_t rhs_ev[2] = {nullptr, nullptr};
     double pass_ms = 0.0, rhs_ms = 0.0;
     int64_t pass_launches = 0, launches = 0;
+    // correlations: region records of the cubature and the ω mesh of χ
+    double* chi_reg = nullptr;
+    int* chi_split = nullptr;
+    size_t chi_reg_bytes = 0;
+    long long chi_cap = 256;
+    double* chi_box = nullptr;
+    double* chi_out = nullptr;
+    double* chi_mesh = nullptr;
+    int chi_n = 0;
     std::string err;
 
     int fail(int code, const char* fmt, ...) {
@@ -409,6 +418,74 @@ int check_status(pffrg_ctx* ctx) {
     return 0;
 }
 
+// compute_χ! (correlation_su2.jl:58-86) on a device action; the region
+// capacity of the cubature grows (x4) until no integral runs out of it
+int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh, int num_chi, double atol,
+            double rtol, double* chi) {
+    if (ctx->symmetry != PFFRG_SU2) return ctx->fail(PFFRG_E_ARGS, "correlations are implemented for su2 only");
+    if (num_chi < 1 || !chi_mesh || !chi) return ctx->fail(PFFRG_E_ARGS, "empty correlation mesh or output");
+    const int Ns = ctx->L.Ns;
+    if (num_chi > ctx->chi_n) {
+        for (double** p : {&ctx->chi_mesh, &ctx->chi_box, &ctx->chi_out}) {
+            if (*p) CK(cudaFree(*p));
+            *p = nullptr;
+        }
+        CK(cudaMalloc(&ctx->chi_mesh, sizeof(double) * num_chi));
+        CK(cudaMalloc(&ctx->chi_box, sizeof(double) * 9 * (size_t)Ns * num_chi));
+        CK(cudaMalloc(&ctx->chi_out, sizeof(double) * (size_t)Ns * num_chi));
+        ctx->chi_n = num_chi;
+    }
+    CK(cudaMemcpyAsync(ctx->chi_mesh, chi_mesh, sizeof(double) * num_chi, cudaMemcpyHostToDevice, ctx->st));
+    const long long njobs = 9ll * Ns * num_chi;
+    const size_t max_bytes = (size_t)32 << 30;
+    for (;;) {
+        const size_t per_job = (size_t)ctx->chi_cap * (7 * sizeof(double) + sizeof(int));
+        const size_t need = per_job * (size_t)njobs;
+        if (need > ctx->chi_reg_bytes) {
+            if (ctx->chi_reg) CK(cudaFree(ctx->chi_reg));
+            if (ctx->chi_split) CK(cudaFree(ctx->chi_split));
+            ctx->chi_reg = nullptr;
+            ctx->chi_split = nullptr;
+            ctx->chi_reg_bytes = 0;
+            CK(cudaMalloc(&ctx->chi_reg, sizeof(double) * 7 * (size_t)ctx->chi_cap * njobs));
+            CK(cudaMalloc(&ctx->chi_split, sizeof(int) * (size_t)ctx->chi_cap * njobs));
+            ctx->chi_reg_bytes = need;
+        }
+        ChiArgs c;
+        c.L = ctx->L;
+        c.a = a;
+        c.mesh = ctx->mesh;
+        c.chi_mesh = ctx->chi_mesh;
+        c.num_chi = num_chi;
+        c.exch = ctx->lat.exch;
+        c.Lam = Lam;
+        c.atol = atol;
+        c.rtol = rtol;
+        c.twoS = 2.0 * ctx->S;
+        c.reg = ctx->chi_reg;
+        c.reg_split = ctx->chi_split;
+        c.cap = ctx->chi_cap;
+        c.box_out = ctx->chi_box;
+        c.chi = ctx->chi_out;
+        c.status = ctx->status;
+        ctx->launches += 2;
+        CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
+        CK(launch_chi(c, ctx->st));
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        if (h) CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
+        if (h & 1) return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity exceeded in χ");
+        if (!(h & 2)) break;
+        if (per_job * 4 * (size_t)njobs > max_bytes)
+            return ctx->fail(PFFRG_E_LIMIT, "cubature regions of χ exceed %zu bytes", max_bytes);
+        ctx->chi_cap *= 4;
+    }
+    CK(cudaMemcpyAsync(chi, ctx->chi_out, sizeof(double) * (size_t)Ns * num_chi, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
 // compute_dΣ! on device actions
 template <typename R>
 int dsigma_dev(pffrg_ctx* ctx, double Lam, const double* a, double* da, double atol, double rtol) {
@@ -598,7 +675,8 @@ void pffrg_destroy(pffrg_ctx* ctx) {
     void* ptrs[] = {ctx->lat.exch, ctx->lat.mult, ctx->lat.ov_off, ctx->lat.ov_rows, ctx->wave_mem,
                     ctx->mesh, ctx->log_bounds, ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig, ctx->sig_tmp, ctx->f_a, ctx->f_da,
                     ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
-                    ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red};
+                    ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red, ctx->chi_reg, ctx->chi_split,
+                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
@@ -974,6 +1052,22 @@ int pffrg_accept(pffrg_ctx* ctx) {
                        cudaMemcpyDeviceToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return 0;
+}
+
+int pffrg_chi(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, const double* chi_mesh, int num_chi,
+              double atol, double rtol, double* chi) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    if (int rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_A], a, true)) return rc;
+    return chi_dev(ctx, Lam, ctx->slot[PFFRG_SLOT_A], chi_mesh, num_chi, atol, rtol, chi);
+}
+
+int pffrg_chi_slot(pffrg_ctx* ctx, double Lam, int slot, const double* chi_mesh, int num_chi, double atol,
+                   double rtol, double* chi) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (slot < 0 || slot >= PFFRG_NUM_SLOTS) return ctx->fail(PFFRG_E_ARGS, "bad slot");
+    CK(cudaSetDevice(ctx->device));
+    return chi_dev(ctx, Lam, ctx->slot[slot], chi_mesh, num_chi, atol, rtol, chi);
 }
 
 void* pffrg_host_alloc(int64_t bytes) {

@@ -140,6 +140,24 @@ struct CorrsArgs {
 template <typename R>
 cudaError_t launch_corrs(const CorrsArgs<R>& a, cudaStream_t st);
 
+// correlations χ (FP64)
+struct ChiArgs {
+    Layout L;
+    const double* a;         // the state (FP64)
+    const double* mesh;
+    const double* chi_mesh;  // [num_chi]
+    int num_chi;
+    const int* exch;
+    double Lam, atol, rtol, twoS;
+    double* reg;             // [njobs][7][cap] region records
+    int* reg_split;          // [njobs][cap]
+    long long cap;           // regions per (ω, site, box) integral
+    double* box_out;         // [num_chi][Ns][9]
+    double* chi;             // [Ns][num_chi] column-major
+    int* status;             // bit 1: GK segments, bit 2: cubature regions exhausted
+};
+cudaError_t launch_chi(const ChiArgs& a, cudaStream_t st);
+
 // elementwise action kernels (FP64)
 cudaError_t launch_symmetrize(const Layout& L, const int* exch, double* a, cudaStream_t st);
 cudaError_t launch_symmetrize_add_to(const Layout& L, const int* exch, const double* al, double* a,

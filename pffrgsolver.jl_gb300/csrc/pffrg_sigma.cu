@@ -338,6 +338,349 @@ cudaError_t launch_corrs(const CorrsArgs<R>& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// correlations χ (src/Observable/correlation_lib/correlation_lib.jl:2-30,
+// correlation_su2.jl:14-87).  The reference integrates the vertex part over
+// nine boxes of the compactified (v, v') plane with Cubature.jl's hcubature_v
+// (compat 1.5, wrapping S. G. Johnson's cubature library, not in the
+// reference tree); its published algorithm is restated: Genz-Malik
+// degree-7/5 rule for dim = 2 (17 points, error |R7 - R5|), split along the
+// dimension with the largest fourth difference, and per round the bisection
+// of every largest-error region needed to bring the remaining error under
+// max(atol, rtol |I|).  One warp per (ω, site, box) integral, FP64; the
+// regions live in device scratch (capacity per integral: chi_cap).
+// ---------------------------------------------------------------------------
+constexpr double kGL2 = 0.3585685828003180919906451539079374954541;  // sqrt(9/70)
+constexpr double kGL4 = 0.9486832980505137995996680633298155601160;  // sqrt(9/10)
+constexpr double kGL5 = 0.6882472016116852977216287342936235251269;  // sqrt(9/19)
+
+struct ChiRegions {
+    double* c0;
+    double* c1;
+    double* h0;
+    double* h1;
+    double* vol;
+    double* val;
+    double* err;
+    int* split;  // bit 0: split dimension, bit 1: pending evaluation, bit 2: made in the current round,
+                 // bits 3+: the region it was cut from (for the second half of a cut)
+};
+
+// point k of the 17 Genz-Malik points of region (c, h), the library's order
+__device__ __forceinline__ void gm_point(int k, double c0, double c1, double h0, double h1, double& x, double& y) {
+    x = c0;
+    y = c1;
+    if (k == 0) return;
+    if (k <= 8) {
+        const int d = (k - 1) >> 2, q = (k - 1) & 3;
+        const double hw = d == 0 ? h0 : h1;
+        const double off = (q < 2 ? hw * kGL2 : hw * kGL4) * ((q & 1) ? 1.0 : -1.0);
+        if (d == 0) x = c0 + off;
+        else y = c1 + off;
+        return;
+    }
+    if (k <= 12) {
+        const double a = h0 * kGL4, b = h1 * kGL4;
+        const int q = k - 9;  // (-,-), (+,-), (+,+), (-,+)
+        x = c0 + ((q == 1 || q == 2) ? a : -a);
+        y = c1 + ((q >= 2) ? b : -b);
+        return;
+    }
+    const double a = h0 * kGL5, b = h1 * kGL5;
+    const int q = k - 13;  // (+,+), (-,+), (-,-), (+,-)
+    x = c0 + ((q == 0 || q == 3) ? a : -a);
+    y = c1 + ((q <= 1) ? b : -b);
+}
+
+// rule75genzmalik_evalError for dim = 2 on the 17 values v
+__device__ __forceinline__ void gm_rule(const double* v, double vol, double& val, double& err, int& split) {
+    const double n = 2.0;
+    const double w1 = (12824.0 - 9120.0 * n + 400.0 * n * n) / 19683.0;
+    const double w2 = 980.0 / 6561.0;
+    const double w3 = (1820.0 - 400.0 * n) / 19683.0;
+    const double w4 = 200.0 / 19683.0;
+    const double w5 = 6859.0 / 19683.0 / 4.0;
+    const double e1 = (729.0 - 950.0 * n + 50.0 * n * n) / 729.0;
+    const double e2 = 245.0 / 486.0;
+    const double e3 = (265.0 - 100.0 * n) / 1458.0;
+    const double e4 = 25.0 / 729.0;
+    const double ratio = (kGL2 * kGL2) / (kGL4 * kGL4);
+    const double val0 = v[0];
+    double sum2 = 0.0, sum3 = 0.0, diff[2];
+    for (int d = 0; d < 2; ++d) {
+        const double v0 = v[1 + 4 * d], v1 = v[2 + 4 * d], v2 = v[3 + 4 * d], v3 = v[4 + 4 * d];
+        sum2 += v0 + v1;
+        sum3 += v2 + v3;
+        diff[d] = fabs(v0 + v1 - 2 * val0 - ratio * (v2 + v3 - 2 * val0));
+    }
+    double sum4 = 0.0, sum5 = 0.0;
+    for (int q = 0; q < 4; ++q) sum4 += v[9 + q];
+    for (int q = 0; q < 4; ++q) sum5 += v[13 + q];
+    const double result = vol * (w1 * val0 + w2 * sum2 + w3 * sum3 + w4 * sum4 + w5 * sum5);
+    const double res5 = vol * (e1 * val0 + e2 * sum2 + e3 * sum3 + e4 * sum4);
+    val = result;
+    err = fabs(res5 - result);
+    split = diff[1] > diff[0] ? 1 : 0;
+}
+
+// compute_χ_kernel! (correlation_su2.jl:14-55) at (x, y) of [0,1]^2
+struct ChiKernel {
+    const ChiArgs& A;
+    const SMesh<double>& M;
+    int site;
+    double w;
+    __device__ double operator()(double x, double y) const {
+        const Layout& L = A.L;
+        const double v = (2.0 * x - 1.0) / ((1.0 - x) * x);
+        const double vp = (2.0 * y - 1.0) / ((1.0 - y) * y);
+        const double dv = (2.0 * x * x - 2.0 * x + 1) / ((1.0 - x) * (1.0 - x) * x * x);
+        const double dvp = (2.0 * y * y - 2.0 * y + 1) / ((1.0 - y) * (1.0 - y) * y * y);
+        Plan<double> p1[3];
+        make_plan<double>(p1[0], 0, v + vp, 0.5 * (v - w - vp), 0.5 * (-v - w + vp), M, L.Ns, L.NO, L.Nn);
+        make_plan<double>(p1[1], 1, w, v, vp, M, L.Ns, L.NO, L.Nn);
+        make_plan<double>(p1[2], 2, v - vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp), M, L.Ns, L.NO, L.Nn);
+        const double twoS = A.twoS;
+        const double tp2 = two_pi<double>() * two_pi<double>();
+        const int ei = ldg(A.exch + site);
+        double val = -(twoS * twoS) * site_value<double>(L, A.a, p1, CH_ALL, 0, site, ei) / tp2;
+        if (site == 0) {
+            Plan<double> p2[3];
+            make_plan<double>(p2[0], 0, v + vp, 0.5 * (v - w - vp), 0.5 * (v + w - vp), M, L.Ns, L.NO, L.Nn);
+            make_plan<double>(p2[1], 1, -v + vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp), M, L.Ns, L.NO, L.Nn);
+            make_plan<double>(p2[2], 2, -w, v, vp, M, L.Ns, L.NO, L.Nn);
+            const double vs = site_value<double>(L, A.a, p2, CH_ALL, 0, 0, ei);
+            const double vd = site_value<double>(L, A.a, p2, CH_ALL, 1, 0, ei);
+            val -= twoS * (vs - vd) / (2.0 * tp2);
+        }
+        const double Lam = A.Lam;
+        val *= G_full(M, L.Nsig, A.a, Lam, v - 0.5 * w) * G_full(M, L.Nsig, A.a, Lam, v + 0.5 * w) * dv;
+        val *= G_full(M, L.Nsig, A.a, Lam, vp - 0.5 * w) * G_full(M, L.Nsig, A.a, Lam, vp + 0.5 * w) * dvp;
+        return val;
+    }
+};
+
+// evaluate the pending regions [first, first + count) of one integral (17 points each over the lanes)
+template <class F>
+__device__ void chi_eval_regions(const F& f, ChiRegions R, const int* idx, int count, double* fbuf) {
+    const int lane = threadIdx.x & 31;
+    for (int base = 0; base < count * 17; base += 32) {
+        const int e = base + lane;
+        if (e < count * 17) {
+            const int r = idx[e / 17], k = e % 17;
+            double x, y;
+            gm_point(k, R.c0[r], R.c1[r], R.h0[r], R.h1[r], x, y);
+            fbuf[e] = f(x, y);
+        }
+    }
+    __syncwarp();
+    for (int q = lane; q < count; q += 32) {
+        const int r = idx[q];
+        double val, err;
+        int sp;
+        gm_rule(fbuf + 17 * q, R.vol[r], val, err, sp);
+        R.val[r] = val;
+        R.err[r] = err;
+        R.split[r] = (R.split[r] & ~7) | sp | 4;
+    }
+    __syncwarp();
+}
+
+constexpr int kChiWarps = 2;
+constexpr int kChiPend = 64;  // regions evaluated per batch
+
+__global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SMesh<double>& M = *reinterpret_cast<SMesh<double>*>(smem_raw);
+    double* fb = reinterpret_cast<double*>(smem_raw + sizeof(SMesh<double>));
+    int* pend = reinterpret_cast<int*>(fb + kChiWarps * kChiPend * 17);
+    load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long job = (long long)blockIdx.x * kChiWarps + warp;
+    const long long njobs = (long long)A.num_chi * A.L.Ns * 9;
+    if (job >= njobs) return;
+    double* fbuf = fb + warp * kChiPend * 17;
+    int* pidx = pend + warp * kChiPend;
+    const int box = (int)(job % 9), site = (int)((job / 9) % A.L.Ns), wi = (int)(job / (9ll * A.L.Ns));
+    const double wv = A.chi_mesh[wi];
+    // integrate_χ_boxes: the nine boxes around the image of ±width = ±4 (Λ + ω / 2)
+    const double width = 4.0 * (A.Lam + 0.5 * wv);
+    const double wp = (width - 2.0 + sqrt(width * width + 4.0)) / (2.0 * width);
+    const double s = fabs(wp - 0.5);
+    const double lo[3] = {0.0, 0.5 - s, 0.5 + s}, hi[3] = {0.5 - s, 0.5 + s, 1.0};
+    const int row = 2 - box / 3, col = box % 3;  // the reference's order: top line first
+    ChiRegions R;
+    const size_t cap = A.cap;
+    const size_t off = (size_t)job * cap;
+    R.c0 = A.reg + off * 7;
+    R.c1 = R.c0 + cap;
+    R.h0 = R.c1 + cap;
+    R.h1 = R.h0 + cap;
+    R.vol = R.h1 + cap;
+    R.val = R.vol + cap;
+    R.err = R.val + cap;
+    R.split = A.reg_split + off;
+    ChiKernel f{A, M, site, wv};
+    if (lane == 0) {
+        R.c0[0] = 0.5 * (lo[col] + hi[col]);
+        R.c1[0] = 0.5 * (lo[row] + hi[row]);
+        R.h0[0] = 0.5 * (hi[col] - lo[col]);
+        R.h1[0] = 0.5 * (hi[row] - lo[row]);
+        R.vol[0] = (2.0 * R.h0[0]) * (2.0 * R.h1[0]);
+        pidx[0] = 0;
+    }
+    __syncwarp();
+    chi_eval_regions(f, R, pidx, 1, fbuf);
+    int n = 1;
+    double tot_val = R.val[0], tot_err = R.err[0];
+    long long numeval = 17;
+    const long long maxevals = 10000000;
+    bool overflow = false;
+    auto converged = [&](double err, double val) { return !(err > A.atol && err > fabs(val) * A.rtol); };
+    while (numeval < maxevals) {
+        if (converged(tot_err, tot_val)) break;
+        double ee_err = tot_err;
+        const double ee_val = tot_val;
+        const int n0 = n;
+        int npend = 0;
+        bool stop = false;
+        // pop the largest-error regions (cubature's parallel mode), bisect each into two pending ones
+        do {
+            double best = -1.0;
+            int bi = 0;
+            for (int k = lane; k < n; k += 32) {
+                const double e = (R.split[k] & 6) ? -1.0 : R.err[k];
+                if (e > best) {
+                    best = e;
+                    bi = k;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) {
+                    best = ob;
+                    bi = oi;
+                }
+            }
+            if (best < 0.0) break;  // no region left to pop
+            if (n + 1 > (int)cap) {
+                overflow = true;
+                stop = true;
+                break;
+            }
+            const double pv = R.val[bi], pe = R.err[bi];
+            tot_val -= pv;
+            tot_err -= pe;
+            ee_err -= pe;
+            if (lane == 0) {
+                const int d = R.split[bi] & 1;
+                R.c0[n] = R.c0[bi];
+                R.c1[n] = R.c1[bi];
+                R.h0[n] = R.h0[bi];
+                R.h1[n] = R.h1[bi];
+                if (d == 0) {
+                    R.h0[bi] *= 0.5;
+                    R.h0[n] = R.h0[bi];
+                    R.c0[bi] -= R.h0[bi];
+                    R.c0[n] += R.h0[bi];
+                } else {
+                    R.h1[bi] *= 0.5;
+                    R.h1[n] = R.h1[bi];
+                    R.c1[bi] -= R.h1[bi];
+                    R.c1[n] += R.h1[bi];
+                }
+                R.vol[bi] *= 0.5;
+                R.vol[n] = (2.0 * R.h0[n]) * (2.0 * R.h1[n]);
+                R.split[bi] = 2;
+                R.split[n] = 2 | (bi << 3);
+                pidx[npend] = bi;
+                pidx[npend + 1] = n;
+            }
+            __syncwarp();
+            npend += 2;
+            ++n;
+            numeval += 34;
+            if (converged(ee_err, ee_val)) break;
+            if (npend + 2 > kChiPend) {
+                // evaluate this batch and keep popping in the same round
+                chi_eval_regions(f, R, pidx, npend, fbuf);
+                npend = 0;
+            }
+        } while (numeval < maxevals);
+        if (npend) chi_eval_regions(f, R, pidx, npend, fbuf);
+        // the round's regions join the heap, added to the totals in the order they were cut
+        for (int k = n0; k < n; ++k) {
+            const int tw = R.split[k] >> 3;
+            tot_val += R.val[tw];
+            tot_val += R.val[k];
+            tot_err += R.err[tw];
+            tot_err += R.err[k];
+        }
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) R.split[k] &= ~6;
+        __syncwarp();
+        if (stop) break;
+    }
+    double I = 0.0;
+    for (int k = 0; k < n; ++k) I += R.val[k];
+    if (lane == 0) {
+        A.box_out[job] = I;
+        if (overflow) atomicOr(A.status, 2);
+    }
+}
+
+// local term (correlation_su2.jl:77-81) and the sum of the nine boxes
+__global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SMesh<double>& M = *reinterpret_cast<SMesh<double>*>(smem_raw);
+    SegStore* segs = reinterpret_cast<SegStore*>(smem_raw + sizeof(SMesh<double>));
+    load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wi = blockIdx.x * kSigWarps + warp;
+    if (wi >= A.num_chi) return;
+    const double wv = A.chi_mesh[wi];
+    const double ref = A.Lam + 0.5 * wv;
+    struct G2 {
+        const ChiArgs& A;
+        const SMesh<double>& M;
+        double w;
+        __device__ double operator()(double v) const {
+            return A.twoS * G_full(M, A.L.Nsig, A.a, A.Lam, v - 0.5 * w) * G_full(M, A.L.Nsig, A.a, A.Lam, v + 0.5 * w) /
+                   (2.0 * two_pi<double>());
+        }
+    } g{A, M, wv};
+    const double inf = INFINITY;
+    const double pts[5] = {-inf, -2.0 * ref, 0.0, 2.0 * ref, inf};
+    double t[5], s0;
+    const int mode = map_points(pts, 5, t, s0);
+    const double loc = warp_quadgk(g, mode, s0, t, 5, A.atol, A.rtol, segs[warp], A.status);
+    if (lane == 0) {
+        for (int i = 0; i < A.L.Ns; ++i) {
+            const double* b = A.box_out + ((size_t)wi * A.L.Ns + i) * 9;
+            double c = b[0];
+            for (int k = 1; k < 9; ++k) c += b[k];
+            if (i == 0) c += loc;
+            A.chi[i + (size_t)A.L.Ns * wi] = c;
+        }
+    }
+}
+
+cudaError_t launch_chi(const ChiArgs& a, cudaStream_t st) {
+    const long long njobs = (long long)a.num_chi * a.L.Ns * 9;
+    const size_t smem = sizeof(SMesh<double>) + sizeof(double) * kChiWarps * kChiPend * 17 + sizeof(int) * kChiWarps * kChiPend;
+    cudaError_t e = cudaFuncSetAttribute(chi_box_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    chi_box_kernel<<<(unsigned)((njobs + kChiWarps - 1) / kChiWarps), kChiWarps * 32, smem, st>>>(a);
+    if ((e = cudaGetLastError())) return e;
+    const size_t smem2 = sizeof(SMesh<double>) + sizeof(SegStore) * kSigWarps;
+    e = cudaFuncSetAttribute(chi_local_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    if (e != cudaSuccess) return e;
+    chi_local_kernel<<<(a.num_chi + kSigWarps - 1) / kSigWarps, kSigWarps * 32, smem2, st>>>(a);
+    return cudaGetLastError();
+}
+
 template cudaError_t launch_sigma<double>(const SigmaArgs<double>&, cudaStream_t);
 template cudaError_t launch_sigma<float>(const SigmaArgs<float>&, cudaStream_t);
 template cudaError_t launch_corrs<double>(const CorrsArgs<double>&, cudaStream_t);

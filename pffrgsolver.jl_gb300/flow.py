@@ -108,6 +108,24 @@ class FlowContext:
         v1, v2 = _capi.action_view(a1), _capi.action_view(a2)
         self._check(self.lib.pffrg_bse(self.h, Lam, ctypes.byref(v1), ctypes.byref(v2), eval_, *gamma_tol), "bse")
 
+    def compute_chi(self, Lam: float, a: Action, chi_mesh, chi_tol=(1e-8, 1e-4)) -> np.ndarray:
+        """compute_χ! (correlation_su2.jl:58-86): χ[i, w] as an [Ns, num_chi] array (column-major)."""
+        av = _capi.action_view(a)
+        return self._chi(lambda mp, n, out: self.lib.pffrg_chi(self.h, Lam, ctypes.byref(av), mp, n, chi_tol[0],
+                                                                chi_tol[1], out), chi_mesh)
+
+    def chi_slot(self, Lam: float, slot: int, chi_mesh, chi_tol=(1e-8, 1e-4)) -> np.ndarray:
+        """χ of the device-resident action in `slot`."""
+        return self._chi(lambda mp, n, out: self.lib.pffrg_chi_slot(self.h, Lam, slot, mp, n, chi_tol[0],
+                                                                     chi_tol[1], out), chi_mesh)
+
+    def _chi(self, call, chi_mesh) -> np.ndarray:
+        mesh = np.ascontiguousarray(chi_mesh, dtype=np.float64)
+        out = np.zeros((self.num_sites, len(mesh)), dtype=np.float64, order="F")
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(call(mesh.ctypes.data_as(dp), len(mesh), out.ctypes.data_as(dp)), "chi")
+        return out
+
     # ---- device-resident interface ----
     def upload(self, slot: int, a: Action) -> None:
         v = _capi.action_view(a)

@@ -186,6 +186,7 @@ def resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, 
 @dataclass
 class FlowResult:
     Lam: list = field(default_factory=list)       # accepted cutoffs
+    chi: list = field(default_factory=list)       # (Λ, χ mesh, χ[Ns, num_chi]) per measurement
     dLam: list = field(default_factory=list)
     err: list = field(default_factory=list)
     abs_max: list = field(default_factory=list)
@@ -208,12 +209,14 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
            gamma_tol=(1e-8, 1e-4), chi_tol=(1e-8, 1e-4), parquet_tol=(1e-8, 1e-4), ode_tol=(1e-8, 1e-2),
            loops: int = 1, parquet: bool = True, sigma_corr: bool = True, initial: float = 5.0,
            final: float = 0.05, bmin: float = 1e-4, bmax: float = 0.1, cps=(), precision: str = "mixed",
-           device: int = 0, measure=None, verbose: bool = False) -> FlowResult:
+           device: int = 0, measure=None, correlations: bool = True, verbose: bool = False) -> FlowResult:
     """Run the FRG flow from ``initial`` to ``final`` (launch!, Launcher.jl:565-773).
 
-    ``measure(Λ, dΛ, m, a, ctx)`` is called after every accepted step with the
-    new state (the reference computes χ and writes observables there); it may
-    return False to stop the flow (the reference stops on non-monotone χ).
+    After every accepted step the static correlations χ of the new state are
+    computed on the GPU (``correlations``; measure, Launcher.jl:2-60), the flow
+    stops when the dominant on-site χ falls by more than 0.5 %, and χ steers
+    the χ mesh of the resampling.  ``measure(Λ, dΛ, m, a, ctx)`` is an extra
+    user callback after every accepted step; returning False stops the flow.
     """
     t0 = time.perf_counter()
     if symmetry not in A.SYMMETRIES:
@@ -238,7 +241,7 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
         _flow(ctx, r, m, a, res, loops=loops, sigma_corr=sigma_corr and loops >= 3, Li=initial, Lf=final,
               dLi=bmax * initial, bmin=bmin, bmax=bmax, min_eval=min_eval, max_eval=max_eval, sigma_tol=sigma_tol,
               gamma_tol=gamma_tol, ode_tol=ode_tol, p=(p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds),
-              cps=list(cps), measure=measure, verbose=verbose)
+              cps=list(cps), measure=measure, chi_tol=chi_tol if correlations else None, verbose=verbose)
     finally:
         ctx.close()
     res.seconds = time.perf_counter() - t0
@@ -246,7 +249,7 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
 
 
 def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, Lf, dLi, bmin, bmax, min_eval,
-          max_eval, sigma_tol, gamma_tol, ode_tol, p, cps, measure, verbose):
+          max_eval, sigma_tol, gamma_tol, ode_tol, p, cps, measure, chi_tol=None, verbose=False):
     """Bogacki-Shampine loop of launch_1l!/2l!/ml! (launcher_1l.jl:56-198) with device stages."""
     p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds = p
     Lam, dLam = Li, dLi
@@ -258,6 +261,17 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
     ctx.upload(_capi.SLOT_A, a)
     a_next = A.Action.empty_like(a)
     a_new = A.Action.empty_like(a)
+    chi = np.zeros((r.num_sites, m.num_chi), order="F")  # get_χ_empty
+
+    def measure_chi():
+        # compute_χ! on the new state and the monotonicity test of measure (Launcher.jl:23-35)
+        nonlocal chi
+        chi_prev = chi
+        chi = ctx.chi_slot(Lam, _capi.SLOT_NEXT, m.chi, chi_tol)
+        res.chi.append((Lam, np.array(m.chi), chi))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return bool(np.float64(chi[0, 0]) / np.float64(chi_prev[0, 0]) >= 0.995)
+
     while Lam > Lf:
         eval_ = get_eval(Lam, min_eval, max_eval)
         err, amax = ctx.bs_step(Lam, dLam, eval_, loops=loops, gamma_tol=gamma_tol, sigma_tol=sigma_tol,
@@ -286,16 +300,21 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
             ctx.download(_capi.SLOT_NEXT, a_next)
             if amax >= 1000.0:
                 res.reason = "vertex has diverged"
+                if chi_tol is not None:
+                    measure_chi()
                 if measure:
                     measure(Lam, dLam, m, a_next, ctx)
                 break
+            monotone = measure_chi() if chi_tol is not None else True
             if measure and measure(Lam, dLam, m, a_next, ctx) is False:
+                monotone = False
+            if not monotone:
                 res.reason = "flowing correlations show non-monotonicity"
                 break
             # new meshes and resampled state (launcher_1l.jl:177)
             a_new.buf[:] = a_next.buf
             m = resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m, a_next, a_new,
-                                 getattr(measure, "chi", None))
+                                 [chi] if chi_tol is not None else None)
             ctx.set_mesh(m)
             ctx.upload(_capi.SLOT_A, a_new)
         else:

@@ -72,13 +72,16 @@ def test_bs_step_matches_oracle(pkg, O, loops):
     assert amax == pytest.approx(np.max(np.abs(ref_next[a.q3_mask()])), rel=1e-12)
 
 
-def test_launch_runs_to_final(pkg):
+def test_launch_runs_to_final(pkg, O):
+    from pffrg_gb300 import lattice as L
     from pffrg_gb300.launcher import launch
 
     seen = []
+    last = {}
 
     def measure(Lam, dLam, m, a, ctx):
         seen.append(Lam)
+        last.update(m=m, buf=a.buf.copy())
         return True
 
     res = launch("t", "square", 3, "heisenberg", "su2", [[1.0]], num_sigma=10, num_omega=4, num_nu=3, num_chi=4,
@@ -86,6 +89,15 @@ def test_launch_runs_to_final(pkg):
     assert res.finished and res.Lam[-1] <= 3.0 + 1e-12
     assert seen == res.Lam and all(np.diff(res.Lam) < 0)
     assert res.integrand_evals > 0
+    # χ of every accepted step (measure, Launcher.jl:23-35); the last one against the oracle
+    assert [c[0] for c in res.chi] == res.Lam
+    Lam, chi_mesh, chi = res.chi[-1]
+    r = L.get_reduced_lattice("heisenberg", [[1.0]], L.get_lattice("square", 3))
+    ref = O.chi(O.Problem(r, last["m"]), Lam, last["buf"], chi_mesh)
+    assert np.max(np.abs(chi - ref)) <= 1e-6 * np.max(np.abs(ref))
+    # the on-site static χ grows as Λ decreases (the flow stops otherwise)
+    onsite = [c[2][0, 0] for c in res.chi]
+    assert all(x > 0 for x in onsite) and all(np.diff(onsite) > -0.005 * np.array(onsite[:-1]))
 
 
 def test_parquet_converges(pkg):

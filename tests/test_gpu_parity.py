@@ -93,3 +93,27 @@ def test_parquet_fp64_small(pkg, O):
         ctx.compute_sigma_sde(1.0, a, a2, 3)
         ctx.compute_gamma_bse(1.0, a, a2, 3)
     assert rel_err(a2.buf, a2_ref) < 1e-10
+
+
+@pytest.mark.parametrize("noise", [0.0, 0.1])
+def test_chi_fp64(pkg, O, noise):
+    """compute_χ! (correlation_su2.jl:58-86) on the GPU against the oracle at the launcher's default
+    χ_tol = (1e-8, 1e-4).  The integrand agrees to rounding, but a last-bit difference can flip one
+    region's convergence test, so the bar is the stated χ tolerance, 1e-6 of max|χ| (observed:
+    exact for the constant vertex, 1.3e-9 for the noisy state)."""
+    import dataclasses
+
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = dataclasses.replace(wl.WORKLOADS["square-L3-1l"], noise=noise)
+    lat, r, m, a = wl.build_state(w, num_sigma=10, num_omega=5, num_nu=4)
+    chi_mesh = np.array([0.0, 0.3, 2.0])
+    ref = O.chi(O.Problem(r, m), 1.0, a.buf, chi_mesh)
+    with FlowContext(r, m, precision="fp64") as ctx:
+        got = ctx.compute_chi(1.0, a, chi_mesh)
+        ctx.upload(0, a)
+        got_slot = ctx.chi_slot(1.0, 0, chi_mesh)
+    assert got.shape == ref.shape
+    assert rel_err(got, ref) < 1e-6
+    assert np.array_equal(got, got_slot)

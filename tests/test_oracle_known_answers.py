@@ -216,3 +216,49 @@ def test_workload_is_seeded(pkg):
     s2 = wl.build_state(wl.WORKLOADS["square-L3-1l"], num_sigma=8, num_omega=4, num_nu=3)[3]
     assert np.array_equal(s1.buf, s2.buf)
     assert s1.Σ[0] == 0.0
+
+
+@pytest.mark.parametrize("which", [0, 1])
+@pytest.mark.parametrize("tol", [(1e-10, 1e-4), (1e-14, 1e-9)])
+def test_hcubature_against_scipy(O, which, tol):
+    """The Genz-Malik cubature behind integrate_χ_boxes (correlation_lib.jl:2-30) on two smooth
+    integrands over a rectangle, against scipy's nested adaptive quadrature."""
+    scipy = pytest.importorskip("scipy.integrate")
+    x0, x1, y0, y1 = 0.1, 0.9, 0.2, 0.7
+    if which == 0:
+        f = lambda y, x: math.exp(-(x * x + 2 * y * y)) * math.cos(3 * x * y)  # noqa: E731
+    else:
+        f = lambda y, x: 1.0 / math.sqrt(x * x + y * y + 1e-3)  # noqa: E731
+    ref = scipy.dblquad(f, x0, x1, y0, y1, epsabs=1e-14, epsrel=1e-13)[0]
+    got = O.test_hcubature(which, x0, x1, y0, y1, *tol)
+    assert got == pytest.approx(ref, rel=30 * tol[1])
+
+
+def test_chi_constant_vertex(pkg, O):
+    """compute_χ! (correlation_su2.jl:58-86) for a frequency-independent vertex and Σ = 0 factorises:
+    χ_i(w) = -(2S)^2 Γ_i I(w)^2 / (2π)^2 for i > 1 and χ_1(w) = 2S I(w) / (4π) (no on-site coupling),
+    with I(w) = ∫ G0(v - w/2) G0(v + w/2) dv and G0(v) = -expm1(-v^2/Λ^2) / v (bubbles.jl:2-14)."""
+    scipy = pytest.importorskip("scipy.integrate")
+    import dataclasses
+
+    import pffrg_gb300.workloads as wl
+
+    w = dataclasses.replace(wl.WORKLOADS["square-L3-1l"], noise=0.0)
+    lat, r, m, a = wl.build_state(w, num_sigma=10, num_omega=5, num_nu=4)
+    Lam, S = 0.8, 0.5
+    chi_mesh = np.array([0.0, 0.4, 3.0])
+    P = O.Problem(r, m)
+    got = O.chi(P, Lam, a.buf, chi_mesh, (1e-12, 1e-9))
+
+    def G0(v):
+        return 0.0 if abs(v) <= 1e-8 else -math.expm1(-v * v / (Lam * Lam)) / v
+
+    spin = a.Γ[0].bare
+    assert spin[0] == 0.0 and a.Γ[1].bare[0] == 0.0
+    for k, wv in enumerate(chi_mesh):
+        g = lambda v: G0(v - 0.5 * wv) * G0(v + 0.5 * wv)  # noqa: E731
+        I = sum(scipy.quad(g, lo, hi, epsabs=1e-14, epsrel=1e-12, limit=400)[0]
+                for lo, hi in [(-np.inf, -10.0), (-10.0, 0.0), (0.0, 10.0), (10.0, np.inf)])
+        want = -(2 * S) ** 2 * spin * I * I / (2 * math.pi) ** 2
+        want[0] = 2 * S * I / (4 * math.pi)
+        assert np.allclose(got[:, k], want, rtol=1e-7, atol=1e-12)
