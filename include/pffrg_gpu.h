@@ -145,11 +145,12 @@ int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, 
 /* accept the step: slot A <- slot NEXT (the reference keeps a_inter for the resampling) */
 int pffrg_accept(pffrg_ctx* ctx);
 
-/* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86): static
- * spin correlations χ[i, w] of the action `a` at Λ on the frequencies
- * chi_mesh[0..num_chi), written column-major into chi[Ns * num_chi] (host).
- * Tolerances are χ_tol = (atol, rtol) (default (1e-8, 1e-4) in
- * src/Launcher/Launcher.jl:111).  su2 only. */
+/* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86,
+ * correlation_u1_dm.jl:152-190): static spin correlations χ[i, w] of the
+ * action `a` at Λ on the frequencies chi_mesh[0..num_chi), written
+ * column-major into chi (host): Ns * num_chi values for su2, three such
+ * blocks χxx | χzz | χxy for u1-dm.  Tolerances are χ_tol = (atol, rtol)
+ * (default (1e-8, 1e-4) in src/Launcher/Launcher.jl:111). */
 int pffrg_chi(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, const double* chi_mesh, int num_chi,
               double atol, double rtol, double* chi);
 /* the same on the device-resident action in `slot` (the measure step of

@@ -1288,7 +1288,6 @@ void sigma_integrals(const Prob& P, SigmaKind kind, double L, const double* a, c
 struct Region2 {
     double c[2], h[2], vol, val, err;
     int split;
-    bool operator<(const Region2& o) const { return err < o.err; }
 };
 
 constexpr double kGML2 = 0.3585685828003180919906451539079374954541;  // sqrt(9/70)
@@ -1358,6 +1357,53 @@ inline void gm_eval(Region2& R, const double* v) {
     R.split = diff[1] > diff[0] ? 1 : 0;
 }
 
+// max-heap of region indices keyed by their error estimate (the cubature
+// library's region heap): push sifts up while the parent's key is smaller;
+// pop moves the last entry to the root and sifts it down along the larger
+// child (the right one only when strictly larger).  The GPU kernel uses the
+// same two rules, so both pop regions in the same order.
+struct RegionHeap {
+    std::vector<double> key;
+    std::vector<int> idx;
+    void push(double k, int i) {
+        int h = (int)key.size();
+        key.push_back(k);
+        idx.push_back(i);
+        while (h > 0) {
+            const int p = (h - 1) / 2;
+            if (key[p] >= k) break;
+            key[h] = key[p];
+            idx[h] = idx[p];
+            h = p;
+        }
+        key[h] = k;
+        idx[h] = i;
+    }
+    int pop() {
+        const int top = idx[0];
+        const double k = key.back();
+        const int i = idx.back();
+        key.pop_back();
+        idx.pop_back();
+        const int n = (int)key.size();
+        if (n > 0) {
+            int h = 0;
+            for (;;) {
+                const int l = 2 * h + 1, r = l + 1;
+                if (l >= n) break;
+                const int c = (r < n && key[r] > key[l]) ? r : l;
+                if (key[c] <= k) break;
+                key[h] = key[c];
+                idx[h] = idx[c];
+                h = c;
+            }
+            key[h] = k;
+            idx[h] = i;
+        }
+        return top;
+    }
+};
+
 template <class F>
 double hcubature2(F& f, const double xmin[2], const double xmax[2], double abstol, double reltol,
                   long long maxevals) {
@@ -1368,15 +1414,16 @@ double hcubature2(F& f, const double xmin[2], const double xmax[2], double absto
         gm_eval(R, v);
     };
     auto converged = [&](double err, double val) { return !(err > abstol && err > std::fabs(val) * reltol); };
-    Region2 R0;
+    std::vector<Region2> regs(1);
+    Region2& R0 = regs[0];
     for (int d = 0; d < 2; ++d) {
         R0.c[d] = 0.5 * (xmin[d] + xmax[d]);
         R0.h[d] = 0.5 * (xmax[d] - xmin[d]);
     }
     R0.vol = (2.0 * R0.h[0]) * (2.0 * R0.h[1]);
     eval(R0);
-    std::priority_queue<Region2> heap;
-    heap.push(R0);
+    RegionHeap heap;
+    heap.push(R0.err, 0);
     double tot_val = R0.val, tot_err = R0.err;
     long long numeval = 17;
     while (numeval < maxevals) {
@@ -1384,14 +1431,14 @@ double hcubature2(F& f, const double xmin[2], const double xmax[2], double absto
         // the round's bound compares the remaining error with the total value at its start
         double ee_err = tot_err;
         const double ee_val = tot_val;
-        std::vector<Region2> Rs;
+        std::vector<int> cut;  // (first half, second half) per cut region
         do {
-            Region2 R = heap.top();
-            heap.pop();
-            tot_val -= R.val;
-            tot_err -= R.err;
-            ee_err -= R.err;
-            // cut_region: halve along the split dimension
+            const int bi = heap.pop();
+            tot_val -= regs[bi].val;
+            tot_err -= regs[bi].err;
+            ee_err -= regs[bi].err;
+            // cut_region: halve along the split dimension; the first half keeps the index
+            Region2 R = regs[bi];
             const int d = R.split;
             Region2 R2 = R;
             R.h[d] *= 0.5;
@@ -1400,23 +1447,23 @@ double hcubature2(F& f, const double xmin[2], const double xmax[2], double absto
             R2.vol = (2.0 * R2.h[0]) * (2.0 * R2.h[1]);
             R.c[d] -= R.h[d];
             R2.c[d] += R.h[d];
-            Rs.push_back(R);
-            Rs.push_back(R2);
+            regs[bi] = R;
+            regs.push_back(R2);
+            cut.push_back(bi);
+            cut.push_back((int)regs.size() - 1);
             numeval += 34;
             if (converged(ee_err, ee_val)) break;
-        } while (!heap.empty() && numeval < maxevals);
-        for (Region2& R : Rs) {
-            eval(R);
-            heap.push(R);
-            tot_val += R.val;
-            tot_err += R.err;
+        } while (!heap.key.empty() && numeval < maxevals);
+        for (int r : cut) eval(regs[r]);
+        for (int r : cut) {
+            heap.push(regs[r].err, r);
+            tot_val += regs[r].val;
+            tot_err += regs[r].err;
         }
     }
+    // the total in heap order, as the library sums it
     double I = 0.0;
-    while (!heap.empty()) {
-        I += heap.top().val;
-        heap.pop();
-    }
+    for (int i : heap.idx) I += regs[i].val;
     return I;
 }
 

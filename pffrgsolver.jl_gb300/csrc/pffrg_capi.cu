@@ -1,6 +1,7 @@
 // C ABI of libpffrg_gpu.so: context, device-resident actions and the
 // sequencing of the flow right-hand side (src/Flow/compute.jl,
 // src/Flow/flow_self.jl, src/Flow/SDE.jl, src/Launcher/launcher_{1l,2l,ml}.jl).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -71,7 +72,8 @@ struct pffrg_ctx {
     double* chi_reg = nullptr;
     int* chi_split = nullptr;
     size_t chi_reg_bytes = 0;
-    long long chi_cap = 256;
+    int* chi_jobs = nullptr;  // job list of a cubature launch
+    int* chi_over = nullptr;  // per-job overflow flags
     double* chi_box = nullptr;
     double* chi_out = nullptr;
     double* chi_mesh = nullptr;
@@ -234,7 +236,7 @@ cudaError_t ensure_wave_space(pffrg_ctx* ctx, long long nsub) {
         if (e != cudaSuccess) return e;
         ctx->wave_mem = nullptr;
     }
-    const size_t bytes = wave_space_bytes(nsub, ctx->L.Ns, qcap);
+    const size_t bytes = wave_space_bytes(nsub, ctx->L.Ns, qcap, ctx->L.C);
     cudaError_t e = cudaMalloc(&ctx->wave_mem, bytes);
     if (e != cudaSuccess) return e;
     ctx->wave_bytes = bytes;
@@ -249,7 +251,7 @@ cudaError_t launch_waves(pffrg_ctx* ctx, const PassArgs<R>& p) {
     cudaError_t e = ensure_wave_space(ctx, nsub);
     if (e != cudaSuccess) return e;
     WaveSpace W;
-    wave_space_carve(W, ctx->wave_mem, nsub, ctx->L.Ns, ctx->wave_qcap);
+    wave_space_carve(W, ctx->wave_mem, nsub, ctx->L.Ns, ctx->wave_qcap, ctx->L.C);
     // this pass uses its own subdomain count; the queues keep the allocated capacity
     W.nsub = (int)nsub;
     e = launch_pass<R>(p, W, ctx->h_wave_counters, ctx->st);
@@ -418,70 +420,101 @@ int check_status(pffrg_ctx* ctx) {
     return 0;
 }
 
-// compute_χ! (correlation_su2.jl:58-86) on a device action; the region
-// capacity of the cubature grows (x4) until no integral runs out of it
+// compute_χ! (correlation_su2.jl:58-86, correlation_u1_dm.jl:152-190) on a
+// device action.  Every (ω, site, component, box) integral starts with a
+// small region capacity; the integrals that run out of it are run again with
+// 8x the capacity, up to the reference's bound of 10^7 integrand evaluations
+// per cubature (10^7 / 34 cuts).
 int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh, int num_chi, double atol,
             double rtol, double* chi) {
-    if (ctx->symmetry != PFFRG_SU2) return ctx->fail(PFFRG_E_ARGS, "correlations are implemented for su2 only");
     if (num_chi < 1 || !chi_mesh || !chi) return ctx->fail(PFFRG_E_ARGS, "empty correlation mesh or output");
     const int Ns = ctx->L.Ns;
+    const int ncomp = ctx->L.C == 2 ? 1 : 3;  // χ, or χxx, χzz, χxy
+    const long long njobs = 9ll * ncomp * Ns * num_chi;
     if (num_chi > ctx->chi_n) {
         for (double** p : {&ctx->chi_mesh, &ctx->chi_box, &ctx->chi_out}) {
             if (*p) CK(cudaFree(*p));
             *p = nullptr;
         }
+        for (int** p : {&ctx->chi_jobs, &ctx->chi_over}) {
+            if (*p) CK(cudaFree(*p));
+            *p = nullptr;
+        }
         CK(cudaMalloc(&ctx->chi_mesh, sizeof(double) * num_chi));
-        CK(cudaMalloc(&ctx->chi_box, sizeof(double) * 9 * (size_t)Ns * num_chi));
-        CK(cudaMalloc(&ctx->chi_out, sizeof(double) * (size_t)Ns * num_chi));
+        CK(cudaMalloc(&ctx->chi_box, sizeof(double) * 9 * 3 * (size_t)Ns * num_chi));
+        CK(cudaMalloc(&ctx->chi_out, sizeof(double) * 3 * (size_t)Ns * num_chi));
+        CK(cudaMalloc(&ctx->chi_jobs, sizeof(int) * 9 * 3 * (size_t)Ns * num_chi));
+        CK(cudaMalloc(&ctx->chi_over, sizeof(int) * 9 * 3 * (size_t)Ns * num_chi));
         ctx->chi_n = num_chi;
     }
     CK(cudaMemcpyAsync(ctx->chi_mesh, chi_mesh, sizeof(double) * num_chi, cudaMemcpyHostToDevice, ctx->st));
-    const long long njobs = 9ll * Ns * num_chi;
-    const size_t max_bytes = (size_t)32 << 30;
-    for (;;) {
-        const size_t per_job = (size_t)ctx->chi_cap * (7 * sizeof(double) + sizeof(int));
-        const size_t need = per_job * (size_t)njobs;
-        if (need > ctx->chi_reg_bytes) {
+    CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
+    ChiArgs c;
+    c.L = ctx->L;
+    c.a = a;
+    c.mesh = ctx->mesh;
+    c.chi_mesh = ctx->chi_mesh;
+    c.num_chi = num_chi;
+    c.ncomp = ncomp;
+    c.exch = ctx->lat.exch;
+    c.Lam = Lam;
+    c.atol = atol;
+    c.rtol = rtol;
+    c.twoS = 2.0 * ctx->S;
+    c.box_out = ctx->chi_box;
+    c.chi = ctx->chi_out;
+    c.status = ctx->status;
+    const long long cap_max = 10000000 / 34 + 2;
+    const size_t budget = (size_t)16 << 30;
+    std::vector<int> todo(njobs), over;
+    for (long long j = 0; j < njobs; ++j) todo[j] = (int)j;
+    long long cap = 512;
+    while (!todo.empty()) {
+        const size_t per_job = (size_t)cap * (8 * sizeof(double) + 2 * sizeof(int));
+        const long long batch = std::max<long long>(1, std::min<long long>((long long)todo.size(),
+                                                                           (long long)(budget / per_job)));
+        if (per_job * (size_t)batch > ctx->chi_reg_bytes) {
             if (ctx->chi_reg) CK(cudaFree(ctx->chi_reg));
             if (ctx->chi_split) CK(cudaFree(ctx->chi_split));
             ctx->chi_reg = nullptr;
             ctx->chi_split = nullptr;
             ctx->chi_reg_bytes = 0;
-            CK(cudaMalloc(&ctx->chi_reg, sizeof(double) * 7 * (size_t)ctx->chi_cap * njobs));
-            CK(cudaMalloc(&ctx->chi_split, sizeof(int) * (size_t)ctx->chi_cap * njobs));
-            ctx->chi_reg_bytes = need;
+            CK(cudaMalloc(&ctx->chi_reg, sizeof(double) * 8 * (size_t)cap * batch));
+            CK(cudaMalloc(&ctx->chi_split, sizeof(int) * 2 * (size_t)cap * batch));
+            ctx->chi_reg_bytes = per_job * (size_t)batch;
         }
-        ChiArgs c;
-        c.L = ctx->L;
-        c.a = a;
-        c.mesh = ctx->mesh;
-        c.chi_mesh = ctx->chi_mesh;
-        c.num_chi = num_chi;
-        c.exch = ctx->lat.exch;
-        c.Lam = Lam;
-        c.atol = atol;
-        c.rtol = rtol;
-        c.twoS = 2.0 * ctx->S;
         c.reg = ctx->chi_reg;
         c.reg_split = ctx->chi_split;
-        c.cap = ctx->chi_cap;
-        c.box_out = ctx->chi_box;
-        c.chi = ctx->chi_out;
-        c.status = ctx->status;
-        ctx->launches += 2;
-        CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
-        CK(launch_chi(c, ctx->st));
-        int h = 0;
-        CK(cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
-        CK(cudaStreamSynchronize(ctx->st));
-        if (h) CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
-        if (h & 1) return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity exceeded in χ");
-        if (!(h & 2)) break;
-        if (per_job * 4 * (size_t)njobs > max_bytes)
-            return ctx->fail(PFFRG_E_LIMIT, "cubature regions of χ exceed %zu bytes", max_bytes);
-        ctx->chi_cap *= 4;
+        c.cap = cap;
+        std::vector<int> next;
+        for (size_t s = 0; s < todo.size(); s += (size_t)batch) {
+            const int nb = (int)std::min<size_t>((size_t)batch, todo.size() - s);
+            CK(cudaMemcpyAsync(ctx->chi_jobs, todo.data() + s, sizeof(int) * nb, cudaMemcpyHostToDevice, ctx->st));
+            ++ctx->launches;
+            CK(launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, ctx->st));
+            over.resize(nb);
+            CK(cudaMemcpyAsync(over.data(), ctx->chi_over, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->st));
+            CK(cudaStreamSynchronize(ctx->st));
+            for (int q = 0; q < nb; ++q)
+                if (over[q]) next.push_back(todo[s + q]);
+        }
+        todo.swap(next);
+        if (!todo.empty()) {
+            if (cap >= cap_max) return ctx->fail(PFFRG_E_LIMIT, "cubature of χ needs more than %lld regions", cap_max);
+            cap = std::min(cap * 8, cap_max);
+        }
     }
-    CK(cudaMemcpyAsync(chi, ctx->chi_out, sizeof(double) * (size_t)Ns * num_chi, cudaMemcpyDeviceToHost, ctx->st));
+    ++ctx->launches;
+    CK(launch_chi_sum(c, ctx->st));
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (h) {
+        CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
+        return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity exceeded in χ");
+    }
+    CK(cudaMemcpyAsync(chi, ctx->chi_out, sizeof(double) * ncomp * (size_t)Ns * num_chi, cudaMemcpyDeviceToHost,
+                       ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return 0;
 }
@@ -676,7 +709,7 @@ void pffrg_destroy(pffrg_ctx* ctx) {
                     ctx->mesh, ctx->log_bounds, ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig, ctx->sig_tmp, ctx->f_a, ctx->f_da,
                     ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
                     ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red, ctx->chi_reg, ctx->chi_split,
-                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh};
+                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
@@ -697,8 +730,8 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
         g_create_error = "invalid lattice view";
         return nullptr;
     }
-    if (symmetry != PFFRG_SU2) {
-        g_create_error = "only su2 symmetry is supported by this build";
+    if (symmetry != PFFRG_SU2 && symmetry != PFFRG_U1_DM) {
+        g_create_error = "unknown symmetry";
         return nullptr;
     }
     if (precision != PFFRG_FP64 && precision != PFFRG_MIXED) {
@@ -728,7 +761,8 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
     if (cudaSetDevice(device) != cudaSuccess) return bail("cudaSetDevice failed");
     if (check_mesh(ctx, mesh)) return bail(ctx->err);
     const int Ns = (int)lat->num_sites;
-    ctx->L = make_layout(Ns, (int)mesh->num_sigma, (int)mesh->num_omega, (int)mesh->num_nu, 2);
+    ctx->L = make_layout(Ns, (int)mesh->num_sigma, (int)mesh->num_omega, (int)mesh->num_nu,
+                         symmetry == PFFRG_SU2 ? 2 : 6);
     const Layout& L = ctx->L;
     if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return bail("stream creation failed");
 
@@ -927,6 +961,7 @@ int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
         p.nchan = 1;
         p.chan_of_y[0] = 0;
         set_slots<R>(p, r1, r1, r1, r1, kMaskReduced);
+        p.reduced = 1;
         p.prop_kind = PROP_PLAIN;
         p.prop_a = r1;
         p.prop_da = r1;

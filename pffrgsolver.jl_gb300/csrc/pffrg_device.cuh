@@ -129,6 +129,7 @@ struct Plan {
     int kernel;  // 0 none, 1 q1, 2 q2_1, 3 q2_2, 4 q3
     int src_ch;  // 0 s, 1 t, 2 u
     int exch;
+    int flags;   // bit 0: sgn_μν, bit 1: sgn_μ, bit 2: sgn_ν
     R sgn_d;
     R w[8];
     int off[8];
@@ -137,17 +138,17 @@ struct Plan {
 template <typename R>
 __device__ __forceinline__ void make_plan(Plan<R>& P, int chan, R w, R v, R vp, const SMesh<R>& M, int Ns,
                                           int NO, int Nn) {
-    bool ex = false, mp = false, sm = false, sn = false;
+    bool ex = false, mp = false, smn = false, sm = false, sn = false;
     if (chan == 0) {  // get_buffer_s (buffer.jl:87-124)
         if (w < (R)0) { w = -w; ex = !ex; }
         if (v < (R)0) { v = -v; ex = !ex; mp = !mp; sm = !sm; }
         if (vp < (R)0) { vp = -vp; mp = !mp; sn = !sn; }
     } else if (chan == 1) {  // get_buffer_t (buffer.jl:126-160)
-        if (w < (R)0) { w = -w; }
+        if (w < (R)0) { w = -w; smn = !smn; }
         if (v < (R)0) { v = -v; sm = !sm; }
         if (vp < (R)0) { vp = -vp; sn = !sn; }
     } else {  // get_buffer_u (buffer.jl:162-199)
-        if (w < (R)0) { w = -w; ex = !ex; }
+        if (w < (R)0) { w = -w; ex = !ex; smn = !smn; }
         if (v < (R)0) { v = -v; ex = !ex; mp = !mp; sn = !sn; }
         if (vp < (R)0) { vp = -vp; mp = !mp; sn = !sn; }
     }
@@ -160,6 +161,7 @@ __device__ __forceinline__ void make_plan(Plan<R>& P, int chan, R w, R v, R vp, 
         return;
     }
     P.exch = ex ? 1 : 0;
+    P.flags = (smn ? 1 : 0) | (sm ? 2 : 0) | (sn ? 4 : 0);
     P.src_ch = (chan == 1) ? 1 : ((chan == 0) == mp ? 2 : 0);
     P.sgn_d = ((sm ? -1 : 1) * (sn ? -1 : 1)) < 0 ? (R)-1 : (R)1;
     const Param<R> p1 = get_param(w, Om, iOm, NO);
@@ -233,6 +235,30 @@ __device__ __forceinline__ R plan_read(const Plan<R>& P, const R* __restrict__ q
             for (int k = 1; k < 8; ++k) val += P.w[k] * ldg(q + P.off[k] + s);
             return val;
     }
+}
+
+// apply_flags_su2 (action_su2.jl:73-92) for C = 2 and apply_flags_u1_dm
+// (action_u1_dm.jl:80-118) for C = 6: the component a plan reads for component
+// c (xx, zz, DM, dd, zd, dz for u1-dm) and the sign of its contribution
+template <typename R>
+__device__ __forceinline__ int comp_read(const Plan<R>& P, int C, int c, R& sgn) {
+    if (C == 2) {
+        sgn = c == 1 ? P.sgn_d : (R)1;
+        return c;
+    }
+    int s = 1;
+    const int f = P.flags;
+    if ((c == 4 || c == 5) && (f & 1)) s = -s;
+    if ((c == 3 || c == 5) && (f & 2)) s = -s;
+    if ((c == 3 || c == 4) && (f & 4)) s = -s;
+    int src = c;
+    if (P.exch) {
+        if (c == 2) s = -s;
+        else if (c == 4) src = 5;
+        else if (c == 5) src = 4;
+    }
+    sgn = (R)s;
+    return src;
 }
 
 __host__ __device__ constexpr int corners_of(int kernel) {

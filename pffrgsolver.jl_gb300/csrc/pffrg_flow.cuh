@@ -31,9 +31,11 @@
 // Node evaluation: a team of T lanes evaluates a batch of up to kBatch nodes.
 // The lanes first split the batch's scalar work (propagator halves,
 // bubbles.jl; 6 or 12 interpolation plans, buffer.jl + channel.jl), then each
-// lane gathers and combines the vertex on its sites (flow_su2_{s,t,u}.jl); the
-// t channel stages both slots in shared memory for the overlap sum
-// (flow_su2_t.jl:66-75) whose rows sit packed in shared memory.
+// lane gathers and combines the vertex on its sites (flow_su2_{s,t,u}.jl,
+// flow_u1_dm_{s,t,u}.jl); the t channel stages both slots in shared memory for
+// the overlap sum (flow_su2_t.jl:66-75) whose rows sit packed in shared memory.
+// Every kernel is templated on the vertex component count C: 2 for SU(2)
+// (spin, density), 6 for U(1)-DM (xx, zz, DM, dd, zd, dz).
 #pragma once
 
 #include "pffrg_internal.h"
@@ -42,26 +44,70 @@ namespace pffrg {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarps = 4;
-constexpr int kC = 2;  // SU(2): spin and density components
-constexpr int kBatch = 8;
 
-template <typename R>
+template <typename R, int C>
 struct NodeScratch {
     R p_half[2];
-    R loc[4];  // t channel: v3s, v3d, v4s, v4d
+    R loc[2 * C];  // t channel: local vertices v3[C], v4[C] at site 1
     Plan<R> plan[4][3];
 };
 
-// nodes per team batch: 8 per warp in total
-template <int T>
+// nodes per team batch: 8 per warp in total for SU(2), 4 for U(1)-DM
+template <int T, int C>
 struct BatchOf {
-    static constexpr int NB = kBatch * T / 32;
+    static constexpr int NB = (C == 2 ? 8 : 4) * T / 32;
 };
 
-template <typename R, int T>
+template <typename R, int T, int C>
 struct TeamScratch {
-    NodeScratch<R> node[BatchOf<T>::NB];
+    NodeScratch<R, C> node[BatchOf<T, C>::NB];
 };
+
+// ---------------------------------------------------------------------------
+// U(1)-DM bubbles of two vertices u, w (components xx, zz, DM, dd, zd, dz), the
+// reference's term order; the same combination serves the Katanin, left,
+// central, BSE and reduced kernels of a channel
+// ---------------------------------------------------------------------------
+// s channel (flow_u1_dm_s.jl:53-58)
+template <typename R>
+__device__ __forceinline__ void u1dm_s(const R* a, const R* b, R* g) {
+    g[0] = a[2] * b[5] - a[2] * b[4] + a[0] * b[3] + a[3] * b[0] - a[0] * b[1] - a[5] * b[2] + a[4] * b[2] - a[1] * b[0];
+    g[1] = a[1] * b[3] + a[3] * b[1] - a[5] * b[4] - (R)2 * a[0] * b[0] - (R)2 * a[2] * b[2] - a[4] * b[5];
+    g[2] = a[3] * b[2] + a[2] * b[3] - a[4] * b[0] - a[0] * b[5] - a[1] * b[2] + a[0] * b[4] - a[2] * b[1] + a[5] * b[0];
+    g[3] = -a[5] * b[5] + (R)2 * a[0] * b[0] + a[3] * b[3] + (R)2 * a[2] * b[2] - a[4] * b[4] + a[1] * b[1];
+    g[4] = a[4] * b[3] + a[3] * b[4] - (R)2 * a[2] * b[0] + a[5] * b[1] + a[1] * b[5] + (R)2 * a[0] * b[2];
+    g[5] = a[4] * b[1] + a[3] * b[5] + a[1] * b[4] + (R)2 * a[2] * b[0] + a[5] * b[3] - (R)2 * a[0] * b[2];
+}
+// u channel (flow_u1_dm_u.jl:52-57)
+template <typename R>
+__device__ __forceinline__ void u1dm_u(const R* a, const R* b, R* g) {
+    g[0] = -a[2] * b[5] - a[2] * b[4] + a[0] * b[3] + a[3] * b[0] + a[0] * b[1] + a[5] * b[2] + a[4] * b[2] + a[1] * b[0];
+    g[1] = a[1] * b[3] + a[3] * b[1] - a[5] * b[4] + (R)2 * a[0] * b[0] + (R)2 * a[2] * b[2] - a[4] * b[5];
+    g[2] = a[3] * b[2] + a[2] * b[3] - a[4] * b[0] + a[0] * b[5] + a[1] * b[2] + a[0] * b[4] + a[2] * b[1] - a[5] * b[0];
+    g[3] = -a[5] * b[5] + (R)2 * a[0] * b[0] + a[3] * b[3] + (R)2 * a[2] * b[2] - a[4] * b[4] + a[1] * b[1];
+    g[4] = a[4] * b[3] + a[3] * b[4] - (R)2 * a[2] * b[0] + a[5] * b[1] + a[1] * b[5] + (R)2 * a[0] * b[2];
+    g[5] = a[4] * b[1] + a[3] * b[5] + a[1] * b[4] - (R)2 * a[2] * b[0] + a[5] * b[3] + (R)2 * a[0] * b[2];
+}
+// t channel, local part: v1, v2 non-local at site i, v3, v4 local at site 1 (flow_u1_dm_t.jl:68-84)
+template <typename R>
+__device__ __forceinline__ void u1dm_t(const R* v1, const R* v2, const R* v3, const R* v4, R* g) {
+    g[0] = v1[2] * v4[5] - v1[2] * v4[4] + v1[0] * v4[3] - v1[0] * v4[1] + v3[3] * v2[0] + v3[5] * v2[2] -
+           v3[4] * v2[2] - v3[1] * v2[0];
+    g[1] = v1[1] * v4[3] + (R)2 * v1[4] * v4[2] - v1[4] * v4[4] + v1[1] * v4[1] - (R)2 * v1[1] * v4[0] -
+           v1[4] * v4[5] - (R)2 * v3[2] * v2[5] - v3[5] * v2[5] + v3[3] * v2[1] - (R)2 * v3[0] * v2[1] +
+           v3[1] * v2[1] - v3[4] * v2[5];
+    g[2] = v1[2] * v4[3] - v1[0] * v4[5] + v1[0] * v4[4] - v1[2] * v4[1] - v3[5] * v2[0] + v3[3] * v2[2] +
+           v3[4] * v2[0] - v3[1] * v2[2];
+    g[3] = -v1[5] * v4[5] + (R)2 * v1[3] * v4[0] + v1[3] * v4[1] - v1[5] * v4[4] - (R)2 * v1[5] * v4[2] +
+           v1[3] * v4[3] + (R)2 * v3[2] * v2[4] + (R)2 * v3[0] * v2[3] + v3[1] * v2[3] - v3[5] * v2[4] +
+           v3[3] * v2[3] - v3[4] * v2[4];
+    g[4] = v1[4] * v4[1] + v1[4] * v4[3] + (R)2 * v1[4] * v4[0] + v1[1] * v4[4] + (R)2 * v1[1] * v4[2] +
+           v1[1] * v4[5] + v3[4] * v2[3] + (R)2 * v3[2] * v2[3] + v3[3] * v2[4] + v3[1] * v2[4] -
+           (R)2 * v3[0] * v2[4] + v3[5] * v2[3];
+    g[5] = -(R)2 * v1[3] * v4[2] + v1[3] * v4[4] + v1[3] * v4[5] + v1[5] * v4[1] + v1[5] * v4[3] -
+           (R)2 * v1[5] * v4[0] + v3[4] * v2[1] + (R)2 * v3[0] * v2[5] + v3[3] * v2[5] + v3[5] * v2[1] -
+           (R)2 * v3[2] * v2[1] + v3[1] * v2[5];
+}
 
 // per-node argument triple (w, v, v') of buffer (slot, ch) for channel X
 // (flow_su2_s.jl:21-28, flow_su2_t.jl:21-43, flow_su2_u.jl:21-28)
@@ -118,8 +164,8 @@ __device__ __forceinline__ void slot_arg(int X, int slot, int ch, R v, R W, R V,
 }
 
 // vertex component c of one slot at one site (single value), for the t-channel local vertices
-template <typename R>
-__device__ __forceinline__ R gather_one(const PassArgs<R>& A, const NodeScratch<R>& ns, int slot, int c, int i,
+template <typename R, int C>
+__device__ __forceinline__ R gather_one(const PassArgs<R>& A, const NodeScratch<R, C>& ns, int slot, int c, int i,
                                         int exch_i) {
     const R* __restrict__ src = A.src[slot];
     R val = ldg(src + A.L.bare(c) + i);
@@ -127,29 +173,54 @@ __device__ __forceinline__ R gather_one(const PassArgs<R>& A, const NodeScratch<
     for (int ch = 0; ch < 3; ++ch) {
         const Plan<R>& P = ns.plan[slot][ch];
         if (P.kernel) {
-            const R* q = src + A.L.qbase(c, P.src_ch, P.kernel - 1);
+            R sgn;
+            const int cs = comp_read(P, C, c, sgn);
+            const R* q = src + A.L.qbase(cs, P.src_ch, P.kernel - 1);
             R acc = plan_read(P, q, P.exch ? exch_i : i);
-            val += (c == 1 ? P.sgn_d : (R)1) * acc;
+            val += sgn * acc;
         }
     }
     return val;
 }
 
-// both components of one slot on this lane's sites: v[c][k] = Γ_c(site tl + k T)
-template <typename R, int T, int SPL>
-__device__ __forceinline__ void gather_slot(const PassArgs<R>& A, const NodeScratch<R>& ns, int slot, int tl,
-                                            const int* site_ex, R v[kC][SPL]) {
+// all components of one slot on this lane's sites: v[c][k] = Γ_c(site tl + k T)
+template <typename R, int T, int SPL, int C>
+__device__ __forceinline__ void gather_slot(const PassArgs<R>& A, const NodeScratch<R, C>& ns, int slot, int tl,
+                                            const int* site_ex, R v[C][SPL]) {
     const R* __restrict__ src = A.src[slot];
     const int Ns = A.L.Ns;
 #pragma unroll
     for (int k = 0; k < SPL; ++k) {
         const int i = tl + k * T;
-        v[0][k] = (R)0;
-        v[1][k] = (R)0;
-        if (i < Ns) {
-            v[0][k] = ldg(src + A.L.bare(0) + i);
-            v[1][k] = ldg(src + A.L.bare(1) + i);
+#pragma unroll
+        for (int c = 0; c < C; ++c) v[c][k] = i < Ns ? ldg(src + A.L.bare(c) + i) : (R)0;
+    }
+    if constexpr (C != 2) {
+        // U(1)-DM: component by component, each with its own read component and sign
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            const Plan<R>& P = ns.plan[slot][ch];
+            const int kern = P.kernel;
+            if (!kern) continue;
+            const int ex = P.exch;
+            const int nc = corners_of(kern);
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                R sgn;
+                const int cs = comp_read(P, C, c, sgn);
+                const R* q = src + A.L.qbase(cs, P.src_ch, kern - 1);
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) {
+                    const int i = tl + k * T;
+                    if (i >= Ns) continue;
+                    const int s = ex ? site_ex[k] : i;
+                    R a = P.w[0] * ldg(q + P.off[0] + s);
+                    for (int qq = 1; qq < nc; ++qq) a += P.w[qq] * ldg(q + P.off[qq] + s);
+                    v[c][k] += sgn * a;
+                }
+            }
         }
+        return;
     }
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
@@ -228,12 +299,12 @@ __device__ __forceinline__ TaskInfo task_of(const PassArgs<R>& A, int sub, int j
     return TaskInfo{A.chan_of_y[y], t.x, t.y, t.z, t.w};
 }
 
-template <typename R, int T, int SPL>
+template <typename R, int T, int SPL, int C>
 struct Team {
     const PassArgs<R>& A;
     const SMesh<R>& M;
-    TeamScratch<R, T>& ts;
-    R* tmp;                 // t channel: [4][Ns] slot values of the current node
+    TeamScratch<R, T, C>& ts;
+    R* tmp;                 // t channel: [2 C][Ns] slot values of the current node
     const unsigned* rows;   // packed overlap rows (shared or global)
     const int* row_off;     // [Ns+1]
     int tl;                 // lane in team
@@ -243,7 +314,8 @@ struct Team {
     // Evaluate the integrand of channel X at up to NB nodes x[0..count) of one task:
     // g[j][c][k] = Γ_c(site tl + k T; x_j).  Team-collective: all lanes of the warp call it
     // together (inactive teams with count = 0).
-    __device__ void eval(const TaskInfo& ti, R W, R V, R VP, const double* x, int count, R g[BatchOf<T>::NB][kC][SPL]) {
+    __device__ void eval(const TaskInfo& ti, R W, R V, R VP, const double* x, int count,
+                         R g[BatchOf<T, C>::NB][C][SPL]) {
         const int X = ti.X;
         const int Ns = A.L.Ns;
         const int nslots = (X == 1) ? 4 : 2;
@@ -258,7 +330,7 @@ struct Team {
         // phase A: scalar work of all nodes of the batch, split over the team's lanes
         for (int it = tl; it < count * nitems; it += T) {
             const int j = it / nitems, item = it - j * nitems;
-            NodeScratch<R>& ns = ts.node[j];
+            NodeScratch<R, C>& ns = ts.node[j];
             const R v = (R)x[j];
             if (item < nprop) {
                 ns.p_half[item] = prop_half<R>(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a, A.prop_da, (R)A.Lam, v, W);
@@ -277,11 +349,11 @@ struct Team {
         }
         __syncwarp();
         if (X == 1) {
-            // local vertices at site 1 (flow_su2_t.jl:46-48)
+            // local vertices at site 1 (flow_su2_t.jl:46-48, flow_u1_dm_t.jl:44-46)
             const int e0 = ldg(A.exch);
-            for (int it = tl; it < count * 4; it += T) {
-                const int j = it >> 2, q = it & 3;
-                ts.node[j].loc[q] = gather_one(A, ts.node[j], 2 + (q >> 1), q & 1, 0, e0);
+            for (int it = tl; it < count * 2 * C; it += T) {
+                const int j = it / (2 * C), q = it - j * (2 * C);
+                ts.node[j].loc[q] = gather_one<R, C>(A, ts.node[j], 2 + q / C, q % C, 0, e0);
             }
         }
         __syncwarp();
@@ -292,19 +364,23 @@ struct Team {
                     for (int ch = 0; ch < 3; ++ch) (s < 2 ? cs : c1) += corners_of(ts.node[j].plan[s][ch].kernel);
                 unsigned long long v = cs * Ns + c1 + 3ull * Ns;
                 if (X == 1) v += 2ull * row_off[Ns];
-                alg += v * kC;
+                alg += v * C;
             }
         }
         // phase B: gathers and per-site combination, node by node
         for (int j = 0; j < mx; ++j) {
             const bool act = j < count;
-            const NodeScratch<R>& ns = ts.node[act ? j : 0];
+            const NodeScratch<R, C>& ns = ts.node[act ? j : 0];
             R p = (R)0;
-            R v1[kC][SPL], v2[kC][SPL];
+            R v1[C][SPL], v2[C][SPL];
             if (act) {
                 p = (nprop == 2) ? ns.p_half[0] + ns.p_half[1] : ns.p_half[0];
-                gather_slot<R, T, SPL>(A, ns, 0, tl, site_ex, v1);
-                gather_slot<R, T, SPL>(A, ns, 1, tl, site_ex, v2);
+                gather_slot<R, T, SPL, C>(A, ns, 0, tl, site_ex, v1);
+                gather_slot<R, T, SPL, C>(A, ns, 1, tl, site_ex, v2);
+            }
+            if constexpr (C != 2) {
+                eval_u1dm(X, j, act, p, ns, v1, v2, g);
+                continue;
             }
             if (act && X != 1) {
                 const R two = (X == 0) ? (R)-2 : (R)2;
@@ -355,6 +431,84 @@ struct Team {
             __syncwarp();
         }
     }
+
+    // phase B of one node for U(1)-DM (flow_u1_dm_{s,t,u}.jl); team-collective like eval
+    __device__ void eval_u1dm(int X, int j, bool act, R p, const NodeScratch<R, C>& ns, const R v1[C][SPL],
+                              const R v2[C][SPL], R g[BatchOf<T, C>::NB][C][SPL]) {
+        const int Ns = A.L.Ns;
+        if (act && X != 1) {
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                R a[C], b[C], h[C];
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    a[c] = v1[c][k];
+                    b[c] = v2[c][k];
+                }
+                if (X == 0) u1dm_s(a, b, h);
+                else u1dm_u(a, b, h);
+#pragma unroll
+                for (int c = 0; c < C; ++c) g[j][c][k] = -p * h[c];
+                if (A.reduced) {
+                    // the reduced s bubble of the SDE keeps xx, zz, dd (SDE_u1_dm.jl:38-46)
+                    g[j][2][k] = (R)0;
+                    g[j][4][k] = (R)0;
+                    g[j][5][k] = (R)0;
+                }
+            }
+        }
+        const bool tch = act && X == 1;
+        if (tch) {
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int i = tl + k * T;
+                if (i < Ns) {
+#pragma unroll
+                    for (int c = 0; c < C; ++c) {
+                        tmp[c * Ns + i] = v1[c][k];
+                        tmp[(C + c) * Ns + i] = v2[c][k];
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (tch) {
+            const R coef = -p * (R)-2;
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int i = tl + k * T;
+                R a[C], b[C], G[C];
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    a[c] = v1[c][k];
+                    b[c] = v2[c][k];
+                }
+                u1dm_t(a, b, ns.loc, ns.loc + C, G);
+#pragma unroll
+                for (int c = 0; c < C; ++c) G[c] = -p * G[c];
+                if (i < Ns) {
+                    // overlap sum (flow_u1_dm_t.jl:86-110)
+                    const int j0 = row_off[i], j1 = row_off[i + 1];
+                    for (int r = j0; r < j1; ++r) {
+                        const unsigned row = rows[r];
+                        const int ia = row & 0xff, ib = (row >> 8) & 0xff;
+                        const R mm = coef * (R)(row >> 16);
+                        const R* t1 = tmp + ia;
+                        const R* t2 = tmp + C * Ns + ib;
+                        G[0] += mm * (t1[0] * t2[0] - t1[2 * Ns] * t2[2 * Ns]);
+                        G[1] += mm * (t1[Ns] * t2[Ns] - t1[4 * Ns] * t2[5 * Ns]);
+                        G[2] += mm * (t1[2 * Ns] * t2[0] + t1[0] * t2[2 * Ns]);
+                        G[3] += mm * (t1[3 * Ns] * t2[3 * Ns] - t1[5 * Ns] * t2[4 * Ns]);
+                        G[4] += mm * (t1[4 * Ns] * t2[3 * Ns] + t1[Ns] * t2[4 * Ns]);
+                        G[5] += mm * (t1[3 * Ns] * t2[5 * Ns] + t1[5 * Ns] * t2[Ns]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < C; ++c) g[j][c][k] = G[c];
+            }
+        }
+        __syncwarp();
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -399,27 +553,27 @@ __device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const SMesh<R>&
 }
 
 // shared-memory layout common to the wave kernels
-template <typename R, int T>
+template <typename R, int T, int C>
 struct SmemLayout {
     static constexpr int NPW = 32 / T;
     size_t mesh, teams, tmp, rows, total;
     __host__ __device__ SmemLayout(int Ns, long long R_rows, bool rows_in_smem) {
         mesh = 0;
         teams = mesh + sizeof(SMesh<R>);
-        tmp = teams + sizeof(TeamScratch<R, T>) * kWarps * NPW;
-        rows = tmp + ((sizeof(R) * (size_t)kWarps * NPW * 4 * Ns + 15) & ~(size_t)15);
+        tmp = teams + sizeof(TeamScratch<R, T, C>) * kWarps * NPW;
+        rows = tmp + ((sizeof(R) * (size_t)kWarps * NPW * 2 * C * Ns + 15) & ~(size_t)15);
         total = rows + (rows_in_smem ? sizeof(unsigned) * (size_t)(R_rows + Ns + 1) : 0);
     }
 };
 
-template <typename R, int T, int SPL>
-__device__ __forceinline__ Team<R, T, SPL> make_team(const PassArgs<R>& A, unsigned char* smem, const SMesh<R>& M,
-                                                     int warp, int team, int tl) {
+template <typename R, int T, int SPL, int C>
+__device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, unsigned char* smem,
+                                                        const SMesh<R>& M, int warp, int team, int tl) {
     constexpr int NPW = 32 / T;
     const int Ns = A.L.Ns;
-    SmemLayout<R, T> lay(Ns, A.rows_total, A.rows_in_smem);
-    TeamScratch<R, T>* teams = reinterpret_cast<TeamScratch<R, T>*>(smem + lay.teams);
-    R* tmp = reinterpret_cast<R*>(smem + lay.tmp) + (size_t)(warp * NPW + team) * 4 * Ns;
+    SmemLayout<R, T, C> lay(Ns, A.rows_total, A.rows_in_smem);
+    TeamScratch<R, T, C>* teams = reinterpret_cast<TeamScratch<R, T, C>*>(smem + lay.teams);
+    R* tmp = reinterpret_cast<R*>(smem + lay.tmp) + (size_t)(warp * NPW + team) * 2 * C * Ns;
     const unsigned* rows;
     const int* roff;
     if (A.rows_in_smem) {
@@ -429,7 +583,7 @@ __device__ __forceinline__ Team<R, T, SPL> make_team(const PassArgs<R>& A, unsig
         rows = A.ov_rows;
         roff = A.ov_off;
     }
-    Team<R, T, SPL> t{A, M, teams[warp * NPW + team], tmp, rows, roff, tl, {}, 0, 0};
+    Team<R, T, SPL, C> t{A, M, teams[warp * NPW + team], tmp, rows, roff, tl, {}, 0, 0};
 #pragma unroll
     for (int k = 0; k < SPL; ++k) {
         const int i = tl + k * T;
@@ -438,12 +592,12 @@ __device__ __forceinline__ Team<R, T, SPL> make_team(const PassArgs<R>& A, unsig
     return t;
 }
 
-template <typename R, int T>
+template <typename R, int T, int C>
 __device__ __forceinline__ void load_common(const PassArgs<R>& A, unsigned char* smem) {
     SMesh<R>& M = *reinterpret_cast<SMesh<R>*>(smem);
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     if (A.rows_in_smem) {
-        SmemLayout<R, T> lay(A.L.Ns, A.rows_total, true);
+        SmemLayout<R, T, C> lay(A.L.Ns, A.rows_total, true);
         unsigned* rows = reinterpret_cast<unsigned*>(smem + lay.rows);
         for (long long k = threadIdx.x; k < A.rows_total; k += blockDim.x) rows[k] = ldg(A.ov_rows + k);
         int* roff = reinterpret_cast<int*>(rows + A.rows_total);
@@ -485,12 +639,12 @@ __device__ __forceinline__ bool sub_range(const PassArgs<R>& A, const TaskInfo& 
 }
 
 // the reference's convergence test of simps! on one team's sites; returns 1 when done
-template <int T, int SPL>
-__device__ __forceinline__ int simps_test(const double s_old[kC][SPL], const double s_new[kC][SPL], long long n,
+template <int T, int SPL, int C>
+__device__ __forceinline__ int simps_test(const double s_old[C][SPL], const double s_new[C][SPL], long long n,
                                           double atol, double rtol, int team, bool in_team0_only) {
     double ss_r = 0.0, ss_n = 0.0, ss_d = 0.0;
 #pragma unroll
-    for (int c = 0; c < kC; ++c)
+    for (int c = 0; c < C; ++c)
 #pragma unroll
         for (int k = 0; k < SPL; ++k) {
             const double rich = s_old[c][k] * (-1.0 / 15.0) + (16.0 / 15.0) * s_new[c][k];
@@ -510,19 +664,19 @@ __device__ __forceinline__ int simps_test(const double s_old[kC][SPL], const dou
 }
 
 // ---- wave 0: first five nodes of every subdomain, boundary nodes, first test ----
-template <typename R, int T, int SPL>
+template <typename R, int T, int SPL, int C>
 __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveSpace Wsp) {
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
-    load_common<R, T>(A, smem);
+    load_common<R, T, C>(A, smem);
     const SMesh<R>& M = *reinterpret_cast<const SMesh<R>*>(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
-    Team<R, T, SPL> tm = make_team<R, T, SPL>(A, smem, M, warp, team, tl);
+    Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
     const int Ns = A.L.Ns;
     const int jobs = 4 * A.eval + 1;
     const long long nwarps = (long long)gridDim.x * kWarps;
-    constexpr int NB = BatchOf<T>::NB;
+    constexpr int NB = BatchOf<T, C>::NB;
     for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < Wsp.nsub; base += nwarps * NPW) {
         const int sub = (int)(base + team);
         const bool valid = sub < Wsp.nsub;
@@ -557,14 +711,14 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
         R W = 0, V = 0, VP = 0;
         if (valid) task_freqs(A, M, ti, W, V, VP);
         // all teams of the warp evaluate together (cnt = 0 for idle teams), NB nodes at a time
-        R g[5][kC][SPL];
+        R g[5][C][SPL];
         for (int b = 0; b < 5; b += NB) {
-            R gb[NB][kC][SPL];
+            R gb[NB][C][SPL];
             const int nb = max(0, min(NB, cnt - b));
             tm.eval(ti, W, V, VP, x + b, nb, gb);
             for (int j = 0; j < NB && b + j < 5; ++j)
 #pragma unroll
-                for (int c = 0; c < kC; ++c)
+                for (int c = 0; c < C; ++c)
 #pragma unroll
                     for (int k = 0; k < SPL; ++k) g[b + j][c][k] = gb[j][c][k];
         }
@@ -573,9 +727,9 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
         const double we = 1.0 * (hi - lo) / 6.0, wm = 2.0 * (hi - lo) / 3.0;
         const double h = 0.5 * (hi - lo) / 2.0;
         const double wn = 4.0 * h / 3.0, wo = -2.0 * h / 3.0;
-        double s_old[kC][SPL], s_new[kC][SPL], f_new[kC][SPL];
+        double s_old[C][SPL], s_new[C][SPL], f_new[C][SPL];
 #pragma unroll
-        for (int c = 0; c < kC; ++c)
+        for (int c = 0; c < C; ++c)
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 s_old[c][k] = s_new[c][k] = f_new[c][k] = 0.0;
@@ -587,14 +741,14 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
                 s_new[c][k] = 0.5 * s_old[c][k] + wn * f_new[c][k] + wo * (double)g[2][c][k];
             }
         // every lane takes part in the test's team reductions
-        const int done = simps_test<T, SPL>(s_old, s_new, 2, A.atol, A.rtol, team, false);
+        const int done = simps_test<T, SPL, C>(s_old, s_new, 2, A.atol, A.rtol, team, false);
         if (!valid) continue;
-        double* sA = Wsp.stA + (size_t)sub * kC * Ns;
-        double* sB = Wsp.stB + (size_t)sub * kC * Ns;
+        double* sA = Wsp.stA + (size_t)sub * C * Ns;
+        double* sB = Wsp.stB + (size_t)sub * C * Ns;
         if (!simpson) {
             // boundary corrections (two nodes weighted by corrs) or an empty range
 #pragma unroll
-            for (int c = 0; c < kC; ++c)
+            for (int c = 0; c < C; ++c)
 #pragma unroll
                 for (int k = 0; k < SPL; ++k) {
                     const int i = tl + k * T;
@@ -604,7 +758,7 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
             continue;
         }
 #pragma unroll
-        for (int c = 0; c < kC; ++c)
+        for (int c = 0; c < C; ++c)
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 const int i = tl + k * T;
@@ -632,21 +786,21 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
 }
 
 // ---- wave k >= 1: evaluate queued chunks, one partial node sum per chunk ----
-template <typename R, int T, int SPL>
+template <typename R, int T, int SPL, int C>
 __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
-    load_common<R, T>(A, smem);
+    load_common<R, T, C>(A, smem);
     const SMesh<R>& M = *reinterpret_cast<const SMesh<R>*>(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
-    Team<R, T, SPL> tm = make_team<R, T, SPL>(A, smem, M, warp, team, tl);
+    Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
     const int Ns = A.L.Ns;
     const int jobs = 4 * A.eval + 1;
     const int nchunks = Wsp.counters[par];
     const long long nwarps = (long long)gridDim.x * kWarps;
-    constexpr int NB = BatchOf<T>::NB;
-    R g[NB][kC][SPL];
+    constexpr int NB = BatchOf<T, C>::NB;
+    R g[NB][C][SPL];
     for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < nchunks; base += nwarps * NPW) {
         const int chunk = (int)(base + team);
         const bool valid = chunk < nchunks;
@@ -668,9 +822,9 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
         int mx = cnt;
 #pragma unroll
         for (int o = T; o < 32; o <<= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
-        Acc<R> acc[kC][SPL];
+        Acc<R> acc[C][SPL];
 #pragma unroll
-        for (int c = 0; c < kC; ++c)
+        for (int c = 0; c < C; ++c)
 #pragma unroll
             for (int k = 0; k < SPL; ++k) acc[c][k] = Acc<R>{(R)0, (R)0};
         for (int b = 0; b < mx; b += NB) {
@@ -683,14 +837,14 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
             tm.eval(ti, W, V, VP, x, nb, g);
             for (int j = 0; j < nb; ++j)
 #pragma unroll
-                for (int c = 0; c < kC; ++c)
+                for (int c = 0; c < C; ++c)
 #pragma unroll
                     for (int k = 0; k < SPL; ++k) acc_add(acc[c][k], g[j][c][k]);
         }
         if (!valid) continue;
-        double* P = Wsp.part + (size_t)chunk * kC * Ns;
+        double* P = Wsp.part + (size_t)chunk * C * Ns;
 #pragma unroll
-        for (int c = 0; c < kC; ++c)
+        for (int c = 0; c < C; ++c)
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 const int i = tl + k * T;
@@ -704,7 +858,7 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
 }
 
 // ---- wave k >= 1: per subdomain, next Simpson sum, test, result or next level ----
-template <int T, int SPL>
+template <int T, int SPL, int C>
 __global__ void __launch_bounds__(kWarps * 32) decide_kernel(WaveSpace Wsp, int Ns, double atol, double rtol, int par) {
     constexpr int NPW = 32 / T;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -718,28 +872,28 @@ __global__ void __launch_bounds__(kWarps * 32) decide_kernel(WaveSpace Wsp, int 
         SubRec S;
         if (valid) S = Wsp.subs[sub];
         else S.n = 1, S.nchunk = 0, S.chunk0 = 0, S.lo = 0, S.hi = 0;
-        double* sA = Wsp.stA + (size_t)sub * kC * Ns;
-        double* sB = Wsp.stB + (size_t)sub * kC * Ns;
-        double s_old[kC][SPL], s_new[kC][SPL], f_new[kC][SPL];
+        double* sA = Wsp.stA + (size_t)sub * C * Ns;
+        double* sB = Wsp.stB + (size_t)sub * C * Ns;
+        double s_old[C][SPL], s_new[C][SPL], f_new[C][SPL];
         const double h = 0.5 * (S.hi - S.lo) / (double)S.n;
         const double wn = 4.0 * h / 3.0, wo = -2.0 * h / 3.0;
 #pragma unroll
-        for (int c = 0; c < kC; ++c)
+        for (int c = 0; c < C; ++c)
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 const int i = tl + k * T;
                 s_old[c][k] = s_new[c][k] = f_new[c][k] = 0.0;
                 if (!valid || i >= Ns) continue;
                 double f = 0.0;
-                for (int q = 0; q < S.nchunk; ++q) f += Wsp.part[(size_t)(S.chunk0 + q) * kC * Ns + c * Ns + i];
+                for (int q = 0; q < S.nchunk; ++q) f += Wsp.part[(size_t)(S.chunk0 + q) * C * Ns + c * Ns + i];
                 f_new[c][k] = f;
                 s_old[c][k] = sA[c * Ns + i];
                 s_new[c][k] = 0.5 * s_old[c][k] + wn * f + wo * sB[c * Ns + i];
             }
-        const int done = simps_test<T, SPL>(s_old, s_new, S.n, atol, rtol, team, false);
+        const int done = simps_test<T, SPL, C>(s_old, s_new, S.n, atol, rtol, team, false);
         if (!valid) continue;
 #pragma unroll
-        for (int c = 0; c < kC; ++c)
+        for (int c = 0; c < C; ++c)
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 const int i = tl + k * T;
@@ -759,7 +913,7 @@ __global__ void __launch_bounds__(kWarps * 32) decide_kernel(WaveSpace Wsp, int 
 }
 
 // ---- sum each task's subdomain results (range order, boundary last) into the output ----
-template <typename R>
+template <typename R, int C>
 __global__ void reduce_kernel(PassArgs<R> A, WaveSpace Wsp) {
     const int ct = blockIdx.x;  // channel task
     const int jobs = 4 * A.eval + 1;
@@ -773,34 +927,35 @@ __global__ void reduce_kernel(PassArgs<R> A, WaveSpace Wsp) {
         case 3: off = (int64_t)Ns * (ti.w1 + (int64_t)L.NO * ti.w3); break;
         default: off = (int64_t)Ns * (ti.w1 + (int64_t)L.NO * (ti.w2 + (int64_t)L.Nn * ti.w3)); break;
     }
-    for (int e = threadIdx.x; e < kC * Ns; e += blockDim.x) {
+    for (int e = threadIdx.x; e < C * Ns; e += blockDim.x) {
         const int c = e / Ns, i = e % Ns;
         double s = 0.0;
-        for (int j = 0; j < jobs; ++j) s += Wsp.stA[((size_t)ct * jobs + j) * kC * Ns + c * Ns + i];
+        for (int j = 0; j < jobs; ++j) s += Wsp.stA[((size_t)ct * jobs + j) * C * Ns + c * Ns + i];
         A.out[L.qbase(c, ti.X, ti.kernel - 1) + off + i] = s;
     }
 }
 
 // team width T = lanes per node batch, SPL = sites per lane
-template <typename R>
+template <typename R, int C>
 struct PassLauncher {
     template <int T, int SPL>
     static cudaError_t run(const PassArgs<R>& a0, WaveSpace& Wsp, int* h_counters, cudaStream_t st, int grid_cap) {
         // overlap rows in shared memory when they fit next to the rest
         PassArgs<R> a = a0;
-        a.rows_in_smem = SmemLayout<R, T>(a.L.Ns, a.rows_total, true).total <= (size_t)160 * 1024;
-        SmemLayout<R, T> lay(a.L.Ns, a.rows_total, a.rows_in_smem);
+        a.rows_in_smem = SmemLayout<R, T, C>(a.L.Ns, a.rows_total, true).total <= (size_t)160 * 1024;
+        SmemLayout<R, T, C> lay(a.L.Ns, a.rows_total, a.rows_in_smem);
         const size_t smem = lay.total;
+        if (smem > (size_t)227 * 1024) return cudaErrorInvalidConfiguration;
         cudaError_t e;
-        if ((e = cudaFuncSetAttribute(wave0_kernel<R, T, SPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+        if ((e = cudaFuncSetAttribute(wave0_kernel<R, T, SPL, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
             return e;
-        if ((e = cudaFuncSetAttribute(eval_kernel<R, T, SPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+        if ((e = cudaFuncSetAttribute(eval_kernel<R, T, SPL, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
             return e;
         constexpr int NPW = 32 / T;
         const int teams_per_block = kWarps * NPW;
         if ((e = cudaMemsetAsync(Wsp.counters, 0, sizeof(int) * 5, st))) return e;
         int g0 = (Wsp.nsub + teams_per_block - 1) / teams_per_block;
-        wave0_kernel<R, T, SPL><<<g0 < grid_cap ? g0 : grid_cap, kWarps * 32, smem, st>>>(a, Wsp);
+        wave0_kernel<R, T, SPL, C><<<g0 < grid_cap ? g0 : grid_cap, kWarps * 32, smem, st>>>(a, Wsp);
         if ((e = cudaGetLastError())) return e;
         int par = 1;
         for (int wave = 1; wave <= 21; ++wave) {
@@ -813,30 +968,30 @@ struct PassLauncher {
             if ((e = cudaMemsetAsync(Wsp.counters + (par ^ 1), 0, sizeof(int), st))) return e;
             if ((e = cudaMemsetAsync(Wsp.counters + 2 + (par ^ 1), 0, sizeof(int), st))) return e;
             int ge = (nchunks + teams_per_block - 1) / teams_per_block;
-            eval_kernel<R, T, SPL><<<ge < grid_cap ? ge : grid_cap, kWarps * 32, smem, st>>>(a, Wsp, par);
+            eval_kernel<R, T, SPL, C><<<ge < grid_cap ? ge : grid_cap, kWarps * 32, smem, st>>>(a, Wsp, par);
             if ((e = cudaGetLastError())) return e;
             int gd = (nact + teams_per_block - 1) / teams_per_block;
-            decide_kernel<T, SPL><<<gd < grid_cap ? gd : grid_cap, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol,
+            decide_kernel<T, SPL, C><<<gd < grid_cap ? gd : grid_cap, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol,
                                                                                            par);
             if ((e = cudaGetLastError())) return e;
             par ^= 1;
         }
-        reduce_kernel<R><<<a.ntasks * a.nchan, 128, 0, st>>>(a, Wsp);
+        reduce_kernel<R, C><<<a.ntasks * a.nchan, 128, 0, st>>>(a, Wsp);
         return cudaGetLastError();
     }
 };
 
-template <typename R>
+template <typename R, int C>
 cudaError_t launch_pass_impl(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st) {
     const int Ns = a.L.Ns;
     if (a.ntasks == 0) return cudaSuccess;
     const int cap = 152 * 32;
-    if (Ns <= 8) return PassLauncher<R>::template run<8, 1>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 16) return PassLauncher<R>::template run<16, 1>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 32) return PassLauncher<R>::template run<32, 1>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 64) return PassLauncher<R>::template run<32, 2>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 128) return PassLauncher<R>::template run<32, 4>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 256) return PassLauncher<R>::template run<32, 8>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 8) return PassLauncher<R, C>::template run<8, 1>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 16) return PassLauncher<R, C>::template run<16, 1>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 32) return PassLauncher<R, C>::template run<32, 1>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 64) return PassLauncher<R, C>::template run<32, 2>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 128) return PassLauncher<R, C>::template run<32, 4>(a, Wsp, h_counters, st, cap);
+    if (Ns <= 256) return PassLauncher<R, C>::template run<32, 8>(a, Wsp, h_counters, st, cap);
     return cudaErrorInvalidValue;
 }
 

@@ -46,6 +46,7 @@ struct PassArgs {
     double Lam, atol, rtol;
     int eval;
     double twoS;
+    int reduced;          // reduced s bubble of the SDE (U(1)-DM keeps xx, zz, dd only)
     unsigned long long* node_counter;  // optional: [0] integrand evaluations, [1] algorithmic values read
 };
 
@@ -61,27 +62,27 @@ struct SubRec {
 
 struct WaveSpace {
     SubRec* subs;    // [nsub]
-    double* stA;     // [nsub][2 Ns]: Simpson sum of the last level, then the result
-    double* stB;     // [nsub][2 Ns]: node sum of the last level's new nodes
+    double* stA;     // [nsub][C Ns]: Simpson sum of the last level, then the result
+    double* stB;     // [nsub][C Ns]: node sum of the last level's new nodes
     int4* queue[2];  // chunk records (sub, first node, count, -) of the current / next level
     int* active[2];  // subdomains with chunks in the current / next level
-    double* part;    // [qcap][2 Ns] chunk partial node sums
+    double* part;    // [qcap][C Ns] chunk partial node sums
     int* counters;   // [0..1] chunks, [2..3] active subdomains per parity, [4] queue overflow
     int nsub, qcap;
 };
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// bytes of the wave workspace for nsub subdomains, Ns sites and qcap chunks
-inline size_t wave_space_bytes(long long nsub, int Ns, long long qcap) {
-    const size_t vec = sizeof(double) * 2 * (size_t)Ns;
+// bytes of the wave workspace for nsub subdomains, C components on Ns sites and qcap chunks
+inline size_t wave_space_bytes(long long nsub, int Ns, long long qcap, int C) {
+    const size_t vec = sizeof(double) * C * (size_t)Ns;
     return align256(sizeof(SubRec) * nsub) + 2 * align256(vec * nsub) + 2 * align256(sizeof(int4) * qcap) +
            2 * align256(sizeof(int) * nsub) + align256(vec * qcap) + align256(sizeof(int) * 8);
 }
 
-inline void wave_space_carve(WaveSpace& W, void* base, long long nsub, int Ns, long long qcap) {
+inline void wave_space_carve(WaveSpace& W, void* base, long long nsub, int Ns, long long qcap, int C) {
     char* p = static_cast<char*>(base);
-    const size_t vec = sizeof(double) * 2 * (size_t)Ns;
+    const size_t vec = sizeof(double) * C * (size_t)Ns;
     W.subs = reinterpret_cast<SubRec*>(p);
     p += align256(sizeof(SubRec) * nsub);
     W.stA = reinterpret_cast<double*>(p);
@@ -105,6 +106,9 @@ inline void wave_space_carve(WaveSpace& W, void* base, long long nsub, int Ns, l
 
 template <typename R>
 cudaError_t launch_pass(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st);
+// the U(1)-DM (C = 6) instantiation, in its own translation unit
+template <typename R>
+cudaError_t launch_pass_u1dm(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st);
 
 // GK integrals of the self energy / corrections (QuadGK-equivalent)
 enum SigmaKind { SIG_FLOW = 0, SIG_CORR1 = 1, SIG_CORR2 = 2, SIG_SDE = 3 };
@@ -147,16 +151,20 @@ struct ChiArgs {
     const double* mesh;
     const double* chi_mesh;  // [num_chi]
     int num_chi;
+    int ncomp;               // 1 (SU(2)) or 3 (U(1)-DM: xx, zz, xy)
     const int* exch;
     double Lam, atol, rtol, twoS;
-    double* reg;             // [njobs][7][cap] region records
-    int* reg_split;          // [njobs][cap]
-    long long cap;           // regions per (ω, site, box) integral
-    double* box_out;         // [num_chi][Ns][9]
-    double* chi;             // [Ns][num_chi] column-major
+    double* reg;             // [job slot][8][cap] region records and heap keys
+    int* reg_split;          // [job slot][2][cap] split / cut-from words and heap indices
+    long long cap;           // regions per integral
+    double* box_out;         // [ncomp][num_chi][Ns][9]
+    double* chi;             // [ncomp][Ns][num_chi], each column-major
     int* status;             // bit 1: GK segments, bit 2: cubature regions exhausted
 };
-cudaError_t launch_chi(const ChiArgs& a, cudaStream_t st);
+// the box integrals of the listed jobs (overflow[slot] = 1: region capacity exhausted)
+cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st);
+// the local term and the sums of the boxes into χ
+cudaError_t launch_chi_sum(const ChiArgs& a, cudaStream_t st);
 
 // elementwise action kernels (FP64)
 cudaError_t launch_symmetrize(const Layout& L, const int* exch, double* a, cudaStream_t st);

@@ -167,7 +167,7 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     const size_t o_corrs = o;
     o = align_up(o + sizeof(double) * 6 * NO);
     const size_t o_wave = o;
-    o += wave_space_bytes(nsub, Ns, qcap);
+    o += wave_space_bytes(nsub, Ns, qcap, 2);
     if (o > kNoAllocScratchBytes)
         return fail(PFFRG_E_LIMIT,
                     "problem needs %zu bytes of scratch, the no-allocation entry point holds %zu "
@@ -181,7 +181,7 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     NK(cudaMemcpyAsync(base + o_bounds, bounds.data(), sizeof(double) * bounds.size(), cudaMemcpyHostToDevice, st));
     NK(cudaMemcpyAsync(base + o_tasks, tasks.data(), sizeof(int4) * tasks.size(), cudaMemcpyHostToDevice, st));
     WaveSpace W;
-    wave_space_carve(W, base + o_wave, nsub, Ns, qcap);
+    wave_space_carve(W, base + o_wave, nsub, Ns, qcap, 2);
     // the wave counters are the only scratch read before this call writes it
     NK(cudaMemsetAsync(W.counters, 0, sizeof(int) * 8, st));
 

@@ -191,14 +191,17 @@ __device__ __forceinline__ R site_value(const Layout& L, const R* __restrict__ s
     for (int ch = 0; ch < 3; ++ch) {
         const Plan<R>& P = pl[ch];
         if ((mask & (1 << ch)) && P.kernel) {
-            const R* q = src + L.qbase(c, P.src_ch, P.kernel - 1);
-            val += (c == 1 ? P.sgn_d : (R)1) * plan_read(P, q, P.exch ? ei : i);
+            R sgn;
+            const int cs = comp_read(P, L.C, c, sgn);
+            const R* q = src + L.qbase(cs, P.src_ch, P.kernel - 1);
+            val += sgn * plan_read(P, q, P.exch ? ei : i);
         }
     }
     return val;
 }
 
-// self-energy kernels (flow_su2_self.jl:2-102, SDE_su2.jl:45-77)
+// self-energy kernels (flow_su2_self.jl:2-102, SDE_su2.jl:45-77; U(1)-DM:
+// flow_u1_dm_self.jl:2-108, SDE_u1_dm.jl:59-91)
 template <typename R>
 struct SigmaKernel {
     const SigmaArgs<R>& A;
@@ -232,11 +235,22 @@ struct SigmaKernel {
             }
         }
         const int e0 = ldg(A.exch);
-        R val = (R)3 * site_value(L, src, p2, m_loc, 0, 0, e0) + site_value(L, src, p2, m_loc, 1, 0, e0);
-        const R twoS = (R)A.twoS;
-        for (int j = 0; j < L.Ns; ++j) {
-            const int ej = ldg(A.exch + j);
-            val -= (R)2 * (R)ldg(A.mult + j) * twoS * site_value(L, src, p1, m_non, 1, j, ej);
+        R val;
+        if (L.C == 2) {
+            val = (R)3 * site_value(L, src, p2, m_loc, 0, 0, e0) + site_value(L, src, p2, m_loc, 1, 0, e0);
+            const R twoS = (R)A.twoS;
+            for (int j = 0; j < L.Ns; ++j) {
+                const int ej = ldg(A.exch + j);
+                val -= (R)2 * (R)ldg(A.mult + j) * twoS * site_value(L, src, p1, m_non, 1, j, ej);
+            }
+        } else {
+            // 2 Γxx + Γzz + Γdd on site 1, Γdd over the lattice
+            val = (R)2 * site_value(L, src, p2, m_loc, 0, 0, e0) + site_value(L, src, p2, m_loc, 1, 0, e0) +
+                  site_value(L, src, p2, m_loc, 3, 0, e0);
+            for (int j = 0; j < L.Ns; ++j) {
+                const int ej = ldg(A.exch + j);
+                val -= (R)2 * (R)ldg(A.mult + j) * site_value(L, src, p1, m_non, 3, j, ej);
+            }
         }
         const R Lam = (R)A.Lam;
         switch (kind) {
@@ -362,9 +376,46 @@ struct ChiRegions {
     double* vol;
     double* val;
     double* err;
-    int* split;  // bit 0: split dimension, bit 1: pending evaluation, bit 2: made in the current round,
-                 // bits 3+: the region it was cut from (for the second half of a cut)
+    int* split;    // bit 0: split dimension; bits 1+: the region the second half of a cut was cut from
+    double* hkey;  // max-heap of region indices keyed by error
+    int* hidx;
 };
+
+// region heap of one integral (lane 0 only): the same sift rules as the oracle's
+__device__ __forceinline__ void heap_push(ChiRegions& R, int& hn, double k, int i) {
+    int h = hn++;
+    while (h > 0) {
+        const int p = (h - 1) / 2;
+        if (R.hkey[p] >= k) break;
+        R.hkey[h] = R.hkey[p];
+        R.hidx[h] = R.hidx[p];
+        h = p;
+    }
+    R.hkey[h] = k;
+    R.hidx[h] = i;
+}
+
+__device__ __forceinline__ int heap_pop(ChiRegions& R, int& hn) {
+    const int top = R.hidx[0];
+    const int n = --hn;
+    const double k = R.hkey[n];
+    const int i = R.hidx[n];
+    if (n > 0) {
+        int h = 0;
+        for (;;) {
+            const int l = 2 * h + 1, r = l + 1;
+            if (l >= n) break;
+            const int c = (r < n && R.hkey[r] > R.hkey[l]) ? r : l;
+            if (R.hkey[c] <= k) break;
+            R.hkey[h] = R.hkey[c];
+            R.hidx[h] = R.hidx[c];
+            h = c;
+        }
+        R.hkey[h] = k;
+        R.hidx[h] = i;
+    }
+    return top;
+}
 
 // point k of the 17 Genz-Malik points of region (c, h), the library's order
 __device__ __forceinline__ void gm_point(int k, double c0, double c1, double h0, double h1, double& x, double& y) {
@@ -423,11 +474,13 @@ __device__ __forceinline__ void gm_rule(const double* v, double vol, double& val
     split = diff[1] > diff[0] ? 1 : 0;
 }
 
-// compute_χ_kernel! (correlation_su2.jl:14-55) at (x, y) of [0,1]^2
+// compute_χ_kernel! (correlation_su2.jl:14-55) and compute_χ_kernel_{xx,zz,xy}!
+// (correlation_u1_dm.jl:14-149, component k = 0, 1, 2) at (x, y) of [0,1]^2
 struct ChiKernel {
     const ChiArgs& A;
     const SMesh<double>& M;
     int site;
+    int k;
     double w;
     __device__ double operator()(double x, double y) const {
         const Layout& L = A.L;
@@ -442,15 +495,29 @@ struct ChiKernel {
         const double twoS = A.twoS;
         const double tp2 = two_pi<double>() * two_pi<double>();
         const int ei = ldg(A.exch + site);
-        double val = -(twoS * twoS) * site_value<double>(L, A.a, p1, CH_ALL, 0, site, ei) / tp2;
+        double val;
+        if (L.C == 2) val = -(twoS * twoS) * site_value<double>(L, A.a, p1, CH_ALL, 0, site, ei) / tp2;
+        else val = -site_value<double>(L, A.a, p1, CH_ALL, k, site, ei) / tp2;  // Γxx, Γzz, ΓDM
         if (site == 0) {
             Plan<double> p2[3];
             make_plan<double>(p2[0], 0, v + vp, 0.5 * (v - w - vp), 0.5 * (v + w - vp), M, L.Ns, L.NO, L.Nn);
             make_plan<double>(p2[1], 1, -v + vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp), M, L.Ns, L.NO, L.Nn);
             make_plan<double>(p2[2], 2, -w, v, vp, M, L.Ns, L.NO, L.Nn);
-            const double vs = site_value<double>(L, A.a, p2, CH_ALL, 0, 0, ei);
-            const double vd = site_value<double>(L, A.a, p2, CH_ALL, 1, 0, ei);
-            val -= twoS * (vs - vd) / (2.0 * tp2);
+            auto g = [&](int c) { return site_value<double>(L, A.a, p2, CH_ALL, c, 0, ei); };
+            if (L.C == 2) {
+                const double vs = g(0);
+                const double vd = g(1);
+                val -= twoS * (vs - vd) / (2.0 * tp2);
+            } else if (k == 0) {
+                const double vzz = g(1), vdd = g(3);
+                val -= (vzz - vdd) / (2.0 * tp2);
+            } else if (k == 1) {
+                const double vxx = g(0), vzz = g(1), vdd = g(3);
+                val -= (2.0 * vxx - vzz - vdd) / (2.0 * tp2);
+            } else {
+                const double vzd = g(4), vdz = g(5);
+                val -= (vzd - vdz) / (2.0 * tp2);
+            }
         }
         const double Lam = A.Lam;
         val *= G_full(M, L.Nsig, A.a, Lam, v - 0.5 * w) * G_full(M, L.Nsig, A.a, Lam, v + 0.5 * w) * dv;
@@ -480,7 +547,7 @@ __device__ void chi_eval_regions(const F& f, ChiRegions R, const int* idx, int c
         gm_rule(fbuf + 17 * q, R.vol[r], val, err, sp);
         R.val[r] = val;
         R.err[r] = err;
-        R.split[r] = (R.split[r] & ~7) | sp | 4;
+        R.split[r] = (R.split[r] & ~1) | sp;
     }
     __syncwarp();
 }
@@ -488,7 +555,11 @@ __device__ void chi_eval_regions(const F& f, ChiRegions R, const int* idx, int c
 constexpr int kChiWarps = 2;
 constexpr int kChiPend = 64;  // regions evaluated per batch
 
-__global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A) {
+// One warp per (ω, site, component, box) integral of the job list; a job that
+// runs out of region capacity raises its overflow flag and is run again with a
+// larger capacity.
+__global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, const int* __restrict__ jobs, int njobs,
+                                                                  int* overflow) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SMesh<double>& M = *reinterpret_cast<SMesh<double>*>(smem_raw);
     double* fb = reinterpret_cast<double*>(smem_raw + sizeof(SMesh<double>));
@@ -496,12 +567,16 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A) {
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long job = (long long)blockIdx.x * kChiWarps + warp;
-    const long long njobs = (long long)A.num_chi * A.L.Ns * 9;
-    if (job >= njobs) return;
+    const long long slot = (long long)blockIdx.x * kChiWarps + warp;
+    if (slot >= njobs) return;
+    const long long job = jobs[slot];
     double* fbuf = fb + warp * kChiPend * 17;
     int* pidx = pend + warp * kChiPend;
-    const int box = (int)(job % 9), site = (int)((job / 9) % A.L.Ns), wi = (int)(job / (9ll * A.L.Ns));
+    // job = ((ω index * Ns + site) * ncomp + component) * 9 + box
+    const int box = (int)(job % 9);
+    const long long rj = job / 9;
+    const int k = (int)(rj % A.ncomp);
+    const int site = (int)((rj / A.ncomp) % A.L.Ns), wi = (int)(rj / ((long long)A.ncomp * A.L.Ns));
     const double wv = A.chi_mesh[wi];
     // integrate_χ_boxes: the nine boxes around the image of ±width = ±4 (Λ + ω / 2)
     const double width = 4.0 * (A.Lam + 0.5 * wv);
@@ -511,31 +586,35 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A) {
     const int row = 2 - box / 3, col = box % 3;  // the reference's order: top line first
     ChiRegions R;
     const size_t cap = A.cap;
-    const size_t off = (size_t)job * cap;
-    R.c0 = A.reg + off * 7;
+    const size_t off = (size_t)slot * cap;
+    R.c0 = A.reg + off * 8;
     R.c1 = R.c0 + cap;
     R.h0 = R.c1 + cap;
     R.h1 = R.h0 + cap;
     R.vol = R.h1 + cap;
     R.val = R.vol + cap;
     R.err = R.val + cap;
-    R.split = A.reg_split + off;
-    ChiKernel f{A, M, site, wv};
+    R.hkey = R.err + cap;
+    R.split = A.reg_split + off * 2;
+    R.hidx = R.split + cap;
+    ChiKernel f{A, M, site, k, wv};
     if (lane == 0) {
         R.c0[0] = 0.5 * (lo[col] + hi[col]);
         R.c1[0] = 0.5 * (lo[row] + hi[row]);
         R.h0[0] = 0.5 * (hi[col] - lo[col]);
         R.h1[0] = 0.5 * (hi[row] - lo[row]);
         R.vol[0] = (2.0 * R.h0[0]) * (2.0 * R.h1[0]);
+        R.split[0] = 0;
         pidx[0] = 0;
     }
     __syncwarp();
     chi_eval_regions(f, R, pidx, 1, fbuf);
-    int n = 1;
+    int n = 1, hn = 0;
+    if (lane == 0) heap_push(R, hn, R.err[0], 0);
     double tot_val = R.val[0], tot_err = R.err[0];
     long long numeval = 17;
     const long long maxevals = 10000000;
-    bool overflow = false;
+    bool over = false;
     auto converged = [&](double err, double val) { return !(err > A.atol && err > fabs(val) * A.rtol); };
     while (numeval < maxevals) {
         if (converged(tot_err, tot_val)) break;
@@ -543,32 +622,16 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A) {
         const double ee_val = tot_val;
         const int n0 = n;
         int npend = 0;
-        bool stop = false;
-        // pop the largest-error regions (cubature's parallel mode), bisect each into two pending ones
+        // pop the largest-error regions (the library's parallel mode) and halve each
         do {
-            double best = -1.0;
-            int bi = 0;
-            for (int k = lane; k < n; k += 32) {
-                const double e = (R.split[k] & 6) ? -1.0 : R.err[k];
-                if (e > best) {
-                    best = e;
-                    bi = k;
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) {
-                    best = ob;
-                    bi = oi;
-                }
-            }
-            if (best < 0.0) break;  // no region left to pop
             if (n + 1 > (int)cap) {
-                overflow = true;
-                stop = true;
+                over = true;
                 break;
             }
+            int bi = 0;
+            if (lane == 0) bi = heap_pop(R, hn);
+            bi = __shfl_sync(0xffffffffu, bi, 0);
+            hn = __shfl_sync(0xffffffffu, hn, 0);
             const double pv = R.val[bi], pe = R.err[bi];
             tot_val -= pv;
             tot_err -= pe;
@@ -592,8 +655,8 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A) {
                 }
                 R.vol[bi] *= 0.5;
                 R.vol[n] = (2.0 * R.h0[n]) * (2.0 * R.h1[n]);
-                R.split[bi] = 2;
-                R.split[n] = 2 | (bi << 3);
+                R.split[bi] = 0;
+                R.split[n] = bi << 1;
                 pidx[npend] = bi;
                 pidx[npend + 1] = n;
             }
@@ -603,30 +666,33 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A) {
             numeval += 34;
             if (converged(ee_err, ee_val)) break;
             if (npend + 2 > kChiPend) {
-                // evaluate this batch and keep popping in the same round
                 chi_eval_regions(f, R, pidx, npend, fbuf);
                 npend = 0;
             }
-        } while (numeval < maxevals);
+        } while (hn > 0 && numeval < maxevals);
         if (npend) chi_eval_regions(f, R, pidx, npend, fbuf);
-        // the round's regions join the heap, added to the totals in the order they were cut
-        for (int k = n0; k < n; ++k) {
-            const int tw = R.split[k] >> 3;
+        // the round's regions join the heap, in the order they were cut
+        for (int q = n0; q < n; ++q) {
+            const int tw = R.split[q] >> 1;
             tot_val += R.val[tw];
-            tot_val += R.val[k];
             tot_err += R.err[tw];
-            tot_err += R.err[k];
+            tot_val += R.val[q];
+            tot_err += R.err[q];
+            if (lane == 0) {
+                heap_push(R, hn, R.err[tw], tw);
+                heap_push(R, hn, R.err[q], q);
+            }
         }
+        hn = __shfl_sync(0xffffffffu, hn, 0);
         __syncwarp();
-        for (int k = lane; k < n; k += 32) R.split[k] &= ~6;
-        __syncwarp();
-        if (stop) break;
+        if (over) break;
     }
+    // the total in heap order, as the library sums it
     double I = 0.0;
-    for (int k = 0; k < n; ++k) I += R.val[k];
     if (lane == 0) {
+        for (int q = 0; q < hn; ++q) I += R.val[R.hidx[q]];
         A.box_out[job] = I;
-        if (overflow) atomicOr(A.status, 2);
+        overflow[slot] = over ? 1 : 0;
     }
 }
 
@@ -647,7 +713,8 @@ __global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
         const SMesh<double>& M;
         double w;
         __device__ double operator()(double v) const {
-            return A.twoS * G_full(M, A.L.Nsig, A.a, A.Lam, v - 0.5 * w) * G_full(M, A.L.Nsig, A.a, A.Lam, v + 0.5 * w) /
+            const double pref = A.L.C == 2 ? A.twoS : 1.0;
+            return pref * G_full(M, A.L.Nsig, A.a, A.Lam, v - 0.5 * w) * G_full(M, A.L.Nsig, A.a, A.Lam, v + 0.5 * w) /
                    (2.0 * two_pi<double>());
         }
     } g{A, M, wv};
@@ -657,25 +724,31 @@ __global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
     const int mode = map_points(pts, 5, t, s0);
     const double loc = warp_quadgk(g, mode, s0, t, 5, A.atol, A.rtol, segs[warp], A.status);
     if (lane == 0) {
+        const size_t plane = (size_t)A.L.Ns * A.num_chi;
         for (int i = 0; i < A.L.Ns; ++i) {
-            const double* b = A.box_out + ((size_t)wi * A.L.Ns + i) * 9;
-            double c = b[0];
-            for (int k = 1; k < 9; ++k) c += b[k];
-            if (i == 0) c += loc;
-            A.chi[i + (size_t)A.L.Ns * wi] = c;
+            for (int k = 0; k < A.ncomp; ++k) {
+                const double* b = A.box_out + (((size_t)wi * A.L.Ns + i) * A.ncomp + k) * 9;
+                double c = b[0];
+                for (int q = 1; q < 9; ++q) c += b[q];
+                if (i == 0 && k < 2) c += loc;  // χ (SU(2)) or χxx and χzz (U(1)-DM)
+                A.chi[k * plane + i + (size_t)A.L.Ns * wi] = c;
+            }
         }
     }
 }
 
-cudaError_t launch_chi(const ChiArgs& a, cudaStream_t st) {
-    const long long njobs = (long long)a.num_chi * a.L.Ns * 9;
+cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st) {
     const size_t smem = sizeof(SMesh<double>) + sizeof(double) * kChiWarps * kChiPend * 17 + sizeof(int) * kChiWarps * kChiPend;
     cudaError_t e = cudaFuncSetAttribute(chi_box_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    chi_box_kernel<<<(unsigned)((njobs + kChiWarps - 1) / kChiWarps), kChiWarps * 32, smem, st>>>(a);
-    if ((e = cudaGetLastError())) return e;
+    chi_box_kernel<<<(unsigned)((njobs + kChiWarps - 1) / kChiWarps), kChiWarps * 32, smem, st>>>(a, jobs, njobs,
+                                                                                                   overflow);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chi_sum(const ChiArgs& a, cudaStream_t st) {
     const size_t smem2 = sizeof(SMesh<double>) + sizeof(SegStore) * kSigWarps;
-    e = cudaFuncSetAttribute(chi_local_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    cudaError_t e = cudaFuncSetAttribute(chi_local_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
     if (e != cudaSuccess) return e;
     chi_local_kernel<<<(a.num_chi + kSigWarps - 1) / kSigWarps, kSigWarps * 32, smem2, st>>>(a);
     return cudaGetLastError();

@@ -14,7 +14,25 @@ static int grid_for(int64_t n, int block) {
     return (int)(g < cap ? (g > 0 ? g : 1) : cap);
 }
 
-// symmetrize!: q3[i,w,v,v'] = q3[x(i),w,v',v] for v < v', x = exchange (s, t) or identity (u)
+// image of (component c, channel ch) under v <-> v': the component it is read
+// from and the sign (SU(2): itself, +; U(1)-DM, action_u1_dm.jl:170-339: s and t
+// channels DM -> -DM, zd -> -dz, dz -> -zd; u channel zd -> -zd, dz -> -dz)
+__device__ __forceinline__ int swap_image(int C, int c, int ch, double& sgn) {
+    sgn = 1.0;
+    if (C == 2) return c;
+    if (ch == 2) {
+        if (c == 4 || c == 5) sgn = -1.0;
+        return c;
+    }
+    if (c == 2) sgn = -1.0;
+    if (c == 4 || c == 5) {
+        sgn = -1.0;
+        return 9 - c;
+    }
+    return c;
+}
+
+// symmetrize!: q3[i,w,v,v'] = ± q3'[x(i),w,v',v] for v < v', x = exchange (s, t) or identity (u)
 __global__ void symmetrize_kernel(Layout L, const int* __restrict__ exch, double* a) {
     const int Ns = L.Ns, NO = L.NO, Nn = L.Nn;
     const int64_t npair = (int64_t)Nn * (Nn - 1) / 2;
@@ -37,10 +55,14 @@ __global__ void symmetrize_kernel(Layout L, const int* __restrict__ exch, double
             ++v;
         }
         const int vp = v + 1 + (int)pr;
+        double sgn;
+        const int sc = swap_image(L.C, c, ch, sgn);
         double* q3 = a + L.qbase(c, ch, 3);
+        const double* s3 = a + L.qbase(sc, ch, 3);
         const int src = ch == 2 ? i : exch[i];
+        // the lower triangle read here is never written
         q3[i + (int64_t)Ns * (w + (int64_t)NO * (v + (int64_t)Nn * vp))] =
-            q3[src + (int64_t)Ns * (w + (int64_t)NO * (vp + (int64_t)Nn * v))];
+            sgn * s3[src + (int64_t)Ns * (w + (int64_t)NO * (vp + (int64_t)Nn * v))];
     }
 }
 
@@ -54,16 +76,18 @@ __global__ void symmetrize_add_kernel(Layout L, const int* __restrict__ exch, co
         const int64_t cc = e / L.chan;
         const int ch = (int)(cc % 3), c = (int)(cc / 3);
         const int64_t base = L.qbase(c, ch, 0);
+        double sgn;
+        const int64_t sbase = L.qbase(swap_image(L.C, c, ch, sgn), ch, 0);
         const int i = (int)(k % Ns);
         const int ex = ch == 2 ? i : exch[i];
         int64_t src;
         if (k < L.K1) {
-            src = base + (k - i + ex);
+            src = sbase + (k - i + ex);
         } else if (k < L.K1 + 2 * L.K2) {
             const bool first = k < L.K1 + L.K2;
             const int64_t kk = first ? k - L.K1 : k - L.K1 - L.K2;
             // q2_1 <- q2_2 image and q2_2 <- q2_1 image at the exchanged site
-            src = base + (first ? L.K1 + L.K2 : L.K1) + (kk - i + ex);
+            src = sbase + (first ? L.K1 + L.K2 : L.K1) + (kk - i + ex);
         } else {
             const int64_t kk = k - L.K1 - 2 * L.K2;
             int64_t r = kk / Ns;
@@ -71,9 +95,9 @@ __global__ void symmetrize_add_kernel(Layout L, const int* __restrict__ exch, co
             r /= NO;
             const int v = (int)(r % Nn);
             const int vp = (int)(r / Nn);
-            src = base + L.K1 + 2 * L.K2 + ex + (int64_t)Ns * (w + (int64_t)NO * (vp + (int64_t)Nn * v));
+            src = sbase + L.K1 + 2 * L.K2 + ex + (int64_t)Ns * (w + (int64_t)NO * (vp + (int64_t)Nn * v));
         }
-        a[base + k] += al[base + k] + al[src];
+        a[base + k] += al[base + k] + sgn * al[src];
     }
 }
 

@@ -108,8 +108,9 @@ class FlowContext:
         v1, v2 = _capi.action_view(a1), _capi.action_view(a2)
         self._check(self.lib.pffrg_bse(self.h, Lam, ctypes.byref(v1), ctypes.byref(v2), eval_, *gamma_tol), "bse")
 
-    def compute_chi(self, Lam: float, a: Action, chi_mesh, chi_tol=(1e-8, 1e-4)) -> np.ndarray:
-        """compute_χ! (correlation_su2.jl:58-86): χ[i, w] as an [Ns, num_chi] array (column-major)."""
+    def compute_chi(self, Lam: float, a: Action, chi_mesh, chi_tol=(1e-8, 1e-4)):
+        """compute_χ! (correlation_su2.jl:58-86): χ[i, w] as an [Ns, num_chi] array (column-major);
+        for u1-dm the list [χxx, χzz, χxy] of such arrays (correlation_u1_dm.jl:152-190)."""
         av = _capi.action_view(a)
         return self._chi(lambda mp, n, out: self.lib.pffrg_chi(self.h, Lam, ctypes.byref(av), mp, n, chi_tol[0],
                                                                 chi_tol[1], out), chi_mesh)
@@ -119,12 +120,15 @@ class FlowContext:
         return self._chi(lambda mp, n, out: self.lib.pffrg_chi_slot(self.h, Lam, slot, mp, n, chi_tol[0],
                                                                      chi_tol[1], out), chi_mesh)
 
-    def _chi(self, call, chi_mesh) -> np.ndarray:
+    def _chi(self, call, chi_mesh):
         mesh = np.ascontiguousarray(chi_mesh, dtype=np.float64)
-        out = np.zeros((self.num_sites, len(mesh)), dtype=np.float64, order="F")
+        ncomp = 1 if self.symmetry == "su2" else 3
+        n = self.num_sites * len(mesh)
+        out = np.zeros(ncomp * n, dtype=np.float64)
         dp = ctypes.POINTER(ctypes.c_double)
         self._check(call(mesh.ctypes.data_as(dp), len(mesh), out.ctypes.data_as(dp)), "chi")
-        return out
+        mats = [out[k * n:(k + 1) * n].reshape((self.num_sites, len(mesh)), order="F") for k in range(ncomp)]
+        return mats[0] if ncomp == 1 else mats
 
     # ---- device-resident interface ----
     def upload(self, slot: int, a: Action) -> None:

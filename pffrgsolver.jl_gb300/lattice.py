@@ -455,9 +455,45 @@ def init_model_triangular_dm_c3(J, lat: Lattice) -> None:
                 lat.add_bond(Jzz, i, j, 2, 2)
 
 
+def init_model_kagome_xxz_dm(J, lat: Lattice) -> None:
+    """Nearest-neighbour XXZ + out-of-plane DM model on the kagome lattice, J = [[J⊥, Jz, Dz]].
+
+    Not a model of the reference: it extends its bond-matrix convention
+    (model_triangular_dm_c3.jl:14-73: exchange[1,1] = exchange[2,2] = J⊥,
+    exchange[3,3] = Jz, exchange[1,2] = +D, exchange[2,1] = -D) with the usual
+    kagome DM pattern: D_ij = +Dz ẑ when i -> j runs counterclockwise around the
+    triangle that contains the bond, -Dz ẑ otherwise.
+    """
+    if lat.name != "kagome":
+        raise ValueError("Model requires kagome lattice.")
+    if len(J) != 1 or len(J[0]) != 3:
+        raise ValueError("Model takes nearest-neighbour couplings [[Jperp, Jz, Dz]] only.")
+    Jp, Jz, Dz = (float(x) for x in J[0])
+    max_nbs = _nbs_fast(1, 0, lat.vecs)
+    metric = max(get_metric(lat.sites[0], lat.sites[int(i)], lat.uc) for i in max_nbs)
+    _grow_test_sites(lat, metric)
+    nbs = [set(int(j) for j in _nbs_fast(1, i, lat.vecs)) for i in range(len(lat.sites))]
+    for i in range(len(lat.sites)):
+        for j in sorted(nbs[i]):
+            # the third corner of the bond's triangle: the common nearest neighbour of i and j
+            common = nbs[i] & nbs[j]
+            if len(common) == 1:
+                k = next(iter(common))
+                a = lat.vecs[j] - lat.vecs[i]
+                b = lat.vecs[k] - lat.vecs[i]
+                ccw = a[0] * b[1] - a[1] * b[0] > 0.0
+                d = Dz if ccw else -Dz
+                lat.add_bond(+d, i, j, 0, 1)
+                lat.add_bond(-d, i, j, 1, 0)
+            lat.add_bond(Jp, i, j, 0, 0)
+            lat.add_bond(Jp, i, j, 1, 1)
+            lat.add_bond(Jz, i, j, 2, 2)
+
+
 MODELS = {
     "heisenberg": init_model_heisenberg,
     "triangular-dm-c3": init_model_triangular_dm_c3,
+    "kagome-xxz-dm": init_model_kagome_xxz_dm,
 }
 
 

@@ -261,16 +261,20 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
     ctx.upload(_capi.SLOT_A, a)
     a_next = A.Action.empty_like(a)
     a_new = A.Action.empty_like(a)
-    chi = np.zeros((r.num_sites, m.num_chi), order="F")  # get_χ_empty
+    ncomp = 1 if ctx.symmetry == "su2" else 3
+    chi = [np.zeros((r.num_sites, m.num_chi), order="F") for _ in range(ncomp)]  # get_χ_empty
 
     def measure_chi():
-        # compute_χ! on the new state and the monotonicity test of measure (Launcher.jl:23-35)
+        # compute_χ! on the new state and the monotonicity test of measure (Launcher.jl:23-35):
+        # the static on-site value of the component with the largest |χ|
         nonlocal chi
         chi_prev = chi
-        chi = ctx.chi_slot(Lam, _capi.SLOT_NEXT, m.chi, chi_tol)
-        res.chi.append((Lam, np.array(m.chi), chi))
+        got = ctx.chi_slot(Lam, _capi.SLOT_NEXT, m.chi, chi_tol)
+        chi = [got] if ncomp == 1 else got
+        res.chi.append((Lam, np.array(m.chi), got))
+        idx = int(np.argmax([np.max(np.abs(c)) for c in chi]))
         with np.errstate(divide="ignore", invalid="ignore"):
-            return bool(np.float64(chi[0, 0]) / np.float64(chi_prev[0, 0]) >= 0.995)
+            return bool(np.float64(chi[idx][0, 0]) / np.float64(chi_prev[idx][0, 0]) >= 0.995)
 
     while Lam > Lf:
         eval_ = get_eval(Lam, min_eval, max_eval)
@@ -314,7 +318,7 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
             # new meshes and resampled state (launcher_1l.jl:177)
             a_new.buf[:] = a_next.buf
             m = resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m, a_next, a_new,
-                                 [chi] if chi_tol is not None else None)
+                                 chi if chi_tol is not None else None)
             ctx.set_mesh(m)
             ctx.upload(_capi.SLOT_A, a_new)
         else:

@@ -117,3 +117,86 @@ def test_chi_fp64(pkg, O, noise):
     assert got.shape == ref.shape
     assert rel_err(got, ref) < 1e-6
     assert np.array_equal(got, got_slot)
+
+
+U1DM_CASES = [("triangular", 3, "triangular-dm-c3", [[1.0, 0.8, 0.3]]), ("kagome", 3, "kagome-xxz-dm", [[1.0, 0.8, 0.2]])]
+
+
+@pytest.mark.parametrize("lattice,size,model,J", U1DM_CASES)
+@pytest.mark.parametrize("loops", [1, 2, 3])
+def test_dgamma_u1dm_fp64(pkg, O, lattice, size, model, J, loops):
+    """U(1)-DM right-hand side (flow_u1_dm_{s,t,u}.jl, flow_u1_dm_self.jl) on the GPU against the oracle."""
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = wl.Workload("t", lattice, size, model, J, loops, 1.0, 10, 4, 3, 0.1, 11, symmetry="u1-dm")
+    lat, r, m, a = wl.build_state(w)
+    P = O.Problem(r, m, symmetry="u1-dm")
+    ref = np.zeros_like(a.buf)
+    O.dsigma(P, 1.0, a.buf, ref)
+    O.dgamma(P, loops, 1.0, a.buf, ref, 2, sigma_corr=loops >= 3)
+    da = pkg.action.Action.empty_like(a)
+    with FlowContext(r, m, symmetry="u1-dm", precision="fp64") as ctx:
+        ctx.compute_dsigma(1.0, a, da)
+        ctx.compute_dgamma(1.0, a, da, 2, loops=loops, sigma_corr=loops >= 3)
+    assert rel_err(da.Σ, ref[: m.num_sigma]) < 1e-10
+    assert rel_err(da.buf, ref) < 1e-10
+
+
+def test_dgamma_u1dm_mixed(pkg, O):
+    """U(1)-DM mixed precision against the FP64 oracle (bound 1e-4 relative in the max norm)."""
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    model, J = "kagome-xxz-dm", [[1.0, 0.8, 0.2]]
+    w = wl.Workload("t", "kagome", 3, model, J, 2, 1.0, 10, 4, 3, 0.1, 11, symmetry="u1-dm")
+    lat, r, m, a = wl.build_state(w)
+    P = O.Problem(r, m, symmetry="u1-dm")
+    ref = np.zeros_like(a.buf)
+    O.dsigma(P, 1.0, a.buf, ref)
+    O.dgamma(P, 2, 1.0, a.buf, ref, 2)
+    da = pkg.action.Action.empty_like(a)
+    with FlowContext(r, m, symmetry="u1-dm", precision="mixed") as ctx:
+        ctx.compute_dsigma(1.0, a, da)
+        ctx.compute_dgamma(1.0, a, da, 2, loops=2)
+    e = rel_err(da.buf, ref)
+    print(f"u1-dm mixed vs FP64 oracle: {e:.3e}")
+    assert e < 1e-4
+
+
+def test_parquet_u1dm_fp64(pkg, O):
+    """compute_Σ! / compute_Γ! for U(1)-DM (SDE_u1_dm.jl, BSE_u1_dm_*.jl) against the oracle."""
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = wl.Workload("t", "triangular", 3, "triangular-dm-c3", [[1.0, 0.8, 0.3]], 1, 1.0, 10, 4, 3, 0.1, 11,
+                    symmetry="u1-dm")
+    lat, r, m, a = wl.build_state(w)
+    P = O.Problem(r, m, symmetry="u1-dm")
+    ref = np.zeros_like(a.buf)
+    corrs = O.sde(P, 1.0, a.buf, ref, 2)
+    ref2 = np.zeros_like(a.buf)
+    O.bse(P, 1.0, a.buf, ref2, corrs, 2)
+    a2 = pkg.action.Action.empty_like(a)
+    a3 = pkg.action.Action.empty_like(a)
+    with FlowContext(r, m, symmetry="u1-dm", precision="fp64") as ctx:
+        ctx.compute_sigma_sde(1.0, a, a2, 2)
+        ctx.compute_gamma_bse(1.0, a, a3, 2)
+    assert rel_err(a2.buf, ref) < 1e-10
+    assert rel_err(a3.buf, ref2) < 1e-10
+
+
+def test_chi_u1dm_fp64(pkg, O):
+    """χxx, χzz, χxy (correlation_u1_dm.jl:152-190) on the GPU against the oracle, bar 1e-6 of max|χ|."""
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = wl.Workload("t", "kagome", 3, "kagome-xxz-dm", [[1.0, 0.8, 0.2]], 1, 1.0, 10, 4, 3, 0.02, 11,
+                    symmetry="u1-dm")
+    lat, r, m, a = wl.build_state(w)
+    chi_mesh = np.array([0.0, 0.7])
+    ref = O.chi(O.Problem(r, m, symmetry="u1-dm"), 1.0, a.buf, chi_mesh)
+    with FlowContext(r, m, symmetry="u1-dm", precision="fp64") as ctx:
+        got = ctx.compute_chi(1.0, a, chi_mesh)
+    for g, x in zip(got, ref):
+        assert rel_err(g, x) < 1e-6
