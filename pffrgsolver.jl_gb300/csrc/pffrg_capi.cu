@@ -49,6 +49,10 @@ struct pffrg_ctx {
     double* h_scalars = nullptr;   // pinned [4]
     int* status = nullptr;
     unsigned long long* counter = nullptr;
+    // Gauss-Kronrod segment scratch: gk_slots integrals of gk_cap segments
+    double* gk_seg = nullptr;
+    long long gk_cap = 0, gk_slots = 0;
+    int gk_overflow = 0;
     // wave workspace of the passes (device scratch) and its host-visible counters
     void* wave_mem = nullptr;
     size_t wave_bytes = 0;
@@ -114,6 +118,14 @@ struct pffrg_ctx {
 
 namespace {
 
+// free a device buffer the context's stream may still be reading: wait for the stream first
+cudaError_t stream_free(cudaStream_t st, void* p) {
+    if (!p) return cudaSuccess;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    return cudaFree(p);
+}
+
 std::vector<int4> make_tasks(int NO, int Nn, int mode) {
     // mode 0: w2 >= w3 (compute.jl:73-107), 1: all w2 (compute.jl:135-170), 2: reduced s bubble (SDE.jl:76-86)
     std::vector<int4> T;
@@ -160,7 +172,7 @@ int upload_mesh(pffrg_ctx* ctx, const pffrg_mesh_view* m) {
 int upload_log_bounds(pffrg_ctx* ctx, double Lam, int eval) {
     const Layout& L = ctx->L;
     if (eval > ctx->bounds_cap) {
-        if (ctx->log_bounds) CK(cudaFree(ctx->log_bounds));
+        CK(stream_free(ctx->st, ctx->log_bounds));
         ctx->log_bounds = nullptr;
         CK(cudaMalloc(&ctx->log_bounds, sizeof(double) * 2 * L.NO * (eval + 1)));
         ctx->bounds_cap = eval;
@@ -232,7 +244,7 @@ cudaError_t ensure_wave_space(pffrg_ctx* ctx, long long nsub) {
     const long long qcap = 8 * nsub + 65536;
     if (nsub <= ctx->wave_nsub && ctx->wave_mem) return cudaSuccess;
     if (ctx->wave_mem) {
-        cudaError_t e = cudaFree(ctx->wave_mem);
+        cudaError_t e = stream_free(ctx->st, ctx->wave_mem);
         if (e != cudaSuccess) return e;
         ctx->wave_mem = nullptr;
     }
@@ -360,9 +372,32 @@ struct Src {
     const R* dtemp;
 };
 
+// Gauss-Kronrod segment scratch for `slots` integrals at the context's capacity
+int ensure_gk(pffrg_ctx* ctx, long long slots) {
+    if (ctx->gk_cap == 0) ctx->gk_cap = kGkCap0;
+    if (ctx->gk_seg && slots <= ctx->gk_slots) return 0;
+    slots = std::max(slots, ctx->gk_slots);
+    CK(stream_free(ctx->st, ctx->gk_seg));
+    ctx->gk_seg = nullptr;
+    CK(cudaMalloc(&ctx->gk_seg, sizeof(double) * 4 * (size_t)ctx->gk_cap * (size_t)slots));
+    ctx->gk_slots = slots;
+    return 0;
+}
+
+// after a Gauss-Kronrod overflow: 8x the segments per integral (up to QuadGK's evaluation cap)
+bool grow_gk(pffrg_ctx* ctx) {
+    if (!ctx->gk_overflow || ctx->gk_cap >= kGkCapMax) return false;
+    ctx->gk_overflow = 0;
+    ctx->gk_cap = std::min(ctx->gk_cap * 8, kGkCapMax);
+    stream_free(ctx->st, ctx->gk_seg);
+    ctx->gk_seg = nullptr;
+    return true;
+}
+
 template <typename R>
 int corrs_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* da, double atol, double rtol,
               double* out) {
+    if (int rc = ensure_gk(ctx, 6ll * ctx->L.NO)) return rc;
     CorrsArgs<R> c;
     c.NO = ctx->L.NO;
     c.Nn = ctx->L.Nn;
@@ -375,6 +410,8 @@ int corrs_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* da, dou
     c.atol = atol;
     c.rtol = rtol;
     c.corrs = out;
+    c.seg = ctx->gk_seg;
+    c.seg_cap = ctx->gk_cap;
     c.status = ctx->status;
     ++ctx->launches;
     CK(launch_corrs<R>(c, ctx->st));
@@ -384,6 +421,7 @@ int corrs_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* da, dou
 template <typename R>
 int sigma_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* aux, double* out, double atol,
               double rtol) {
+    if (int rc = ensure_gk(ctx, ctx->L.Nsig)) return rc;
     SigmaArgs<R> s;
     s.L = ctx->L;
     s.kind = kind;
@@ -397,6 +435,8 @@ int sigma_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* aux, do
     s.atol = atol;
     s.rtol = rtol;
     s.twoS = 2.0 * ctx->S;
+    s.seg = ctx->gk_seg;
+    s.seg_cap = ctx->gk_cap;
     s.status = ctx->status;
     ++ctx->launches;
     CK(launch_sigma<R>(s, ctx->st));
@@ -415,7 +455,8 @@ int check_status(pffrg_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->st));
     if (h) {
         CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
-        return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity exceeded (status %d)", h);
+        ctx->gk_overflow = 1;
+        return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity (%lld) exceeded", ctx->gk_cap);
     }
     return 0;
 }
@@ -433,11 +474,11 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     const long long njobs = 9ll * ncomp * Ns * num_chi;
     if (num_chi > ctx->chi_n) {
         for (double** p : {&ctx->chi_mesh, &ctx->chi_box, &ctx->chi_out}) {
-            if (*p) CK(cudaFree(*p));
+            CK(stream_free(ctx->st, *p));
             *p = nullptr;
         }
         for (int** p : {&ctx->chi_jobs, &ctx->chi_over}) {
-            if (*p) CK(cudaFree(*p));
+            CK(stream_free(ctx->st, *p));
             *p = nullptr;
         }
         CK(cudaMalloc(&ctx->chi_mesh, sizeof(double) * num_chi));
@@ -474,8 +515,8 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
         const long long batch = std::max<long long>(1, std::min<long long>((long long)todo.size(),
                                                                            (long long)(budget / per_job)));
         if (per_job * (size_t)batch > ctx->chi_reg_bytes) {
-            if (ctx->chi_reg) CK(cudaFree(ctx->chi_reg));
-            if (ctx->chi_split) CK(cudaFree(ctx->chi_split));
+            CK(stream_free(ctx->st, ctx->chi_reg));
+            CK(stream_free(ctx->st, ctx->chi_split));
             ctx->chi_reg = nullptr;
             ctx->chi_split = nullptr;
             ctx->chi_reg_bytes = 0;
@@ -504,14 +545,20 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
             cap = std::min(cap * 8, cap_max);
         }
     }
-    ++ctx->launches;
-    CK(launch_chi_sum(c, ctx->st));
-    int h = 0;
-    CK(cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
-    CK(cudaStreamSynchronize(ctx->st));
-    if (h) {
+    for (;;) {
+        if (int rc = ensure_gk(ctx, num_chi)) return rc;
+        c.seg = ctx->gk_seg;
+        c.seg_cap = ctx->gk_cap;
+        ++ctx->launches;
+        CK(launch_chi_sum(c, ctx->st));
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        if (!h) break;
         CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
-        return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity exceeded in χ");
+        ctx->gk_overflow = 1;
+        if (!grow_gk(ctx))
+            return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity exceeded in χ");
     }
     CK(cudaMemcpyAsync(chi, ctx->chi_out, sizeof(double) * ncomp * (size_t)Ns * num_chi, cudaMemcpyDeviceToHost,
                        ctx->st));
@@ -672,6 +719,15 @@ int absmax(pffrg_ctx* ctx, const double* a, double* dst) {
 
 }  // namespace
 
+// rerun a call whose Gauss-Kronrod integrals ran out of segments with 8x the capacity
+template <class Fn>
+int gk_retry(pffrg_ctx* ctx, Fn fn) {
+    for (;;) {
+        const int rc = fn();
+        if (rc != PFFRG_E_LIMIT || !ctx || !grow_gk(ctx)) return rc;
+    }
+}
+
 extern "C" {
 
 const char* pffrg_last_error(const pffrg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -709,7 +765,7 @@ void pffrg_destroy(pffrg_ctx* ctx) {
                     ctx->mesh, ctx->log_bounds, ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig, ctx->sig_tmp, ctx->f_a, ctx->f_da,
                     ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
                     ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red, ctx->chi_reg, ctx->chi_split,
-                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over};
+                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over, ctx->gk_seg};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
@@ -837,6 +893,9 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
     if (!cp) return bail("device initialisation failed");
     // hand the ABI's pinned copies of the 1-based tables back: nothing else to keep
     if (upload_mesh(ctx, mesh)) return bail(ctx->err);
+    // Gauss-Kronrod scratch for the largest launch of the right-hand side (dΣ or the boundary
+    // corrections), so that it is not reallocated between kernels of one call
+    if (ensure_gk(ctx, std::max<long long>(L.Nsig, 6ll * L.NO))) return bail(ctx->err);
     return ctx;
 }
 
@@ -869,7 +928,7 @@ int pffrg_download(pffrg_ctx* ctx, int slot, pffrg_action_view* a) {
     return 0;
 }
 
-int pffrg_dsigma(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, pffrg_action_view* da, double atol,
+static int dsigma_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, pffrg_action_view* da, double atol,
                  double rtol) {
     if (!ctx) return PFFRG_E_ARGS;
     CK(cudaSetDevice(ctx->device));
@@ -885,7 +944,12 @@ int pffrg_dsigma(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, pffrg_a
     return 0;
 }
 
-int pffrg_dgamma(pffrg_ctx* ctx, int loops, double Lam, const pffrg_action_view* a, pffrg_action_view* da, int eval,
+int pffrg_dsigma(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, pffrg_action_view* da, double atol,
+                 double rtol) {
+    return gk_retry(ctx, [&] { return dsigma_once(ctx, Lam, a, da, atol, rtol); });
+}
+
+static int dgamma_once(pffrg_ctx* ctx, int loops, double Lam, const pffrg_action_view* a, pffrg_action_view* da, int eval,
                  double gatol, double grtol, int sigma_corr, double satol, double srtol) {
     if (!ctx) return PFFRG_E_ARGS;
     if (loops < 1 || eval < 1) return ctx->fail(PFFRG_E_ARGS, "loops and eval must be positive");
@@ -905,7 +969,12 @@ int pffrg_dgamma(pffrg_ctx* ctx, int loops, double Lam, const pffrg_action_view*
     return 0;
 }
 
-int pffrg_rhs(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, int eval, double gatol,
+int pffrg_dgamma(pffrg_ctx* ctx, int loops, double Lam, const pffrg_action_view* a, pffrg_action_view* da, int eval,
+                 double gatol, double grtol, int sigma_corr, double satol, double srtol) {
+    return gk_retry(ctx, [&] { return dgamma_once(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol); });
+}
+
+static int rhs_once(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, int eval, double gatol,
               double grtol, double satol, double srtol, int sigma_corr) {
     if (!ctx) return PFFRG_E_ARGS;
     if (a_slot < 0 || a_slot >= PFFRG_NUM_SLOTS || da_slot < 0 || da_slot >= PFFRG_NUM_SLOTS || a_slot == da_slot)
@@ -931,7 +1000,12 @@ int pffrg_rhs(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, in
     return 0;
 }
 
-int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
+int pffrg_rhs(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, int eval, double gatol,
+              double grtol, double satol, double srtol, int sigma_corr) {
+    return gk_retry(ctx, [&] { return rhs_once(ctx, loops, Lam, a_slot, da_slot, eval, gatol, grtol, satol, srtol, sigma_corr); });
+}
+
+static int sde_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
               double grtol, double satol, double srtol) {
     if (!ctx) return PFFRG_E_ARGS;
     CK(cudaSetDevice(ctx->device));
@@ -980,7 +1054,12 @@ int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
     return 0;
 }
 
-int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double atol,
+int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
+              double grtol, double satol, double srtol) {
+    return gk_retry(ctx, [&] { return sde_once(ctx, Lam, a1, a2, eval, gatol, grtol, satol, srtol); });
+}
+
+static int bse_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double atol,
               double rtol) {
     if (!ctx) return PFFRG_E_ARGS;
     CK(cudaSetDevice(ctx->device));
@@ -1018,7 +1097,12 @@ int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
     return 0;
 }
 
-int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, double gatol, double grtol,
+int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double atol,
+              double rtol) {
+    return gk_retry(ctx, [&] { return bse_once(ctx, Lam, a1, a2, eval, atol, rtol); });
+}
+
+static int bs_step_once(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, double gatol, double grtol,
                   double satol, double srtol, int sigma_corr, double ode_atol, double ode_rtol, double* err,
                   double* abs_max_next) {
     if (!ctx) return PFFRG_E_ARGS;
@@ -1078,6 +1162,12 @@ int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, 
     if (abs_max_next) *abs_max_next = ctx->h_scalars[1];
     ctx->last_evals = evals;
     return 0;
+}
+
+int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, double gatol, double grtol,
+                  double satol, double srtol, int sigma_corr, double ode_atol, double ode_rtol, double* err,
+                  double* abs_max_next) {
+    return gk_retry(ctx, [&] { return bs_step_once(ctx, loops, Lam, dLam, eval, gatol, grtol, satol, srtol, sigma_corr, ode_atol, ode_rtol, err, abs_max_next); });
 }
 
 int pffrg_accept(pffrg_ctx* ctx) {

@@ -38,6 +38,8 @@
 // (spin, density), 6 for U(1)-DM (xx, zz, DM, dd, zd, dz).
 #pragma once
 
+#include <type_traits>
+
 #include "pffrg_internal.h"
 
 namespace pffrg {
@@ -367,6 +369,15 @@ struct Team {
                 alg += v * C;
             }
         }
+        if constexpr (C == 2) {
+            // every team of the warp passes the same two warp barriers, whatever its channel
+            if (X == 1) eval_t_stage(count, g);
+            else eval_su(X, count, g);
+            __syncwarp();
+            if (X == 1) eval_t_overlap(count, g);
+            __syncwarp();
+            return;
+        }
         // phase B: gathers and per-site combination, node by node
         for (int j = 0; j < mx; ++j) {
             const bool act = j < count;
@@ -429,6 +440,111 @@ struct Team {
                 }
             }
             __syncwarp();
+        }
+    }
+
+    // phase B of the SU(2) s and u channels (flow_su2_s.jl, flow_su2_u.jl): per node and site
+    __device__ void eval_su(int X, int count, R g[BatchOf<T, C>::NB][C][SPL]) {
+        const R two = (X == 0) ? (R)-2 : (R)2;
+        for (int j = 0; j < count; ++j) {
+            const NodeScratch<R, C>& ns = ts.node[j];
+            const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
+            R v1[C][SPL], v2[C][SPL];
+            gather_slot<R, T, SPL, C>(A, ns, 0, tl, site_ex, v1);
+            gather_slot<R, T, SPL, C>(A, ns, 1, tl, site_ex, v2);
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                g[j][0][k] = -p * (two * v1[0][k] * v2[0][k] + v1[0][k] * v2[1][k] + v1[1][k] * v2[0][k]);
+                g[j][1][k] = -p * ((R)3 * v1[0][k] * v2[0][k] + v1[1][k] * v2[1][k]);
+            }
+        }
+    }
+
+    // phase B of the SU(2) t channel for the whole batch (flow_su2_t.jl:46-81), first half:
+    // the non-local vertices of every node are gathered, their local part combined, and both
+    // slots staged in shared memory as [site][node] pairs (spin, density)
+    __device__ void eval_t_stage(int count, R g[BatchOf<T, C>::NB][C][SPL]) {
+        constexpr int NB = BatchOf<T, C>::NB;
+        using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
+        const int Ns = A.L.Ns;
+        R2* tb1 = reinterpret_cast<R2*>(tmp);  // [Ns][NB]
+        R2* tb2 = tb1 + (size_t)Ns * NB;
+        for (int j = 0; j < count; ++j) {
+            const NodeScratch<R, C>& ns = ts.node[j];
+            const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
+            R v1[C][SPL], v2[C][SPL];
+            gather_slot<R, T, SPL, C>(A, ns, 0, tl, site_ex, v1);
+            gather_slot<R, T, SPL, C>(A, ns, 1, tl, site_ex, v2);
+            const R v3s = ns.loc[0], v3d = ns.loc[1], v4s = ns.loc[2], v4d = ns.loc[3];
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int i = tl + k * T;
+                const R v1s = v1[0][k], v1d = v1[1][k], v2s = v2[0][k], v2d = v2[1][k];
+                g[j][0][k] = -p * ((R)-1 * v1s * v4s + v1s * v4d - (R)1 * v3s * v2s + v3d * v2s);
+                g[j][1][k] = -p * ((R)3 * v1d * v4s + v1d * v4d + (R)3 * v3s * v2d + v3d * v2d);
+                if (i < Ns) {
+                    tb1[(size_t)i * NB + j] = R2{v1s, v1d};
+                    tb2[(size_t)i * NB + j] = R2{v2s, v2d};
+                }
+            }
+        }
+    }
+
+    // second half: the overlap sums (flow_su2_t.jl:66-75) of the whole batch.  Each packed row
+    // is read once per batch, the vertex values of two nodes come in one 16-byte load (FP32),
+    // and a node's row sums are scaled by its -p (-2) (2S) at the end.  Nodes past `count` hold
+    // stale values whose sums are never used.
+    __device__ void eval_t_overlap(int count, R g[BatchOf<T, C>::NB][C][SPL]) {
+        constexpr int NB = BatchOf<T, C>::NB;
+        using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
+        const int Ns = A.L.Ns;
+        const R2* tb1 = reinterpret_cast<const R2*>(tmp);
+        const R2* tb2 = tb1 + (size_t)Ns * NB;
+        const R twoS = (R)A.twoS;
+#pragma unroll
+        for (int k = 0; k < SPL; ++k) {
+            const int i = tl + k * T;
+            R Ss[NB], Sd[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) Ss[j] = Sd[j] = (R)0;
+            if (i < Ns) {
+                const int j0 = row_off[i], j1 = row_off[i + 1];
+                for (int r = j0; r < j1; ++r) {
+                    const unsigned row = rows[r];
+                    const int ia = row & 0xff, ib = (row >> 8) & 0xff;
+                    const R m = (R)(row >> 16);
+                    const R2* a2 = tb1 + (size_t)ia * NB;
+                    const R2* b2 = tb2 + (size_t)ib * NB;
+                    if constexpr (sizeof(R) == 4) {
+                        const float4* a4 = reinterpret_cast<const float4*>(a2);
+                        const float4* b4 = reinterpret_cast<const float4*>(b2);
+#pragma unroll
+                        for (int q = 0; q < NB / 2; ++q) {
+                            const float4 a = a4[q], b = b4[q];
+                            Ss[2 * q] += m * a.x * b.x;
+                            Sd[2 * q] += m * a.y * b.y;
+                            Ss[2 * q + 1] += m * a.z * b.z;
+                            Sd[2 * q + 1] += m * a.w * b.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < NB; ++q) {
+                            const R2 a = a2[q], b = b2[q];
+                            Ss[q] += m * a.x * b.x;
+                            Sd[q] += m * a.y * b.y;
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                if (j >= count) continue;
+                const NodeScratch<R, C>& ns = ts.node[j];
+                const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
+                const R coef = -p * (R)-2 * twoS;
+                g[j][0][k] += coef * Ss[j];
+                g[j][1][k] += coef * Sd[j];
+            }
         }
     }
 
@@ -556,12 +672,16 @@ __device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const SMesh<R>&
 template <typename R, int T, int C>
 struct SmemLayout {
     static constexpr int NPW = 32 / T;
+    // t-channel staging per team: SU(2) both slots of the whole batch, U(1)-DM one node
+    __host__ __device__ static size_t tmp_per_team(int Ns) {
+        return C == 2 ? (size_t)4 * Ns * BatchOf<T, C>::NB : (size_t)2 * C * Ns;
+    }
     size_t mesh, teams, tmp, rows, total;
     __host__ __device__ SmemLayout(int Ns, long long R_rows, bool rows_in_smem) {
         mesh = 0;
         teams = mesh + sizeof(SMesh<R>);
-        tmp = teams + sizeof(TeamScratch<R, T, C>) * kWarps * NPW;
-        rows = tmp + ((sizeof(R) * (size_t)kWarps * NPW * 2 * C * Ns + 15) & ~(size_t)15);
+        tmp = (teams + sizeof(TeamScratch<R, T, C>) * kWarps * NPW + 15) & ~(size_t)15;  // 16-byte loads
+        rows = tmp + ((sizeof(R) * (size_t)kWarps * NPW * tmp_per_team(Ns) + 15) & ~(size_t)15);
         total = rows + (rows_in_smem ? sizeof(unsigned) * (size_t)(R_rows + Ns + 1) : 0);
     }
 };
@@ -573,7 +693,7 @@ __device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, un
     const int Ns = A.L.Ns;
     SmemLayout<R, T, C> lay(Ns, A.rows_total, A.rows_in_smem);
     TeamScratch<R, T, C>* teams = reinterpret_cast<TeamScratch<R, T, C>*>(smem + lay.teams);
-    R* tmp = reinterpret_cast<R*>(smem + lay.tmp) + (size_t)(warp * NPW + team) * 2 * C * Ns;
+    R* tmp = reinterpret_cast<R*>(smem + lay.tmp) + (size_t)(warp * NPW + team) * lay.tmp_per_team(Ns);
     const unsigned* rows;
     const int* roff;
     if (A.rows_in_smem) {

@@ -124,8 +124,15 @@ struct SigmaArgs {
     const int* mult;
     const double* mesh;
     double Lam, atol, rtol, twoS;
+    double* seg;        // Gauss-Kronrod segments: [Nsig - 1][4][seg_cap]
+    long long seg_cap;
     int* status;   // nonzero: segment capacity exceeded
 };
+
+// Gauss-Kronrod segments per integral: the first launch's capacity and the most a
+// 10^7-evaluation integral can use (QuadGK's maxevals, 30 evaluations per bisection)
+constexpr long long kGkCap0 = 2048;
+constexpr long long kGkCapMax = 10000000 / 30 + 8;
 
 template <typename R>
 cudaError_t launch_sigma(const SigmaArgs<R>& a, cudaStream_t st);
@@ -138,6 +145,8 @@ struct CorrsArgs {
     const double* mesh;
     double Lam, atol, rtol;
     double* corrs;  // [2,3,NO]
+    double* seg;          // Gauss-Kronrod segments: [6 NO][4][seg_cap]
+    long long seg_cap;
     int* status;
 };
 
@@ -159,7 +168,9 @@ struct ChiArgs {
     long long cap;           // regions per integral
     double* box_out;         // [ncomp][num_chi][Ns][9]
     double* chi;             // [ncomp][Ns][num_chi], each column-major
-    int* status;             // bit 1: GK segments, bit 2: cubature regions exhausted
+    double* seg;             // Gauss-Kronrod segments of the local term: [num_chi][4][seg_cap]
+    long long seg_cap;
+    int* status;             // bit 1: GK segments exhausted
 };
 // the box integrals of the listed jobs (overflow[slot] = 1: region capacity exhausted)
 cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st);

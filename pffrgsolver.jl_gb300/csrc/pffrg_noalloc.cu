@@ -166,6 +166,8 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     o = align_up(o + sizeof(int4) * tasks.size());
     const size_t o_corrs = o;
     o = align_up(o + sizeof(double) * 6 * NO);
+    const size_t o_gk = o;  // Gauss-Kronrod segments of the 6 NO boundary integrals
+    o = align_up(o + sizeof(double) * 4 * (size_t)kGkCap0 * 6 * NO);
     const size_t o_wave = o;
     o += wave_space_bytes(nsub, Ns, qcap, 2);
     if (o > kNoAllocScratchBytes)
@@ -198,6 +200,8 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     c.atol = atol;
     c.rtol = rtol;
     c.corrs = reinterpret_cast<double*>(base + o_corrs);
+    c.seg = reinterpret_cast<double*>(base + o_gk);
+    c.seg_cap = kGkCap0;
     c.status = W.counters + 5;
     NK(launch_corrs<double>(c, st));
 

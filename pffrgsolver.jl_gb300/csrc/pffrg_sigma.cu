@@ -17,7 +17,6 @@ namespace pffrg {
 
 constexpr unsigned kFullMask = 0xffffffffu;
 constexpr int kSigWarps = 2;
-constexpr int kMaxSeg = 384;
 
 __constant__ double c_gkx[8] = {-0.991455371120812639206854697526329, -0.949107912342758524526189684047851,
                                 -0.864864423359769072789712788640926, -0.741531185599394439863864773280788,
@@ -30,10 +29,21 @@ __constant__ double c_gkw[8] = {0.022935322010529224963732008058970, 0.063092092
 __constant__ double c_gw[4] = {0.129484966168869693270611432679082, 0.279705391489276667901467771423780,
                                0.381830050505118944950369775488975, 0.417959183673469387755102040816327};
 
+// segments of one adaptive integral: [a | b | I | E] arrays of `cap` entries in
+// device scratch (the integral's slot of the launch), node values in shared memory
 struct SegStore {
-    double a[kMaxSeg], b[kMaxSeg], I[kMaxSeg], E[kMaxSeg];
-    double f[32];
+    double* a;
+    double* b;
+    double* I;
+    double* E;
+    long long cap;
+    double* f;  // [32] shared
 };
+
+__device__ __forceinline__ SegStore seg_store(double* base, long long cap, long long slot, double* fsmem) {
+    double* s = base + (size_t)slot * 4 * (size_t)cap;
+    return SegStore{s, s + cap, s + 2 * cap, s + 3 * cap, cap, fsmem};
+}
 
 // node j of the 15-point rule on [a, b] (j < 7: a + (1 + x_j) s, j < 14: a + (1 - x_{j-7}) s, else a + s)
 __device__ __forceinline__ double gk_node(int j, double a, double b) {
@@ -81,7 +91,7 @@ __device__ __forceinline__ double mapped(const F& f, int mode, double s0, double
 // One adaptive GK integral per warp.  pts are already mapped to t.
 template <class F>
 __device__ double warp_quadgk(const F& f, int mode, double s0, const double* pts, int npts, double atol,
-                              double rtol, SegStore& S, int* status) {
+                              double rtol, SegStore S, int* status) {
     const int lane = threadIdx.x & 31;
     const long long maxevals = 10000000;
     int nseg = npts - 1;
@@ -124,7 +134,7 @@ __device__ double warp_quadgk(const F& f, int mode, double s0, const double* pts
                 bi = oi;
             }
         }
-        if (nseg >= kMaxSeg) {
+        if (nseg >= S.cap) {
             if (lane == 0) atomicOr(status, 1);
             break;
         }
@@ -271,18 +281,19 @@ template <typename R>
 __global__ void __launch_bounds__(kSigWarps * 32) sigma_kernel(SigmaArgs<R> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SMesh<R>& M = *reinterpret_cast<SMesh<R>*>(smem_raw);
-    SegStore* segs = reinterpret_cast<SegStore*>(smem_raw + sizeof(SMesh<R>));
+    double* fs = reinterpret_cast<double*>(smem_raw + sizeof(SMesh<R>));
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     __syncthreads();
     const int warp = threadIdx.x >> 5;
     const int i = 1 + blockIdx.x * kSigWarps + warp;  // σ index (index 0 is not computed)
     if (i >= A.L.Nsig) return;
+    const SegStore S = seg_store(A.seg, A.seg_cap, i - 1, fs + 32 * warp);
     SigmaKernel<R> f{A, M, A.mesh[i]};
     const double L2 = 2.0 * A.Lam, inf = INFINITY;
     const double pts[5] = {-inf, -L2, 0.0, L2, inf};
     double t[5], s0;
     const int mode = map_points(pts, 5, t, s0);
-    const double I = warp_quadgk(f, mode, s0, t, 5, A.atol, A.rtol, segs[warp], A.status);
+    const double I = warp_quadgk(f, mode, s0, t, 5, A.atol, A.rtol, S, A.status);
     if ((threadIdx.x & 31) == 0) A.out[i] = I;
 }
 
@@ -290,7 +301,7 @@ template <typename R>
 cudaError_t launch_sigma(const SigmaArgs<R>& a, cudaStream_t st) {
     const int n = a.L.Nsig - 1;
     if (n <= 0) return cudaSuccess;
-    const size_t smem = sizeof(SMesh<R>) + sizeof(SegStore) * kSigWarps;
+    const size_t smem = sizeof(SMesh<R>) + sizeof(double) * 32 * kSigWarps;
     cudaError_t e = cudaFuncSetAttribute(sigma_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     sigma_kernel<R><<<(n + kSigWarps - 1) / kSigWarps, kSigWarps * 32, smem, st>>>(a);
@@ -316,12 +327,13 @@ template <typename R>
 __global__ void __launch_bounds__(kSigWarps * 32) corrs_kernel(CorrsArgs<R> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SMesh<R>& M = *reinterpret_cast<SMesh<R>*>(smem_raw);
-    SegStore* segs = reinterpret_cast<SegStore*>(smem_raw + sizeof(SMesh<R>));
+    double* fs = reinterpret_cast<double*>(smem_raw + sizeof(SMesh<R>));
     load_mesh(M, A.mesh, A.Nsig, A.NO, A.Nn);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int job = blockIdx.x * kSigWarps + warp;
     if (job >= 6 * A.NO) return;
+    const SegStore S = seg_store(A.seg, A.seg_cap, job, fs + 32 * warp);
     const int side = job & 1, ch = (job >> 1) % 3, i = (job >> 1) / 3;
     const double* Os = A.mesh + A.Nsig;
     const double* ns = Os + A.NO;
@@ -337,7 +349,7 @@ __global__ void __launch_bounds__(kSigWarps * 32) corrs_kernel(CorrsArgs<R> A) {
         const double pts[2] = {side == 0 ? -inf : val, side == 0 ? -val : inf};
         double t[2], s0;
         const int mode = map_points(pts, 2, t, s0);
-        res = warp_quadgk(f, mode, s0, t, 2, A.atol, A.rtol, segs[warp], A.status) / bound;
+        res = warp_quadgk(f, mode, s0, t, 2, A.atol, A.rtol, S, A.status) / bound;
     }
     if (lane == 0) A.corrs[side + 2 * (ch + 3 * i)] = res;
 }
@@ -345,7 +357,7 @@ __global__ void __launch_bounds__(kSigWarps * 32) corrs_kernel(CorrsArgs<R> A) {
 template <typename R>
 cudaError_t launch_corrs(const CorrsArgs<R>& a, cudaStream_t st) {
     const int n = 6 * a.NO;
-    const size_t smem = sizeof(SMesh<R>) + sizeof(SegStore) * kSigWarps;
+    const size_t smem = sizeof(SMesh<R>) + sizeof(double) * 32 * kSigWarps;
     cudaError_t e = cudaFuncSetAttribute(corrs_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     corrs_kernel<R><<<(n + kSigWarps - 1) / kSigWarps, kSigWarps * 32, smem, st>>>(a);
@@ -700,12 +712,13 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, cons
 __global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SMesh<double>& M = *reinterpret_cast<SMesh<double>*>(smem_raw);
-    SegStore* segs = reinterpret_cast<SegStore*>(smem_raw + sizeof(SMesh<double>));
+    double* fs = reinterpret_cast<double*>(smem_raw + sizeof(SMesh<double>));
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wi = blockIdx.x * kSigWarps + warp;
     if (wi >= A.num_chi) return;
+    const SegStore S = seg_store(A.seg, A.seg_cap, wi, fs + 32 * warp);
     const double wv = A.chi_mesh[wi];
     const double ref = A.Lam + 0.5 * wv;
     struct G2 {
@@ -722,7 +735,7 @@ __global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
     const double pts[5] = {-inf, -2.0 * ref, 0.0, 2.0 * ref, inf};
     double t[5], s0;
     const int mode = map_points(pts, 5, t, s0);
-    const double loc = warp_quadgk(g, mode, s0, t, 5, A.atol, A.rtol, segs[warp], A.status);
+    const double loc = warp_quadgk(g, mode, s0, t, 5, A.atol, A.rtol, S, A.status);
     if (lane == 0) {
         const size_t plane = (size_t)A.L.Ns * A.num_chi;
         for (int i = 0; i < A.L.Ns; ++i) {
@@ -747,7 +760,7 @@ cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* 
 }
 
 cudaError_t launch_chi_sum(const ChiArgs& a, cudaStream_t st) {
-    const size_t smem2 = sizeof(SMesh<double>) + sizeof(SegStore) * kSigWarps;
+    const size_t smem2 = sizeof(SMesh<double>) + sizeof(double) * 32 * kSigWarps;
     cudaError_t e = cudaFuncSetAttribute(chi_local_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
     if (e != cudaSuccess) return e;
     chi_local_kernel<<<(a.num_chi + kSigWarps - 1) / kSigWarps, kSigWarps * 32, smem2, st>>>(a);

@@ -11,12 +11,14 @@ written by this module.
 from __future__ import annotations
 
 import math
+import os
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
 from . import action as A
+from . import disk, hdf5
 from . import frequency as F
 from . import lattice as L
 from . import _capi
@@ -191,6 +193,9 @@ class FlowResult:
     err: list = field(default_factory=list)
     abs_max: list = field(default_factory=list)
     rejected: int = 0
+    # wall seconds per part of the loop (the reference's timers, src/Flow/timers.jl): ODE steps on the
+    # device, correlations, host transfers and resampling
+    timers: dict = field(default_factory=lambda: {"steps": 0.0, "chi": 0.0, "transfer": 0.0, "resample": 0.0})
     rhs_evals: int = 0
     integrand_evals: int = 0
     parquet_iterations: int = 0
@@ -201,6 +206,57 @@ class FlowResult:
     action: A.Action | None = None
 
 
+class _Output:
+    """The ``f_obs`` / ``f_cp`` files of a run and the reference's measure (Launcher.jl:2-60):
+    Σ and χ of every accepted step to ``*_obs`` (once per cutoff), checkpoints to ``*_cp`` when ``ct``
+    hours have passed since the last one (``ct = 0``: now), or at every step within the last half
+    hour of the wall time ``wt``."""
+
+    def __init__(self, f: str, symmetry: str, wt: float, ct: float):
+        self.obs, self.cp = f + "_obs", f + "_cp"
+        self.symmetry, self.wt, self.ct = symmetry, wt, ct
+        self.t0 = self.t = time.time()
+
+    def exists(self) -> bool:
+        return os.path.isfile(self.obs) and os.path.isfile(self.cp)
+
+    def finished(self) -> bool:
+        with hdf5.File(self.obs, "r") as o, hdf5.File(self.cp, "r") as c:
+            return "finished" in o and "finished" in c
+
+    def start(self, r, euclidean: bool) -> None:
+        for p in (self.obs, self.cp):
+            if os.path.isfile(p):
+                os.remove(p)
+        for p in (self.obs, self.cp):
+            with hdf5.File(p, "cw") as fh:
+                disk.save_lattice(fh, r, euclidean)
+
+    def measure(self, Lam, dLam, m, a, chi, ct=None, wt=None) -> None:
+        ct = self.ct if ct is None else ct
+        wt = self.wt if wt is None else wt
+        with hdf5.File(self.obs, "cw") as o, hdf5.File(self.cp, "cw") as c:
+            if f"χ/{hdf5.julia_float_str(Lam)}" not in o:
+                disk.save_self(o, Lam, m, a)
+                disk.save_chi(o, Lam, self.symmetry, m, chi)
+            now = time.time()
+            h0 = (now - self.t0) / 3600.0
+            has_cp = f"a/{hdf5.julia_float_str(Lam)}" in c
+            if wt - h0 > 0.5:
+                if (now - self.t) / 3600.0 >= ct:
+                    if not has_cp:
+                        disk.checkpoint(c, Lam, dLam, m, a)
+                    self.t = now
+            elif 0.1 < wt - h0 <= 0.5 and not has_cp:
+                disk.checkpoint(c, Lam, dLam, m, a)
+
+    def finish(self) -> None:
+        for p in (self.obs, self.cp):
+            with hdf5.File(p, "cw") as fh:
+                if "finished" not in fh:
+                    fh["finished"] = True
+
+
 def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep: float = 0.0, S: float = 0.5,
            euclidean: bool = False, num_sigma: int = 25, num_omega: int = 15, num_nu: int = 10, num_chi: int = 10,
            p_sigma=F.DEFAULT_P_SIGMA, p_Os=F.DEFAULT_P_OMEGA, p_ns=F.DEFAULT_P_NU, p_Ot=F.DEFAULT_P_OMEGA,
@@ -208,8 +264,9 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
            max_iter: int = 50, min_eval: int = 10, max_eval: int = 100, sigma_tol=(1e-8, 1e-4),
            gamma_tol=(1e-8, 1e-4), chi_tol=(1e-8, 1e-4), parquet_tol=(1e-8, 1e-4), ode_tol=(1e-8, 1e-2),
            loops: int = 1, parquet: bool = True, sigma_corr: bool = True, initial: float = 5.0,
-           final: float = 0.05, bmin: float = 1e-4, bmax: float = 0.1, cps=(), precision: str = "mixed",
-           device: int = 0, measure=None, correlations: bool = True, verbose: bool = False) -> FlowResult:
+           final: float = 0.05, bmin: float = 1e-4, bmax: float = 0.1, cps=(), overwrite: bool = True,
+           wt: float = 23.5, ct: float = 1.0, precision: str = "mixed", device: int = 0, measure=None,
+           correlations: bool = True, verbose: bool = False) -> FlowResult:
     """Run the FRG flow from ``initial`` to ``final`` (launch!, Launcher.jl:565-773).
 
     After every accepted step the static correlations χ of the new state are
@@ -217,31 +274,64 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
     stops when the dominant on-site χ falls by more than 0.5 %, and χ steers
     the χ mesh of the resampling.  ``measure(Λ, dΛ, m, a, ctx)`` is an extra
     user callback after every accepted step; returning False stops the flow.
+
+    With a non-empty ``f`` the run writes the reference's ``f_obs`` / ``f_cp``
+    HDF5 files; ``overwrite = False`` resumes from the last checkpoint of
+    existing files (Launcher.jl:704-760).
     """
     t0 = time.perf_counter()
     if symmetry not in A.SYMMETRIES:
         raise ValueError(f"Symmetry {symmetry} unknown. Valid arguments are su2 and u1-dm.")
-    flat = [float(x) for j in J for x in j] + [float(A_rep)]
-    nrm = math.sqrt(sum(x * x for x in flat))
-    Jn = [[float(x) / nrm for x in j] for j in J]
-    A_n = A_rep / nrm
-    lat = L.get_lattice(name, size, euclidean=euclidean)
-    r = L.get_reduced_lattice(model, Jn, lat)
-    m = F.initial_mesh(initial, num_sigma, num_omega, num_nu, num_chi, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi,
-                       lins, bounds)
-    a = A.get_action_empty(symmetry, r, m, S=S)
-    A.init_action(lat, r, a)
-    A.add_repulsion(A_n, a)
     res = FlowResult()
+    out = _Output(f, symmetry, wt, ct) if f else None
+    p = (p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds)
+    if overwrite or out is None:
+        flat = [float(x) for j in J for x in j] + [float(A_rep)]
+        nrm = math.sqrt(sum(x * x for x in flat))
+        Jn = [[float(x) / nrm for x in j] for j in J]
+        A_n = A_rep / nrm
+        lat = L.get_lattice(name, size, euclidean=euclidean)
+        r = L.get_reduced_lattice(model, Jn, lat)
+        m = F.initial_mesh(initial, num_sigma, num_omega, num_nu, num_chi, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi,
+                           lins, bounds)
+        a = A.get_action_empty(symmetry, r, m, S=S)
+        A.init_action(lat, r, a)
+        A.add_repulsion(A_n, a)
+        if out:
+            out.start(r, euclidean)
+        Li, dLi = initial, bmax * initial
+    else:
+        if not out.exists():
+            res.reason = "found no existing output files"
+            return res
+        if out.finished():
+            res.finished = True
+            res.reason = "calculation has finished already"
+            return res
+        with hdf5.File(out.cp, "r") as c:
+            lat, r = disk.read_lattice(c)
+            Li, dLi, m_old, a_inter = disk.read_checkpoint(c, 0.0)
+        with hdf5.File(out.obs, "r") as o:
+            chi = disk.read_chi_all(o, Li, verbose=False)[1]
+        a = a_inter.copy()
+        m = resample_from_to(Li, *p, m_old, a_inter, a, chi)
+        parquet = False
     ctx = FlowContext(r, m, symmetry=symmetry, S=S, precision=precision, device=device)
     try:
         if parquet:
             res.parquet_iterations = launch_parquet(ctx, r, m, a, initial, max_iter, min_eval, max_eval, sigma_tol,
                                                     gamma_tol, parquet_tol, verbose=verbose)
-        _flow(ctx, r, m, a, res, loops=loops, sigma_corr=sigma_corr and loops >= 3, Li=initial, Lf=final,
-              dLi=bmax * initial, bmin=bmin, bmax=bmax, min_eval=min_eval, max_eval=max_eval, sigma_tol=sigma_tol,
-              gamma_tol=gamma_tol, ode_tol=ode_tol, p=(p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds),
-              cps=list(cps), measure=measure, chi_tol=chi_tol if correlations else None, verbose=verbose)
+            if out:
+                # the parquet solution is measured and checkpointed (parquet.jl:96-98)
+                ctx.upload(_capi.SLOT_NEXT, a)
+                chi0 = ctx.chi_slot(initial, _capi.SLOT_NEXT, m.chi, chi_tol)
+                out.measure(initial, dLi, m, a, chi0, ct=0.0, wt=math.inf)
+        _flow(ctx, r, m, a, res, loops=loops, sigma_corr=sigma_corr and loops >= 3, Li=Li, Lf=final,
+              dLi=dLi, bmin=bmin, bmax=bmax, min_eval=min_eval, max_eval=max_eval, sigma_tol=sigma_tol,
+              gamma_tol=gamma_tol, ode_tol=ode_tol, p=p, cps=list(cps), measure=measure,
+              chi_tol=chi_tol if correlations or out else None, out=out, verbose=verbose)
+        if out:
+            out.finish()
     finally:
         ctx.close()
     res.seconds = time.perf_counter() - t0
@@ -249,7 +339,7 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
 
 
 def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, Lf, dLi, bmin, bmax, min_eval,
-          max_eval, sigma_tol, gamma_tol, ode_tol, p, cps, measure, chi_tol=None, verbose=False):
+          max_eval, sigma_tol, gamma_tol, ode_tol, p, cps, measure, chi_tol=None, out=None, verbose=False):
     """Bogacki-Shampine loop of launch_1l!/2l!/ml! (launcher_1l.jl:56-198) with device stages."""
     p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds = p
     Lam, dLam = Li, dLi
@@ -264,26 +354,37 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
     ncomp = 1 if ctx.symmetry == "su2" else 3
     chi = [np.zeros((r.num_sites, m.num_chi), order="F") for _ in range(ncomp)]  # get_χ_empty
 
-    def measure_chi():
+    def measure_chi(ct=None):
         # compute_χ! on the new state and the monotonicity test of measure (Launcher.jl:23-35):
-        # the static on-site value of the component with the largest |χ|
+        # the static on-site value of the component with the largest |χ|; observables and
+        # checkpoints go to the output files
         nonlocal chi
         chi_prev = chi
+        t0 = time.perf_counter()
         got = ctx.chi_slot(Lam, _capi.SLOT_NEXT, m.chi, chi_tol)
+        res.timers["chi"] += time.perf_counter() - t0
         chi = [got] if ncomp == 1 else got
         res.chi.append((Lam, np.array(m.chi), got))
+        if out:
+            t1 = time.perf_counter()
+            out.measure(Lam, dLam, m, a_next, chi, ct=ct)
+            res.timers["files"] = res.timers.get("files", 0.0) + time.perf_counter() - t1
         idx = int(np.argmax([np.max(np.abs(c)) for c in chi]))
         with np.errstate(divide="ignore", invalid="ignore"):
             return bool(np.float64(chi[idx][0, 0]) / np.float64(chi_prev[idx][0, 0]) >= 0.995)
 
     while Lam > Lf:
         eval_ = get_eval(Lam, min_eval, max_eval)
+        t0 = time.perf_counter()
         err, amax = ctx.bs_step(Lam, dLam, eval_, loops=loops, gamma_tol=gamma_tol, sigma_tol=sigma_tol,
                                 sigma_corr=sigma_corr, ode_tol=ode_tol)
+        t_step = time.perf_counter() - t0
+        res.timers["steps"] += t_step
         res.rhs_evals += 4
         res.integrand_evals += ctx.last_integrand_evals
         if verbose:
-            print(f"Λ = {Lam:.6g}  dΛ = {dLam:.3g}  err = {err:.3g}  Γmax = {amax:.4g}", flush=True)
+            print(f"Λ = {Lam:.6g}  dΛ = {dLam:.3g}  eval = {eval_}  err = {err:.3g}  Γmax = {amax:.4g}  "
+                  f"step {t_step:.3f} s  nodes {ctx.last_integrand_evals}", flush=True)
         if err >= 10.0:
             res.reason = "integration has become unstable"
             break
@@ -301,26 +402,36 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
             res.dLam.append(dLam)
             res.err.append(err)
             res.abs_max.append(amax)
+            t0 = time.perf_counter()
             ctx.download(_capi.SLOT_NEXT, a_next)
+            res.timers["transfer"] += time.perf_counter() - t0
             if amax >= 1000.0:
                 res.reason = "vertex has diverged"
                 if chi_tol is not None:
-                    measure_chi()
+                    measure_chi(ct=0.0)
                 if measure:
                     measure(Lam, dLam, m, a_next, ctx)
                 break
-            monotone = measure_chi() if chi_tol is not None else True
+            # at a requested checkpoint the measurement checkpoints now (launcher_1l.jl:154-167)
+            at_cp = any(math.isclose(Lam, c, rel_tol=1.49e-8) for c in cps)
+            monotone = measure_chi(ct=0.0 if at_cp else None) if chi_tol is not None else True
             if measure and measure(Lam, dLam, m, a_next, ctx) is False:
                 monotone = False
             if not monotone:
                 res.reason = "flowing correlations show non-monotonicity"
+                if out:
+                    out.measure(Lam, dLam, m, a_next, chi, ct=0.0)
                 break
             # new meshes and resampled state (launcher_1l.jl:177)
+            t0 = time.perf_counter()
             a_new.buf[:] = a_next.buf
             m = resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m, a_next, a_new,
                                  chi if chi_tol is not None else None)
+            t1 = time.perf_counter()
+            res.timers["resample"] += t1 - t0
             ctx.set_mesh(m)
             ctx.upload(_capi.SLOT_A, a_new)
+            res.timers["transfer"] += time.perf_counter() - t1
         else:
             dLam = next_dlam(dLam)
             res.rejected += 1

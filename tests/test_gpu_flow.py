@@ -106,3 +106,48 @@ def test_parquet_converges(pkg):
     res = launch("t", "square", 3, "heisenberg", "su2", [[1.0]], num_sigma=10, num_omega=4, num_nu=3, num_chi=4,
                  initial=5.0, final=5.0, parquet=True, precision="fp64", parquet_tol=(1e-8, 1e-6))
     assert 1 <= res.parquet_iterations < 50
+
+
+def test_launch_writes_and_resumes_files(pkg, tmp_path):
+    """launch! with output files (measure, Launcher.jl:2-60): Σ and χ of every accepted step in *_obs,
+    checkpoints in *_cp (ct = 0: every step), the finished flags; an interrupted run resumes from its
+    last checkpoint with overwrite = false (Launcher.jl:704-760)."""
+    from pffrg_gb300 import disk as D, hdf5 as H
+    from pffrg_gb300.launcher import launch
+
+    kw = dict(num_sigma=10, num_omega=4, num_nu=3, num_chi=4, initial=5.0, parquet=False, precision="fp64",
+              ct=0.0)
+    f = str(tmp_path / "run")
+    res = launch(f, "square", 3, "heisenberg", "su2", [[1.0]], final=3.0, **kw)
+    assert res.finished
+    with H.File(f + "_obs", "r") as o, H.File(f + "_cp", "r") as c:
+        assert o.read("finished") is True and c.read("finished") is True
+        cut = sorted((float(k) for k in o.keys("χ")), reverse=True)
+        assert np.allclose(cut, res.Lam)
+        assert o.read("reduced_lattice/model") == "heisenberg"
+        Lam, dLam, m, a = D.read_checkpoint(c, 0.0)
+        assert Lam == res.Lam[-1]
+        assert np.array_equal(a.buf, res.action.buf)
+
+    # interrupted after two accepted steps, then resumed
+    g = str(tmp_path / "cut")
+
+    class Stop(Exception):
+        pass
+
+    seen = []
+
+    def crash(Lam, dLam, m, a, ctx):
+        seen.append(Lam)
+        if len(seen) == 2:
+            raise Stop()
+
+    with pytest.raises(Stop):
+        launch(g, "square", 3, "heisenberg", "su2", [[1.0]], final=3.0, measure=crash, **kw)
+    with H.File(g + "_cp", "r") as c:
+        assert "finished" not in c
+        assert min(float(k) for k in c.keys("a")) == pytest.approx(seen[-1])
+    res2 = launch(g, "square", 3, "heisenberg", "su2", [[1.0]], final=3.0, overwrite=False, **kw)
+    assert res2.finished and res2.Lam[-1] <= 3.0 + 1e-12 and res2.Lam[0] < seen[-1]
+    res3 = launch(g, "square", 3, "heisenberg", "su2", [[1.0]], final=3.0, overwrite=False, **kw)
+    assert res3.reason == "calculation has finished already"
