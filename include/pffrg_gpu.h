@@ -145,6 +145,13 @@ int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, 
 /* accept the step: slot A <- slot NEXT (the reference keeps a_inter for the resampling) */
 int pffrg_accept(pffrg_ctx* ctx);
 
+/* Quadrature levels driven by the device (default 1): the passes read their work
+ * counts on the device and need no host round trip per level, so a whole
+ * right-hand side is one asynchronous launch sequence; 0 selects the
+ * host-driven loop (host reads the level's counts and stops at the last
+ * level).  Both give identical results.  No counterpart in the reference. */
+int pffrg_set_async_waves(pffrg_ctx* ctx, int on);
+
 /* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86,
  * correlation_u1_dm.jl:152-190): static spin correlations χ[i, w] of the
  * action `a` at Λ on the frequencies chi_mesh[0..num_chi), written
@@ -171,6 +178,8 @@ typedef struct pffrg_stats {
     double rhs_ms;              /* summed duration of pffrg_rhs calls since the last reset */
     int64_t pass_launches;      /* channel-task kernel launches since the last reset */
     int64_t launches;           /* all kernel launches since the last reset */
+    int64_t chi_evals;          /* χ integrand evaluations (cubature points) of the last pffrg_chi call */
+    int64_t chi_regions_max;    /* largest region count of one χ integral in that call */
 } pffrg_stats;
 int pffrg_set_timing(pffrg_ctx* ctx, int on);
 int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset);

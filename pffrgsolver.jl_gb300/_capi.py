@@ -27,13 +27,14 @@ EXPORTED = [
     "pffrg_dsigma", "pffrg_dgamma", "pffrg_sde", "pffrg_bse", "pffrg_action_size", "pffrg_upload",
     "pffrg_download", "pffrg_rhs", "pffrg_bs_step", "pffrg_accept", "pffrg_last_integrand_evals",
     "pffrg_host_alloc", "pffrg_host_free", "pffrg_set_timing", "pffrg_read_stats", "pffrg_chi", "pffrg_chi_slot",
+    "pffrg_set_async_waves",
 ]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("integrand_evals", ctypes.c_int64), ("algorithmic_values", ctypes.c_int64),
                 ("pass_ms", ctypes.c_double), ("rhs_ms", ctypes.c_double), ("pass_launches", ctypes.c_int64),
-                ("launches", ctypes.c_int64)]
+                ("launches", ctypes.c_int64), ("chi_evals", ctypes.c_int64), ("chi_regions_max", ctypes.c_int64)]
 
 
 class LatticeView(ctypes.Structure):
@@ -90,6 +91,7 @@ def load():
     L.pffrg_bs_step.argtypes = [vp, ctypes.c_int, d, d, ctypes.c_int, d, d, d, d, ctypes.c_int, d, d,
                                 ctypes.POINTER(d), ctypes.POINTER(d)]
     L.pffrg_accept.argtypes = [vp]
+    L.pffrg_set_async_waves.argtypes = [vp, ctypes.c_int]
     dp = ctypes.POINTER(ctypes.c_double)
     L.pffrg_chi.argtypes = [vp, d, AV, dp, ctypes.c_int, d, d, dp]
     L.pffrg_chi_slot.argtypes = [vp, d, ctypes.c_int, dp, ctypes.c_int, d, d, dp]

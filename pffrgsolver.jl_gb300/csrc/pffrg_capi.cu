@@ -53,6 +53,8 @@ struct pffrg_ctx {
     double* gk_seg = nullptr;
     long long gk_cap = 0, gk_slots = 0;
     int gk_overflow = 0;
+    int async_waves = 1;  // device-driven quadrature levels (no host round trip per level)
+    int64_t chi_evals = 0, chi_regions_max = 0;
     // wave workspace of the passes (device scratch) and its host-visible counters
     void* wave_mem = nullptr;
     size_t wave_bytes = 0;
@@ -326,6 +328,8 @@ PassArgs<R> base_pass(pffrg_ctx* ctx, double Lam, int eval, double atol, double 
     p.chan_of_y[1] = 0;
     p.chan_of_y[2] = 2;
     p.node_counter = ctx->counter;
+    p.async_waves = ctx->async_waves;
+    p.status = ctx->status;
     return p;
 }
 
@@ -455,6 +459,7 @@ int check_status(pffrg_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->st));
     if (h) {
         CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
+        if (h & 8) return ctx->fail(PFFRG_E_LIMIT, "quadrature chunk queue capacity exceeded");
         ctx->gk_overflow = 1;
         return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity (%lld) exceeded", ctx->gk_cap);
     }
@@ -493,6 +498,12 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     ChiArgs c;
     c.L = ctx->L;
     c.a = a;
+    c.af = nullptr;
+    if (ctx->precision == PFFRG_MIXED) {
+        // mixed path: FP32 integrand on the FP32 copy, cubature sums and errors in FP64
+        if (int rc = to_f(ctx, a, ctx->f_a)) return rc;
+        c.af = ctx->f_a;
+    }
     c.mesh = ctx->mesh;
     c.chi_mesh = ctx->chi_mesh;
     c.num_chi = num_chi;
@@ -505,6 +516,8 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     c.box_out = ctx->chi_box;
     c.chi = ctx->chi_out;
     c.status = ctx->status;
+    c.evals = ctx->counter + 2;  // [2], [3] of the context's counters
+    CK(cudaMemsetAsync(c.evals, 0, 2 * sizeof(unsigned long long), ctx->st));
     const long long cap_max = 10000000 / 34 + 2;
     const size_t budget = (size_t)16 << 30;
     std::vector<int> todo(njobs), over;
@@ -562,7 +575,11 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     }
     CK(cudaMemcpyAsync(chi, ctx->chi_out, sizeof(double) * ncomp * (size_t)Ns * num_chi, cudaMemcpyDeviceToHost,
                        ctx->st));
+    unsigned long long ev[2] = {0, 0};
+    CK(cudaMemcpyAsync(ev, c.evals, sizeof(ev), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    ctx->chi_evals = (int64_t)ev[0];
+    ctx->chi_regions_max = (int64_t)ev[1];
     return 0;
 }
 
@@ -750,6 +767,8 @@ int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset) {
     out->rhs_ms = ctx->rhs_ms;
     out->pass_launches = ctx->pass_launches;
     out->launches = ctx->launches;
+    out->chi_evals = ctx->chi_evals;
+    out->chi_regions_max = ctx->chi_regions_max;
     if (reset) {
         ctx->pass_ms = ctx->rhs_ms = 0.0;
         ctx->pass_launches = ctx->launches = 0;
@@ -861,7 +880,7 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
          dalloc((void**)&ctx->corrs_sde, sizeof(double) * 6 * L.NO) &&
          dalloc((void**)&ctx->partial, sizeof(double) * kPartials) &&
          dalloc((void**)&ctx->scalars, sizeof(double) * 4) && dalloc((void**)&ctx->status, sizeof(int)) &&
-         dalloc((void**)&ctx->counter, 2 * sizeof(unsigned long long));
+         dalloc((void**)&ctx->counter, 4 * sizeof(unsigned long long));
     if (!ok) return bail("device allocation failed");
     if (cudaHostAlloc((void**)&ctx->h_scalars, sizeof(double) * 4, cudaHostAllocDefault) != cudaSuccess ||
         cudaHostAlloc((void**)&ctx->h_wave_counters, sizeof(int) * 8, cudaHostAllocDefault) != cudaSuccess)
@@ -1193,6 +1212,12 @@ int pffrg_chi_slot(pffrg_ctx* ctx, double Lam, int slot, const double* chi_mesh,
     if (slot < 0 || slot >= PFFRG_NUM_SLOTS) return ctx->fail(PFFRG_E_ARGS, "bad slot");
     CK(cudaSetDevice(ctx->device));
     return chi_dev(ctx, Lam, ctx->slot[slot], chi_mesh, num_chi, atol, rtol, chi);
+}
+
+int pffrg_set_async_waves(pffrg_ctx* ctx, int on) {
+    if (!ctx) return PFFRG_E_ARGS;
+    ctx->async_waves = on ? 1 : 0;
+    return 0;
 }
 
 void* pffrg_host_alloc(int64_t bytes) {

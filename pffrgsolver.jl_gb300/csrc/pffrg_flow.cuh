@@ -38,6 +38,7 @@
 // (spin, density), 6 for U(1)-DM (xx, zz, DM, dd, zd, dz).
 #pragma once
 
+#include <algorithm>
 #include <type_traits>
 
 #include "pffrg_internal.h"
@@ -54,15 +55,23 @@ struct NodeScratch {
     Plan<R> plan[4][3];
 };
 
-// nodes per team batch: 8 per warp in total for SU(2), 4 for U(1)-DM
-template <int T, int C>
+// nodes per team batch: 8 per warp in total for SU(2), 4 for U(1)-DM; fewer when each lane holds
+// many sites (the SU(2) t-channel staging grows with sites x nodes)
+template <int T, int C, int SPL>
 struct BatchOf {
-    static constexpr int NB = (C == 2 ? 8 : 4) * T / 32;
+    static constexpr int NB = (C == 2 ? (SPL <= 2 ? 8 : (SPL <= 4 ? 4 : 2)) : 4) * T / 32;
 };
 
-template <typename R, int T, int C>
+// SU(2) t-channel staging: per site the NB (spin, density) pairs of a batch, padded by 16 bytes so
+// that the 16-byte loads of lanes reading different sites spread over the shared-memory banks
+template <typename R, int NB>
+__host__ __device__ constexpr int t_site_stride() {
+    return NB + (sizeof(R) == 4 ? 2 : 1);  // in pairs of R
+}
+
+template <typename R, int T, int C, int SPL>
 struct TeamScratch {
-    NodeScratch<R, C> node[BatchOf<T, C>::NB];
+    NodeScratch<R, C> node[BatchOf<T, C, SPL>::NB];
 };
 
 // ---------------------------------------------------------------------------
@@ -305,7 +314,7 @@ template <typename R, int T, int SPL, int C>
 struct Team {
     const PassArgs<R>& A;
     const SMesh<R>& M;
-    TeamScratch<R, T, C>& ts;
+    TeamScratch<R, T, C, SPL>& ts;
     R* tmp;                 // t channel: [2 C][Ns] slot values of the current node
     const unsigned* rows;   // packed overlap rows (shared or global)
     const int* row_off;     // [Ns+1]
@@ -317,7 +326,7 @@ struct Team {
     // g[j][c][k] = Γ_c(site tl + k T; x_j).  Team-collective: all lanes of the warp call it
     // together (inactive teams with count = 0).
     __device__ void eval(const TaskInfo& ti, R W, R V, R VP, const double* x, int count,
-                         R g[BatchOf<T, C>::NB][C][SPL]) {
+                         R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
         const int X = ti.X;
         const int Ns = A.L.Ns;
         const int nslots = (X == 1) ? 4 : 2;
@@ -444,7 +453,7 @@ struct Team {
     }
 
     // phase B of the SU(2) s and u channels (flow_su2_s.jl, flow_su2_u.jl): per node and site
-    __device__ void eval_su(int X, int count, R g[BatchOf<T, C>::NB][C][SPL]) {
+    __device__ void eval_su(int X, int count, R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
         const R two = (X == 0) ? (R)-2 : (R)2;
         for (int j = 0; j < count; ++j) {
             const NodeScratch<R, C>& ns = ts.node[j];
@@ -463,12 +472,13 @@ struct Team {
     // phase B of the SU(2) t channel for the whole batch (flow_su2_t.jl:46-81), first half:
     // the non-local vertices of every node are gathered, their local part combined, and both
     // slots staged in shared memory as [site][node] pairs (spin, density)
-    __device__ void eval_t_stage(int count, R g[BatchOf<T, C>::NB][C][SPL]) {
-        constexpr int NB = BatchOf<T, C>::NB;
+    __device__ void eval_t_stage(int count, R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
+        constexpr int NB = BatchOf<T, C, SPL>::NB;
         using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
         const int Ns = A.L.Ns;
-        R2* tb1 = reinterpret_cast<R2*>(tmp);  // [Ns][NB]
-        R2* tb2 = tb1 + (size_t)Ns * NB;
+        constexpr int SS = t_site_stride<R, NB>();
+        R2* tb1 = reinterpret_cast<R2*>(tmp);  // [Ns][SS]
+        R2* tb2 = tb1 + (size_t)Ns * SS;
         for (int j = 0; j < count; ++j) {
             const NodeScratch<R, C>& ns = ts.node[j];
             const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
@@ -483,74 +493,70 @@ struct Team {
                 g[j][0][k] = -p * ((R)-1 * v1s * v4s + v1s * v4d - (R)1 * v3s * v2s + v3d * v2s);
                 g[j][1][k] = -p * ((R)3 * v1d * v4s + v1d * v4d + (R)3 * v3s * v2d + v3d * v2d);
                 if (i < Ns) {
-                    tb1[(size_t)i * NB + j] = R2{v1s, v1d};
-                    tb2[(size_t)i * NB + j] = R2{v2s, v2d};
+                    tb1[(size_t)i * SS + j] = R2{v1s, v1d};
+                    tb2[(size_t)i * SS + j] = R2{v2s, v2d};
                 }
             }
         }
     }
 
-    // second half: the overlap sums (flow_su2_t.jl:66-75) of the whole batch.  Each packed row
-    // is read once per batch, the vertex values of two nodes come in one 16-byte load (FP32),
-    // and a node's row sums are scaled by its -p (-2) (2S) at the end.  Nodes past `count` hold
-    // stale values whose sums are never used.
-    __device__ void eval_t_overlap(int count, R g[BatchOf<T, C>::NB][C][SPL]) {
-        constexpr int NB = BatchOf<T, C>::NB;
+    // second half: the overlap sums (flow_su2_t.jl:66-75) of the whole batch.  The team's lanes
+    // are (node j of the batch, row group q of G = T / NB): all lanes walk the sites in the same
+    // order, a lane adds every G-th row of a site for its node (the row word is the same for the NB
+    // lanes of a group, the vertex pairs of neighbouring nodes are neighbours in shared memory),
+    // the G partial sums meet by shuffles, and the owner of a site scales its nodes' sums by
+    // -p (-2) (2S) at the end.  Nodes past `count` hold stale values whose sums are never used.
+    __device__ void eval_t_overlap(int count, R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
+        constexpr int NB = BatchOf<T, C, SPL>::NB;
+        constexpr int G = T / NB;  // row groups per node
         using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
         const int Ns = A.L.Ns;
+        constexpr int SS = t_site_stride<R, NB>();
         const R2* tb1 = reinterpret_cast<const R2*>(tmp);
-        const R2* tb2 = tb1 + (size_t)Ns * NB;
+        const R2* tb2 = tb1 + (size_t)Ns * SS;
+        R2* ov = const_cast<R2*>(tb2) + (size_t)Ns * SS;  // [Ns][NB] overlap sums
+        const int j = tl % NB, q = tl / NB;
+        const unsigned team_mask = (T == 32) ? kFull : (((1u << T) - 1u) << ((threadIdx.x & 31) / T * T));
+        for (int i = 0; i < Ns; ++i) {
+            R Ss = (R)0, Sd = (R)0;
+            const int j1 = row_off[i + 1];
+            for (int r = row_off[i] + q; r < j1; r += G) {
+                const unsigned row = rows[r];
+                const int ia = row & 0xff, ib = (row >> 8) & 0xff;
+                const R m = (R)(row >> 16);
+                const R2 a = tb1[(size_t)ia * SS + j], b = tb2[(size_t)ib * SS + j];
+                Ss += m * a.x * b.x;
+                Sd += m * a.y * b.y;
+            }
+#pragma unroll
+            for (int o = NB; o < T; o <<= 1) {
+                Ss += __shfl_xor_sync(team_mask, Ss, o);
+                Sd += __shfl_xor_sync(team_mask, Sd, o);
+            }
+            if (q == 0) ov[(size_t)i * NB + j] = R2{Ss, Sd};
+        }
+        __syncwarp(team_mask);
         const R twoS = (R)A.twoS;
 #pragma unroll
         for (int k = 0; k < SPL; ++k) {
             const int i = tl + k * T;
-            R Ss[NB], Sd[NB];
+            if (i >= Ns) continue;
 #pragma unroll
-            for (int j = 0; j < NB; ++j) Ss[j] = Sd[j] = (R)0;
-            if (i < Ns) {
-                const int j0 = row_off[i], j1 = row_off[i + 1];
-                for (int r = j0; r < j1; ++r) {
-                    const unsigned row = rows[r];
-                    const int ia = row & 0xff, ib = (row >> 8) & 0xff;
-                    const R m = (R)(row >> 16);
-                    const R2* a2 = tb1 + (size_t)ia * NB;
-                    const R2* b2 = tb2 + (size_t)ib * NB;
-                    if constexpr (sizeof(R) == 4) {
-                        const float4* a4 = reinterpret_cast<const float4*>(a2);
-                        const float4* b4 = reinterpret_cast<const float4*>(b2);
-#pragma unroll
-                        for (int q = 0; q < NB / 2; ++q) {
-                            const float4 a = a4[q], b = b4[q];
-                            Ss[2 * q] += m * a.x * b.x;
-                            Sd[2 * q] += m * a.y * b.y;
-                            Ss[2 * q + 1] += m * a.z * b.z;
-                            Sd[2 * q + 1] += m * a.w * b.w;
-                        }
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < NB; ++q) {
-                            const R2 a = a2[q], b = b2[q];
-                            Ss[q] += m * a.x * b.x;
-                            Sd[q] += m * a.y * b.y;
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < NB; ++j) {
-                if (j >= count) continue;
-                const NodeScratch<R, C>& ns = ts.node[j];
+            for (int jj = 0; jj < NB; ++jj) {
+                if (jj >= count) continue;
+                const NodeScratch<R, C>& ns = ts.node[jj];
                 const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
                 const R coef = -p * (R)-2 * twoS;
-                g[j][0][k] += coef * Ss[j];
-                g[j][1][k] += coef * Sd[j];
+                const R2 s = ov[(size_t)i * NB + jj];
+                g[jj][0][k] += coef * s.x;
+                g[jj][1][k] += coef * s.y;
             }
         }
     }
 
     // phase B of one node for U(1)-DM (flow_u1_dm_{s,t,u}.jl); team-collective like eval
     __device__ void eval_u1dm(int X, int j, bool act, R p, const NodeScratch<R, C>& ns, const R v1[C][SPL],
-                              const R v2[C][SPL], R g[BatchOf<T, C>::NB][C][SPL]) {
+                              const R v2[C][SPL], R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
         const int Ns = A.L.Ns;
         if (act && X != 1) {
 #pragma unroll
@@ -669,18 +675,19 @@ __device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const SMesh<R>&
 }
 
 // shared-memory layout common to the wave kernels
-template <typename R, int T, int C>
+template <typename R, int T, int C, int SPL>
 struct SmemLayout {
     static constexpr int NPW = 32 / T;
     // t-channel staging per team: SU(2) both slots of the whole batch, U(1)-DM one node
     __host__ __device__ static size_t tmp_per_team(int Ns) {
-        return C == 2 ? (size_t)4 * Ns * BatchOf<T, C>::NB : (size_t)2 * C * Ns;
+        return C == 2 ? (size_t)4 * Ns * t_site_stride<R, BatchOf<T, C, SPL>::NB>() + (size_t)2 * Ns * BatchOf<T, C, SPL>::NB
+                      : (size_t)2 * C * Ns;
     }
     size_t mesh, teams, tmp, rows, total;
     __host__ __device__ SmemLayout(int Ns, long long R_rows, bool rows_in_smem) {
         mesh = 0;
         teams = mesh + sizeof(SMesh<R>);
-        tmp = (teams + sizeof(TeamScratch<R, T, C>) * kWarps * NPW + 15) & ~(size_t)15;  // 16-byte loads
+        tmp = (teams + sizeof(TeamScratch<R, T, C, SPL>) * kWarps * NPW + 15) & ~(size_t)15;  // 16-byte loads
         rows = tmp + ((sizeof(R) * (size_t)kWarps * NPW * tmp_per_team(Ns) + 15) & ~(size_t)15);
         total = rows + (rows_in_smem ? sizeof(unsigned) * (size_t)(R_rows + Ns + 1) : 0);
     }
@@ -691,8 +698,8 @@ __device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, un
                                                         const SMesh<R>& M, int warp, int team, int tl) {
     constexpr int NPW = 32 / T;
     const int Ns = A.L.Ns;
-    SmemLayout<R, T, C> lay(Ns, A.rows_total, A.rows_in_smem);
-    TeamScratch<R, T, C>* teams = reinterpret_cast<TeamScratch<R, T, C>*>(smem + lay.teams);
+    SmemLayout<R, T, C, SPL> lay(Ns, A.rows_total, A.rows_in_smem);
+    TeamScratch<R, T, C, SPL>* teams = reinterpret_cast<TeamScratch<R, T, C, SPL>*>(smem + lay.teams);
     R* tmp = reinterpret_cast<R*>(smem + lay.tmp) + (size_t)(warp * NPW + team) * lay.tmp_per_team(Ns);
     const unsigned* rows;
     const int* roff;
@@ -712,12 +719,12 @@ __device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, un
     return t;
 }
 
-template <typename R, int T, int C>
+template <typename R, int T, int C, int SPL>
 __device__ __forceinline__ void load_common(const PassArgs<R>& A, unsigned char* smem) {
     SMesh<R>& M = *reinterpret_cast<SMesh<R>*>(smem);
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     if (A.rows_in_smem) {
-        SmemLayout<R, T, C> lay(A.L.Ns, A.rows_total, true);
+        SmemLayout<R, T, C, SPL> lay(A.L.Ns, A.rows_total, true);
         unsigned* rows = reinterpret_cast<unsigned*>(smem + lay.rows);
         for (long long k = threadIdx.x; k < A.rows_total; k += blockDim.x) rows[k] = ldg(A.ov_rows + k);
         int* roff = reinterpret_cast<int*>(rows + A.rows_total);
@@ -788,7 +795,7 @@ template <typename R, int T, int SPL, int C>
 __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveSpace Wsp) {
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
-    load_common<R, T, C>(A, smem);
+    load_common<R, T, C, SPL>(A, smem);
     const SMesh<R>& M = *reinterpret_cast<const SMesh<R>*>(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
@@ -796,7 +803,7 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
     const int Ns = A.L.Ns;
     const int jobs = 4 * A.eval + 1;
     const long long nwarps = (long long)gridDim.x * kWarps;
-    constexpr int NB = BatchOf<T, C>::NB;
+    constexpr int NB = BatchOf<T, C, SPL>::NB;
     for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < Wsp.nsub; base += nwarps * NPW) {
         const int sub = (int)(base + team);
         const bool valid = sub < Wsp.nsub;
@@ -910,7 +917,14 @@ template <typename R, int T, int SPL, int C>
 __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
-    load_common<R, T, C>(A, smem);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // the next level's queue starts empty (its chunks are enqueued by this wave's decide_kernel)
+        Wsp.counters[par ^ 1] = 0;
+        Wsp.counters[2 + (par ^ 1)] = 0;
+    }
+    // blocks without a chunk leave before staging the meshes and rows
+    if ((long long)blockIdx.x * kWarps * NPW >= Wsp.counters[par]) return;
+    load_common<R, T, C, SPL>(A, smem);
     const SMesh<R>& M = *reinterpret_cast<const SMesh<R>*>(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
@@ -919,7 +933,7 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
     const int jobs = 4 * A.eval + 1;
     const int nchunks = Wsp.counters[par];
     const long long nwarps = (long long)gridDim.x * kWarps;
-    constexpr int NB = BatchOf<T, C>::NB;
+    constexpr int NB = BatchOf<T, C, SPL>::NB;
     R g[NB][C][SPL];
     for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < nchunks; base += nwarps * NPW) {
         const int chunk = (int)(base + team);
@@ -1055,15 +1069,21 @@ __global__ void reduce_kernel(PassArgs<R> A, WaveSpace Wsp) {
     }
 }
 
+// a pass whose chunk queue overflowed reports it in the call's status word (bit 3)
+static __global__ void wave_status_kernel(const int* counters, int* status) {
+    if (threadIdx.x == 0 && counters[4]) atomicOr(status, 8);
+}
+
 // team width T = lanes per node batch, SPL = sites per lane
 template <typename R, int C>
 struct PassLauncher {
     template <int T, int SPL>
     static cudaError_t run(const PassArgs<R>& a0, WaveSpace& Wsp, int* h_counters, cudaStream_t st, int grid_cap) {
-        // overlap rows in shared memory when they fit next to the rest
+        // overlap rows in shared memory only while three blocks still fit on an SM (a row word is
+        // read once per batch of nodes, so from L1 it costs little)
         PassArgs<R> a = a0;
-        a.rows_in_smem = SmemLayout<R, T, C>(a.L.Ns, a.rows_total, true).total <= (size_t)160 * 1024;
-        SmemLayout<R, T, C> lay(a.L.Ns, a.rows_total, a.rows_in_smem);
+        a.rows_in_smem = SmemLayout<R, T, C, SPL>(a.L.Ns, a.rows_total, true).total <= (size_t)75 * 1024;
+        SmemLayout<R, T, C, SPL> lay(a.L.Ns, a.rows_total, a.rows_in_smem);
         const size_t smem = lay.total;
         if (smem > (size_t)227 * 1024) return cudaErrorInvalidConfiguration;
         cudaError_t e;
@@ -1077,6 +1097,24 @@ struct PassLauncher {
         int g0 = (Wsp.nsub + teams_per_block - 1) / teams_per_block;
         wave0_kernel<R, T, SPL, C><<<g0 < grid_cap ? g0 : grid_cap, kWarps * 32, smem, st>>>(a, Wsp);
         if ((e = cudaGetLastError())) return e;
+        if (a.async_waves) {
+            // device-driven levels: every wave reads its chunk and subdomain counts from the device,
+            // idle blocks leave at once, and no host round trip separates the waves (the deepest
+            // level the reference allows, n > 2^20 new nodes, is reached by wave 20)
+            const int gd = std::max(1, std::min(grid_cap, (Wsp.nsub + teams_per_block - 1) / teams_per_block));
+            int par = 1;
+            for (int wave = 1; wave <= 21; ++wave) {
+                eval_kernel<R, T, SPL, C><<<grid_cap, kWarps * 32, smem, st>>>(a, Wsp, par);
+                if ((e = cudaGetLastError())) return e;
+                decide_kernel<T, SPL, C><<<gd, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol, par);
+                if ((e = cudaGetLastError())) return e;
+                par ^= 1;
+            }
+            wave_status_kernel<<<1, 32, 0, st>>>(Wsp.counters, a.status);
+            if ((e = cudaGetLastError())) return e;
+            reduce_kernel<R, C><<<a.ntasks * a.nchan, 128, 0, st>>>(a, Wsp);
+            return cudaGetLastError();
+        }
         int par = 1;
         for (int wave = 1; wave <= 21; ++wave) {
             if ((e = cudaMemcpyAsync(h_counters, Wsp.counters, sizeof(int) * 5, cudaMemcpyDeviceToHost, st))) return e;

@@ -47,6 +47,8 @@ struct PassArgs {
     int eval;
     double twoS;
     int reduced;          // reduced s bubble of the SDE (U(1)-DM keeps xx, zz, dd only)
+    int async_waves;      // levels without host round trips; overflow reported in *status (bit 3)
+    int* status;
     unsigned long long* node_counter;  // optional: [0] integrand evaluations, [1] algorithmic values read
 };
 
@@ -157,6 +159,7 @@ cudaError_t launch_corrs(const CorrsArgs<R>& a, cudaStream_t st);
 struct ChiArgs {
     Layout L;
     const double* a;         // the state (FP64)
+    const float* af;         // its FP32 copy: integrand in FP32 (mixed path), or null
     const double* mesh;
     const double* chi_mesh;  // [num_chi]
     int num_chi;
@@ -168,6 +171,7 @@ struct ChiArgs {
     long long cap;           // regions per integral
     double* box_out;         // [ncomp][num_chi][Ns][9]
     double* chi;             // [ncomp][Ns][num_chi], each column-major
+    unsigned long long* evals;  // [0] cubature points evaluated, [1] largest region count
     double* seg;             // Gauss-Kronrod segments of the local term: [num_chi][4][seg_cap]
     long long seg_cap;
     int* status;             // bit 1: GK segments exhausted

@@ -488,53 +488,58 @@ __device__ __forceinline__ void gm_rule(const double* v, double vol, double& val
 
 // compute_χ_kernel! (correlation_su2.jl:14-55) and compute_χ_kernel_{xx,zz,xy}!
 // (correlation_u1_dm.jl:14-149, component k = 0, 1, 2) at (x, y) of [0,1]^2
+// The integrand arithmetic runs in R (FP64, or FP32 on the FP32 copy of the state for
+// the mixed path); the compactified coordinates and their Jacobians are formed in FP64.
+template <typename R>
 struct ChiKernel {
     const ChiArgs& A;
-    const SMesh<double>& M;
+    const SMesh<R>& M;
+    const R* a;  // the state in R
     int site;
     int k;
     double w;
     __device__ double operator()(double x, double y) const {
         const Layout& L = A.L;
-        const double v = (2.0 * x - 1.0) / ((1.0 - x) * x);
-        const double vp = (2.0 * y - 1.0) / ((1.0 - y) * y);
-        const double dv = (2.0 * x * x - 2.0 * x + 1) / ((1.0 - x) * (1.0 - x) * x * x);
-        const double dvp = (2.0 * y * y - 2.0 * y + 1) / ((1.0 - y) * (1.0 - y) * y * y);
-        Plan<double> p1[3];
-        make_plan<double>(p1[0], 0, v + vp, 0.5 * (v - w - vp), 0.5 * (-v - w + vp), M, L.Ns, L.NO, L.Nn);
-        make_plan<double>(p1[1], 1, w, v, vp, M, L.Ns, L.NO, L.Nn);
-        make_plan<double>(p1[2], 2, v - vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp), M, L.Ns, L.NO, L.Nn);
-        const double twoS = A.twoS;
-        const double tp2 = two_pi<double>() * two_pi<double>();
+        const R v = (R)((2.0 * x - 1.0) / ((1.0 - x) * x));
+        const R vp = (R)((2.0 * y - 1.0) / ((1.0 - y) * y));
+        const R dv = (R)((2.0 * x * x - 2.0 * x + 1) / ((1.0 - x) * (1.0 - x) * x * x));
+        const R dvp = (R)((2.0 * y * y - 2.0 * y + 1) / ((1.0 - y) * (1.0 - y) * y * y));
+        const R wr = (R)w, h = (R)0.5;
+        Plan<R> p1[3];
+        make_plan<R>(p1[0], 0, v + vp, h * (v - wr - vp), h * (-v - wr + vp), M, L.Ns, L.NO, L.Nn);
+        make_plan<R>(p1[1], 1, wr, v, vp, M, L.Ns, L.NO, L.Nn);
+        make_plan<R>(p1[2], 2, v - vp, h * (v - wr + vp), h * (v + wr + vp), M, L.Ns, L.NO, L.Nn);
+        const R twoS = (R)A.twoS;
+        const R tp2 = two_pi<R>() * two_pi<R>();
         const int ei = ldg(A.exch + site);
-        double val;
-        if (L.C == 2) val = -(twoS * twoS) * site_value<double>(L, A.a, p1, CH_ALL, 0, site, ei) / tp2;
-        else val = -site_value<double>(L, A.a, p1, CH_ALL, k, site, ei) / tp2;  // Γxx, Γzz, ΓDM
+        R val;
+        if (L.C == 2) val = -(twoS * twoS) * site_value<R>(L, a, p1, CH_ALL, 0, site, ei) / tp2;
+        else val = -site_value<R>(L, a, p1, CH_ALL, k, site, ei) / tp2;  // Γxx, Γzz, ΓDM
         if (site == 0) {
-            Plan<double> p2[3];
-            make_plan<double>(p2[0], 0, v + vp, 0.5 * (v - w - vp), 0.5 * (v + w - vp), M, L.Ns, L.NO, L.Nn);
-            make_plan<double>(p2[1], 1, -v + vp, 0.5 * (v - w + vp), 0.5 * (v + w + vp), M, L.Ns, L.NO, L.Nn);
-            make_plan<double>(p2[2], 2, -w, v, vp, M, L.Ns, L.NO, L.Nn);
-            auto g = [&](int c) { return site_value<double>(L, A.a, p2, CH_ALL, c, 0, ei); };
+            Plan<R> p2[3];
+            make_plan<R>(p2[0], 0, v + vp, h * (v - wr - vp), h * (v + wr - vp), M, L.Ns, L.NO, L.Nn);
+            make_plan<R>(p2[1], 1, -v + vp, h * (v - wr + vp), h * (v + wr + vp), M, L.Ns, L.NO, L.Nn);
+            make_plan<R>(p2[2], 2, -wr, v, vp, M, L.Ns, L.NO, L.Nn);
+            auto g = [&](int c) { return site_value<R>(L, a, p2, CH_ALL, c, 0, ei); };
             if (L.C == 2) {
-                const double vs = g(0);
-                const double vd = g(1);
-                val -= twoS * (vs - vd) / (2.0 * tp2);
+                const R vs = g(0);
+                const R vd = g(1);
+                val -= twoS * (vs - vd) / ((R)2 * tp2);
             } else if (k == 0) {
-                const double vzz = g(1), vdd = g(3);
-                val -= (vzz - vdd) / (2.0 * tp2);
+                const R vzz = g(1), vdd = g(3);
+                val -= (vzz - vdd) / ((R)2 * tp2);
             } else if (k == 1) {
-                const double vxx = g(0), vzz = g(1), vdd = g(3);
-                val -= (2.0 * vxx - vzz - vdd) / (2.0 * tp2);
+                const R vxx = g(0), vzz = g(1), vdd = g(3);
+                val -= ((R)2 * vxx - vzz - vdd) / ((R)2 * tp2);
             } else {
-                const double vzd = g(4), vdz = g(5);
-                val -= (vzd - vdz) / (2.0 * tp2);
+                const R vzd = g(4), vdz = g(5);
+                val -= (vzd - vdz) / ((R)2 * tp2);
             }
         }
-        const double Lam = A.Lam;
-        val *= G_full(M, L.Nsig, A.a, Lam, v - 0.5 * w) * G_full(M, L.Nsig, A.a, Lam, v + 0.5 * w) * dv;
-        val *= G_full(M, L.Nsig, A.a, Lam, vp - 0.5 * w) * G_full(M, L.Nsig, A.a, Lam, vp + 0.5 * w) * dvp;
-        return val;
+        const R Lam = (R)A.Lam;
+        val *= G_full(M, L.Nsig, a, Lam, v - h * wr) * G_full(M, L.Nsig, a, Lam, v + h * wr) * dv;
+        val *= G_full(M, L.Nsig, a, Lam, vp - h * wr) * G_full(M, L.Nsig, a, Lam, vp + h * wr) * dvp;
+        return (double)val;
     }
 };
 
@@ -570,11 +575,12 @@ constexpr int kChiPend = 64;  // regions evaluated per batch
 // One warp per (ω, site, component, box) integral of the job list; a job that
 // runs out of region capacity raises its overflow flag and is run again with a
 // larger capacity.
+template <typename RT>
 __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, const int* __restrict__ jobs, int njobs,
                                                                   int* overflow) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SMesh<double>& M = *reinterpret_cast<SMesh<double>*>(smem_raw);
-    double* fb = reinterpret_cast<double*>(smem_raw + sizeof(SMesh<double>));
+    SMesh<RT>& M = *reinterpret_cast<SMesh<RT>*>(smem_raw);
+    double* fb = reinterpret_cast<double*>(smem_raw + sizeof(SMesh<RT>));
     int* pend = reinterpret_cast<int*>(fb + kChiWarps * kChiPend * 17);
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     __syncthreads();
@@ -609,7 +615,10 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, cons
     R.hkey = R.err + cap;
     R.split = A.reg_split + off * 2;
     R.hidx = R.split + cap;
-    ChiKernel f{A, M, site, k, wv};
+    const RT* state;
+    if constexpr (sizeof(RT) == 8) state = A.a;
+    else state = A.af;
+    ChiKernel<RT> f{A, M, state, site, k, wv};
     if (lane == 0) {
         R.c0[0] = 0.5 * (lo[col] + hi[col]);
         R.c1[0] = 0.5 * (lo[row] + hi[row]);
@@ -705,6 +714,10 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, cons
         for (int q = 0; q < hn; ++q) I += R.val[R.hidx[q]];
         A.box_out[job] = I;
         overflow[slot] = over ? 1 : 0;
+        if (A.evals && !over) {
+            atomicAdd(A.evals, (unsigned long long)numeval);
+            atomicMax(A.evals + 1, (unsigned long long)n);
+        }
     }
 }
 
@@ -750,13 +763,19 @@ __global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
     }
 }
 
-cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st) {
-    const size_t smem = sizeof(SMesh<double>) + sizeof(double) * kChiWarps * kChiPend * 17 + sizeof(int) * kChiWarps * kChiPend;
-    cudaError_t e = cudaFuncSetAttribute(chi_box_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <typename R>
+static cudaError_t launch_chi_boxes_r(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st) {
+    const size_t smem = sizeof(SMesh<R>) + sizeof(double) * kChiWarps * kChiPend * 17 + sizeof(int) * kChiWarps * kChiPend;
+    cudaError_t e = cudaFuncSetAttribute(chi_box_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    chi_box_kernel<<<(unsigned)((njobs + kChiWarps - 1) / kChiWarps), kChiWarps * 32, smem, st>>>(a, jobs, njobs,
-                                                                                                   overflow);
+    chi_box_kernel<R><<<(unsigned)((njobs + kChiWarps - 1) / kChiWarps), kChiWarps * 32, smem, st>>>(a, jobs, njobs,
+                                                                                                      overflow);
     return cudaGetLastError();
+}
+
+cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st) {
+    return a.af ? launch_chi_boxes_r<float>(a, jobs, njobs, overflow, st)
+                : launch_chi_boxes_r<double>(a, jobs, njobs, overflow, st);
 }
 
 cudaError_t launch_chi_sum(const ChiArgs& a, cudaStream_t st) {

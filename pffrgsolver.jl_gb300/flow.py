@@ -130,6 +130,10 @@ class FlowContext:
         mats = [out[k * n:(k + 1) * n].reshape((self.num_sites, len(mesh)), order="F") for k in range(ncomp)]
         return mats[0] if ncomp == 1 else mats
 
+    def set_async_waves(self, on: bool) -> None:
+        """Device-driven quadrature levels (default) or the host-driven loop; same results."""
+        self._check(self.lib.pffrg_set_async_waves(self.h, int(bool(on))), "set_async_waves")
+
     # ---- device-resident interface ----
     def upload(self, slot: int, a: Action) -> None:
         v = _capi.action_view(a)

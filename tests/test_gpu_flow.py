@@ -151,3 +151,18 @@ def test_launch_writes_and_resumes_files(pkg, tmp_path):
     assert res2.finished and res2.Lam[-1] <= 3.0 + 1e-12 and res2.Lam[0] < seen[-1]
     res3 = launch(g, "square", 3, "heisenberg", "su2", [[1.0]], final=3.0, overwrite=False, **kw)
     assert res3.reason == "calculation has finished already"
+
+
+def test_sweep_matches_single_runs(pkg):
+    """Concurrent instances (own context and stream each) give exactly the single-run results."""
+    from pffrg_gb300.launcher import launch
+    from pffrg_gb300.sweep import launch_sweep, square_j1j2_sweep
+
+    inst = square_j1j2_sweep(3, sizes=(3, 4))
+    kw = dict(num_sigma=10, num_omega=4, num_nu=3, num_chi=4, initial=5.0, final=4.0, parquet=False,
+              precision="mixed")
+    res = launch_sweep(inst, workers=3, **kw)
+    for i, r in zip(inst, res):
+        single = launch("", i.name, i.size, i.model, i.symmetry, i.J, **kw)
+        assert r.Lam == single.Lam
+        assert np.array_equal(r.action.buf, single.action.buf)
