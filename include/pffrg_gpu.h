@@ -145,6 +145,20 @@ int pffrg_bs_step(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, 
 /* accept the step: slot A <- slot NEXT (the reference keeps a_inter for the resampling) */
 int pffrg_accept(pffrg_ctx* ctx);
 
+/* Mesh scanning and resampling between accepted steps (resample_from_to,
+ * src/Action/Action.jl:483-557) without a host copy of the action.
+ * pffrg_scan_cuts returns what the scans of Action.jl:361-480 read: Σ of the
+ * slot (sigma[num_sigma]), for every component c and channel ch (index
+ * 3 c + ch) the 0-based column-major index of max |q3| (argmax[3 C]; first of
+ * equal maxima) and the cuts through it (cuts[3 C][num_omega + 3 num_nu]:
+ * q3[s,:,v,v'], q3[s,w,k,k] - q3[s,w,end,end], q3[s,w,:,v'] - q3[s,w,end,v'],
+ * q3[s,w,v,:] - q3[s,w,v,end]).  pffrg_resample interpolates the action in
+ * src_slot (on the context's meshes) onto `mesh` into dst_slot (get_Σ for Σ,
+ * the multilinear read-out of channel.jl:416-471 for every q, bare copied) and
+ * makes `mesh` the context's meshes. */
+int pffrg_scan_cuts(pffrg_ctx* ctx, int slot, double* sigma, int64_t* argmax, double* cuts);
+int pffrg_resample(pffrg_ctx* ctx, int src_slot, int dst_slot, const pffrg_mesh_view* mesh);
+
 /* Quadrature levels driven by the device (default 1): the passes read their work
  * counts on the device and need no host round trip per level, so a whole
  * right-hand side is one asynchronous launch sequence; 0 selects the

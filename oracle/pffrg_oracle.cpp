@@ -1357,12 +1357,14 @@ inline void gm_eval(Region2& R, const double* v) {
     R.split = diff[1] > diff[0] ? 1 : 0;
 }
 
-// max-heap of region indices keyed by their error estimate (the cubature
-// library's region heap): push sifts up while the parent's key is smaller;
-// pop moves the last entry to the root and sifts it down along the larger
-// child (the right one only when strictly larger).  The GPU kernel uses the
-// same two rules, so both pop regions in the same order.
+// max-heap of region indices keyed by their error estimate, 32 children per
+// node (children of h at 32 h + 1 .. 32 h + 32).  push sifts up while the
+// parent's key is smaller; pop moves the last entry to the root and sifts it
+// down to the largest child (the first of equal largest keys) while that child
+// is larger.  The GPU kernel uses the same rules (its pops compare the 32
+// children of a node across a warp), so both pop regions in the same order.
 struct RegionHeap {
+    static constexpr int D = 32;
     std::vector<double> key;
     std::vector<int> idx;
     void push(double k, int i) {
@@ -1370,7 +1372,7 @@ struct RegionHeap {
         key.push_back(k);
         idx.push_back(i);
         while (h > 0) {
-            const int p = (h - 1) / 2;
+            const int p = (h - 1) / D;
             if (key[p] >= k) break;
             key[h] = key[p];
             idx[h] = idx[p];
@@ -1389,9 +1391,11 @@ struct RegionHeap {
         if (n > 0) {
             int h = 0;
             for (;;) {
-                const int l = 2 * h + 1, r = l + 1;
-                if (l >= n) break;
-                const int c = (r < n && key[r] > key[l]) ? r : l;
+                const int c0 = D * h + 1;
+                if (c0 >= n) break;
+                int c = c0;
+                for (int q = c0 + 1; q < std::min(c0 + D, n); ++q)
+                    if (key[q] > key[c]) c = q;
                 if (key[c] <= k) break;
                 key[h] = key[c];
                 idx[h] = idx[c];

@@ -28,6 +28,9 @@ struct pffrg_ctx {
     int precision = PFFRG_FP64;
     DevLattice lat;
     double* mesh = nullptr;  // [σ|Ωs|νs|Ωt|νt]
+    double* mesh_new = nullptr;  // the next step's meshes during a resampling
+    long long* scan_arg = nullptr;  // [3 C] argmax of |q3| per component and channel
+    double* scan_cuts = nullptr;    // [3 C][NO + 3 Nn] cuts through the maxima
     double* slot[PFFRG_NUM_SLOTS] = {};
     double* da_l = nullptr;
     double* da_c = nullptr;
@@ -784,7 +787,8 @@ void pffrg_destroy(pffrg_ctx* ctx) {
                     ctx->mesh, ctx->log_bounds, ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig, ctx->sig_tmp, ctx->f_a, ctx->f_da,
                     ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
                     ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red, ctx->chi_reg, ctx->chi_split,
-                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over, ctx->gk_seg};
+                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over, ctx->gk_seg,
+                    ctx->mesh_new, ctx->scan_arg, ctx->scan_cuts};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
@@ -866,7 +870,10 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
     bool ok = dalloc((void**)&ctx->lat.exch, sizeof(int) * Ns) && dalloc((void**)&ctx->lat.mult, sizeof(int) * Ns) &&
               dalloc((void**)&ctx->lat.ov_off, sizeof(int) * (Ns + 1)) &&
               dalloc((void**)&ctx->lat.ov_rows, sizeof(unsigned) * rows.size()) &&
-              dalloc((void**)&ctx->mesh, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn));
+              dalloc((void**)&ctx->mesh, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
+              dalloc((void**)&ctx->mesh_new, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
+              dalloc((void**)&ctx->scan_arg, sizeof(long long) * 3 * L.C) &&
+              dalloc((void**)&ctx->scan_cuts, sizeof(double) * 3 * L.C * (L.NO + 3 * L.Nn));
     for (int k = 0; k < PFFRG_NUM_SLOTS && ok; ++k) ok = dalloc((void**)&ctx->slot[k], sizeof(double) * L.total);
     ok = ok && dalloc((void**)&ctx->da_l, sizeof(double) * L.total) &&
          dalloc((void**)&ctx->da_c, sizeof(double) * L.total) &&
@@ -1212,6 +1219,44 @@ int pffrg_chi_slot(pffrg_ctx* ctx, double Lam, int slot, const double* chi_mesh,
     if (slot < 0 || slot >= PFFRG_NUM_SLOTS) return ctx->fail(PFFRG_E_ARGS, "bad slot");
     CK(cudaSetDevice(ctx->device));
     return chi_dev(ctx, Lam, ctx->slot[slot], chi_mesh, num_chi, atol, rtol, chi);
+}
+
+int pffrg_scan_cuts(pffrg_ctx* ctx, int slot, double* sigma, int64_t* argmax, double* cuts) {
+    if (!ctx || !sigma || !argmax || !cuts) return ctx ? ctx->fail(PFFRG_E_ARGS, "null output") : PFFRG_E_ARGS;
+    if (slot < 0 || slot >= PFFRG_NUM_SLOTS) return ctx->fail(PFFRG_E_ARGS, "bad slot");
+    CK(cudaSetDevice(ctx->device));
+    const Layout& L = ctx->L;
+    ++ctx->launches;
+    CK(launch_scan_cuts(L, ctx->slot[slot], ctx->scan_arg, ctx->scan_cuts, ctx->st));
+    CK(cudaMemcpyAsync(sigma, ctx->slot[slot], sizeof(double) * L.Nsig, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(argmax, ctx->scan_arg, sizeof(long long) * 3 * L.C, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(cuts, ctx->scan_cuts, sizeof(double) * 3 * L.C * (L.NO + 3 * L.Nn), cudaMemcpyDeviceToHost,
+                       ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pffrg_resample(pffrg_ctx* ctx, int src_slot, int dst_slot, const pffrg_mesh_view* mesh) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (src_slot < 0 || src_slot >= PFFRG_NUM_SLOTS || dst_slot < 0 || dst_slot >= PFFRG_NUM_SLOTS ||
+        src_slot == dst_slot)
+        return ctx->fail(PFFRG_E_ARGS, "bad slots");
+    if (int rc = check_mesh(ctx, mesh)) return rc;
+    const Layout& L = ctx->L;
+    if (mesh->num_sigma != L.Nsig || mesh->num_omega != L.NO || mesh->num_nu != L.Nn)
+        return ctx->fail(PFFRG_E_ARGS, "mesh sizes differ from the context's");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<double> h;
+    h.insert(h.end(), mesh->sigma, mesh->sigma + mesh->num_sigma);
+    h.insert(h.end(), mesh->omega_s, mesh->omega_s + mesh->num_omega);
+    h.insert(h.end(), mesh->nu_s, mesh->nu_s + mesh->num_nu);
+    h.insert(h.end(), mesh->omega_t, mesh->omega_t + mesh->num_omega);
+    h.insert(h.end(), mesh->nu_t, mesh->nu_t + mesh->num_nu);
+    CK(cudaMemcpyAsync(ctx->mesh_new, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->st));
+    ++ctx->launches;
+    CK(launch_resample(L, ctx->mesh, ctx->mesh_new, ctx->slot[src_slot], ctx->slot[dst_slot], ctx->st));
+    // the new meshes become the context's
+    return upload_mesh(ctx, mesh);
 }
 
 int pffrg_set_async_waves(pffrg_ctx* ctx, int on) {

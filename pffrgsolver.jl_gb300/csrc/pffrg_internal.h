@@ -155,6 +155,11 @@ struct CorrsArgs {
 template <typename R>
 cudaError_t launch_corrs(const CorrsArgs<R>& a, cudaStream_t st);
 
+// mesh scanning and resampling between flow steps
+cudaError_t launch_scan_cuts(const Layout& L, const double* a, long long* argmax, double* cuts, cudaStream_t st);
+cudaError_t launch_resample(const Layout& L, const double* mesh_old, const double* mesh_new, const double* a,
+                            double* b, cudaStream_t st);
+
 // correlations χ (FP64)
 struct ChiArgs {
     Layout L;

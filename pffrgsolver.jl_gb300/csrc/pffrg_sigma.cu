@@ -393,11 +393,14 @@ struct ChiRegions {
     int* hidx;
 };
 
-// region heap of one integral (lane 0 only): the same sift rules as the oracle's
+// region heap of one integral: 32 children per node, the oracle's sift rules.  push runs on
+// lane 0; pop is warp-collective, one lane per child of the node being sifted.
+constexpr int kHeapD = 32;
+
 __device__ __forceinline__ void heap_push(ChiRegions& R, int& hn, double k, int i) {
     int h = hn++;
     while (h > 0) {
-        const int p = (h - 1) / 2;
+        const int p = (h - 1) / kHeapD;
         if (R.hkey[p] >= k) break;
         R.hkey[h] = R.hkey[p];
         R.hidx[h] = R.hidx[p];
@@ -407,25 +410,44 @@ __device__ __forceinline__ void heap_push(ChiRegions& R, int& hn, double k, int 
     R.hidx[h] = i;
 }
 
-__device__ __forceinline__ int heap_pop(ChiRegions& R, int& hn) {
+__device__ __forceinline__ int heap_pop_warp(ChiRegions& R, int& hn) {
+    const int lane = threadIdx.x & 31;
     const int top = R.hidx[0];
     const int n = --hn;
     const double k = R.hkey[n];
     const int i = R.hidx[n];
+    __syncwarp();
+    int h = 0;
     if (n > 0) {
-        int h = 0;
         for (;;) {
-            const int l = 2 * h + 1, r = l + 1;
-            if (l >= n) break;
-            const int c = (r < n && R.hkey[r] > R.hkey[l]) ? r : l;
-            if (R.hkey[c] <= k) break;
-            R.hkey[h] = R.hkey[c];
-            R.hidx[h] = R.hidx[c];
-            h = c;
+            const int c0 = kHeapD * h + 1;
+            if (c0 >= n) break;
+            const int c = c0 + lane;
+            double best = (c < n) ? R.hkey[c] : -1.0;
+            int bc = (c < n) ? c : 0x7fffffff;
+            // the largest child, the first of equal largest keys
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oc = __shfl_xor_sync(0xffffffffu, bc, o);
+                if (ob > best || (ob == best && oc < bc)) {
+                    best = ob;
+                    bc = oc;
+                }
+            }
+            if (best <= k) break;
+            if (lane == 0) {
+                R.hkey[h] = best;
+                R.hidx[h] = R.hidx[bc];
+            }
+            __syncwarp();
+            h = bc;
         }
-        R.hkey[h] = k;
-        R.hidx[h] = i;
+        if (lane == 0) {
+            R.hkey[h] = k;
+            R.hidx[h] = i;
+        }
     }
+    __syncwarp();
     return top;
 }
 
@@ -632,6 +654,8 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, cons
     chi_eval_regions(f, R, pidx, 1, fbuf);
     int n = 1, hn = 0;
     if (lane == 0) heap_push(R, hn, R.err[0], 0);
+    hn = __shfl_sync(0xffffffffu, hn, 0);  // the heap size is kept uniform across the warp
+    __syncwarp();
     double tot_val = R.val[0], tot_err = R.err[0];
     long long numeval = 17;
     const long long maxevals = 10000000;
@@ -649,10 +673,7 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, cons
                 over = true;
                 break;
             }
-            int bi = 0;
-            if (lane == 0) bi = heap_pop(R, hn);
-            bi = __shfl_sync(0xffffffffu, bi, 0);
-            hn = __shfl_sync(0xffffffffu, hn, 0);
+            const int bi = heap_pop_warp(R, hn);
             const double pv = R.val[bi], pe = R.err[bi];
             tot_val -= pv;
             tot_err -= pe;

@@ -159,6 +159,171 @@ __global__ void max_reduce_kernel(const double* partial, int n, double* out) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// mesh scanning and resampling between flow steps (Action.jl:361-557, channel.jl:416-471)
+// ---------------------------------------------------------------------------
+// argmax |q3| of every (component, channel), the first of equal maxima in column-major order
+// (Julia's argmax), and the four cuts through it that scan_channel reads (Action.jl:452-480):
+// q3[s, :, v, v'], q3[s, w, k, k] - q3[s, w, end, end], q3[s, w, :, v'] - q3[s, w, end, v'],
+// q3[s, w, v, :] - q3[s, w, v, end].  One block per (component, channel).
+__global__ void scan_cuts_kernel(Layout L, const double* __restrict__ a, long long* argmax, double* cuts) {
+    const int cc = blockIdx.x;  // component * 3 + channel
+    const int c = cc / 3, ch = cc % 3;
+    const double* q3 = a + L.qbase(c, ch, 3);
+    double best = -1.0;
+    long long bi = 0;
+    for (long long e = threadIdx.x; e < L.K3; e += blockDim.x) {
+        const double m = fabs(q3[e]);
+        if (m > best) {  // the first maximum of this thread's stride
+            best = m;
+            bi = e;
+        }
+    }
+    __shared__ double sb[32];
+    __shared__ long long si[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const long long oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sb[threadIdx.x >> 5] = best;
+        si[threadIdx.x >> 5] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int nw = blockDim.x / 32;
+        best = threadIdx.x < nw ? sb[threadIdx.x] : -1.0;
+        bi = threadIdx.x < nw ? si[threadIdx.x] : 0x7fffffffffffffffll;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const long long oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        if (threadIdx.x == 0) si[0] = bi;
+    }
+    __syncthreads();
+    bi = si[0];
+    const int Ns = L.Ns, NO = L.NO, Nn = L.Nn;
+    long long r = bi;
+    const int s = (int)(r % Ns);
+    r /= Ns;
+    const int w = (int)(r % NO);
+    r /= NO;
+    const int v = (int)(r % Nn);
+    const int vp = (int)(r / Nn);
+    auto at = [&](int ww, int x, int y) { return q3[s + (long long)Ns * (ww + (long long)NO * (x + (long long)Nn * y))]; };
+    double* out = cuts + (size_t)cc * (NO + 3 * Nn);
+    for (int k = threadIdx.x; k < NO; k += blockDim.x) out[k] = at(k, v, vp);
+    for (int k = threadIdx.x; k < Nn; k += blockDim.x) {
+        out[NO + k] = at(w, k, k) - at(w, Nn - 1, Nn - 1);
+        out[NO + Nn + k] = at(w, k, vp) - at(w, Nn - 1, vp);
+        out[NO + 2 * Nn + k] = at(w, v, k) - at(w, v, Nn - 1);
+    }
+    if (threadIdx.x == 0) argmax[cc] = bi;
+}
+
+// resample_from_to (Action.jl:537-557): Σ by get_Σ on the old σ mesh, every q by the multilinear
+// interpolation of the old channel at the new frequencies (channel.jl:416-471), bare copied.
+// mesh_old / mesh_new: [σ | Ωs | νs | Ωt | νt] blocks.
+__global__ void resample_kernel(Layout L, const double* __restrict__ mesh_old, const double* __restrict__ mesh_new,
+                                const double* __restrict__ a, double* b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SMesh<double>& M = *reinterpret_cast<SMesh<double>*>(smem_raw);
+    load_mesh(M, mesh_old, L.Nsig, L.NO, L.Nn);
+    __syncthreads();
+    const int Ns = L.Ns, NO = L.NO, Nn = L.Nn;
+    const double* sig_new = mesh_new;
+    const double* Os_new = sig_new + L.Nsig;
+    const double* ns_new = Os_new + NO;
+    const double* Ot_new = ns_new + Nn;
+    const double* nt_new = Ot_new + NO;
+    const long long n = L.total;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        if (e < L.Nsig) {
+            b[e] = get_sigma(M, L.Nsig, a, sig_new[e]);
+            continue;
+        }
+        const long long in_comp = (e - L.Nsig) % L.comp;
+        if (in_comp < Ns) {  // bare
+            b[e] = a[e];
+            continue;
+        }
+        const long long rc = in_comp - Ns;
+        const int ch = (int)(rc / L.chan);
+        long long k = rc % L.chan;
+        const double* Om = ch == 1 ? M.Ot : M.Os;
+        const double* iOm = ch == 1 ? M.iOt : M.iOs;
+        const double* nu = ch == 1 ? M.nt : M.ns;
+        const double* inu = ch == 1 ? M.int_ : M.ins;
+        const double* Onew = ch == 1 ? Ot_new : Os_new;
+        const double* nnew = ch == 1 ? nt_new : ns_new;
+        const double* q = a + (e - in_comp) + Ns + (long long)ch * L.chan;  // this channel of the old action
+        const int s = (int)(k % Ns);
+        double val;
+        if (k < L.K1) {  // q1 (channel.jl:55-75)
+            const int w = (int)(k / Ns);
+            const Param<double> p1 = get_param(Onew[w], Om, iOm, NO);
+            val = p1.wl * q[s + (long long)Ns * p1.lo];
+            val += p1.wu * q[s + (long long)Ns * p1.hi];
+        } else if (k < L.K1 + 2 * L.K2) {  // q2_1, q2_2 (channel.jl:104-184)
+            const bool first = k < L.K1 + L.K2;
+            const long long kk = k - L.K1 - (first ? 0 : L.K2);
+            const int w = (int)((kk / Ns) % NO), v = (int)(kk / ((long long)Ns * NO));
+            const Param<double> pa = get_param(Onew[w], Om, iOm, NO);
+            const Param<double> pb = get_param(nnew[v], nu, inu, Nn);
+            const double* Q = q + L.K1 + (first ? 0 : L.K2);
+            auto ix = [&](int ww, int vv) { return s + (long long)Ns * (ww + (long long)NO * vv); };
+            val = pa.wl * pb.wl * Q[ix(pa.lo, pb.lo)];
+            val += pa.wu * pb.wl * Q[ix(pa.hi, pb.lo)];
+            val += pa.wl * pb.wu * Q[ix(pa.lo, pb.hi)];
+            val += pa.wu * pb.wu * Q[ix(pa.hi, pb.hi)];
+        } else {  // q3 (channel.jl:226-305)
+            const long long kk = k - L.K1 - 2 * L.K2;
+            long long r = kk / Ns;
+            const int w = (int)(r % NO);
+            r /= NO;
+            const int v = (int)(r % Nn), vp = (int)(r / Nn);
+            const Param<double> p1 = get_param(Onew[w], Om, iOm, NO);
+            const Param<double> p2 = get_param(nnew[v], nu, inu, Nn);
+            const Param<double> p3 = get_param(nnew[vp], nu, inu, Nn);
+            const double* Q = q + L.K1 + 2 * L.K2;
+            auto ix = [&](int ww, int x, int y) {
+                return s + (long long)Ns * (ww + (long long)NO * (x + (long long)Nn * y));
+            };
+            val = p1.wl * p2.wl * p3.wl * Q[ix(p1.lo, p2.lo, p3.lo)];
+            val += p1.wu * p2.wl * p3.wl * Q[ix(p1.hi, p2.lo, p3.lo)];
+            val += p1.wl * p2.wu * p3.wl * Q[ix(p1.lo, p2.hi, p3.lo)];
+            val += p1.wu * p2.wu * p3.wl * Q[ix(p1.hi, p2.hi, p3.lo)];
+            val += p1.wl * p2.wl * p3.wu * Q[ix(p1.lo, p2.lo, p3.hi)];
+            val += p1.wu * p2.wl * p3.wu * Q[ix(p1.hi, p2.lo, p3.hi)];
+            val += p1.wl * p2.wu * p3.wu * Q[ix(p1.lo, p2.hi, p3.hi)];
+            val += p1.wu * p2.wu * p3.wu * Q[ix(p1.hi, p2.hi, p3.hi)];
+        }
+        b[e] = val;
+    }
+}
+
+cudaError_t launch_scan_cuts(const Layout& L, const double* a, long long* argmax, double* cuts, cudaStream_t st) {
+    scan_cuts_kernel<<<3 * L.C, 256, 0, st>>>(L, a, argmax, cuts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resample(const Layout& L, const double* mesh_old, const double* mesh_new, const double* a,
+                            double* b, cudaStream_t st) {
+    const size_t smem = sizeof(SMesh<double>);
+    cudaError_t e = cudaFuncSetAttribute(resample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    resample_kernel<<<grid_for(L.total, 256), 256, smem, st>>>(L, mesh_old, mesh_new, a, b);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_symmetrize(const Layout& L, const int* exch, double* a, cudaStream_t st) {
     const int64_t n = (int64_t)L.Nn * (L.Nn - 1) / 2 * L.NO * L.Ns * 3 * L.C;
     if (n == 0) return cudaSuccess;

@@ -38,6 +38,7 @@ class FlowContext:
             raise _capi.PffrgError(self.lib.pffrg_last_error(None).decode())
         self.h = h
         self.num_sites = r.num_sites
+        self._layout = (m.num_sigma, m.num_omega, m.num_nu, 2 if symmetry == "su2" else 6)
 
     def close(self):
         if getattr(self, "h", None):
@@ -69,6 +70,23 @@ class FlowContext:
     def set_mesh(self, m) -> None:
         self._mesh, self._mesh_keep = _capi.mesh_view(m)
         self._check(self.lib.pffrg_set_mesh(self.h, ctypes.byref(self._mesh)), "set_mesh")
+
+    def scan_cuts(self, slot: int):
+        """(Σ, argmax[3 C], cuts[3 C, NΩ + 3 Nν]) of the action in `slot` for the mesh scans."""
+        lay = self._layout
+        sig = np.zeros(lay[0])
+        arg = np.zeros(3 * lay[3], dtype=np.int64)
+        cuts = np.zeros((3 * lay[3], lay[1] + 3 * lay[2]))
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(self.lib.pffrg_scan_cuts(self.h, slot, sig.ctypes.data_as(dp),
+                                             arg.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                             cuts.ctypes.data_as(dp)), "scan_cuts")
+        return sig, arg, cuts
+
+    def resample(self, src_slot: int, dst_slot: int, m) -> None:
+        """Interpolate the action in src_slot onto the meshes m into dst_slot; m becomes the context's."""
+        self._mesh, self._mesh_keep = _capi.mesh_view(m)
+        self._check(self.lib.pffrg_resample(self.h, src_slot, dst_slot, ctypes.byref(self._mesh)), "resample")
 
     def set_precision(self, precision: str) -> None:
         p = _capi.PFFRG_FP64 if precision == "fp64" else _capi.PFFRG_MIXED

@@ -96,14 +96,29 @@ def scan(x, y, p0, p1, p2, p3, p4) -> float:
     return min(max(num_lin * p3, min(da, db)), p4)
 
 
-def scan_channel(Lam, p_O, p_n, Om, nu, q3):
-    """(Ω_lin, ν_lin) of one channel from cuts through its maximum (Action.jl:452-480)."""
+def channel_cuts(q3):
+    """The cuts through max |q3| that scan_channel reads (Action.jl:452-480): q3[s, :, v, v'],
+    q3[s, w, k, k] - q3[s, w, end, end], q3[s, w, :, v'] - q3[s, w, end, v'], q3[s, w, v, :] - q3[s, w, v, end]."""
     idx = np.unravel_index(int(np.argmax(np.abs(q3).reshape(-1, order="F"))), q3.shape, order="F")
     s, w, v, vp = idx
+    nu = q3.shape[2]
     cut_O = q3[s, :, v, vp]
-    cut_1 = np.array([q3[s, w, k, k] - q3[s, w, -1, -1] for k in range(len(nu))])
+    cut_1 = np.array([q3[s, w, k, k] - q3[s, w, -1, -1] for k in range(nu)])
     cut_2 = q3[s, w, :, vp] - q3[s, w, -1, vp]
     cut_3 = q3[s, w, v, :] - q3[s, w, v, -1]
+    return np.concatenate([cut_O, cut_1, cut_2, cut_3])
+
+
+def scan_channel(Lam, p_O, p_n, Om, nu, q3):
+    """(Ω_lin, ν_lin) of one channel from cuts through its maximum (Action.jl:452-480)."""
+    return scan_cuts(Lam, p_O, p_n, Om, nu, channel_cuts(q3))
+
+
+def scan_cuts(Lam, p_O, p_n, Om, nu, cuts):
+    """scan_channel on its four cuts (as returned by channel_cuts or the device)."""
+    NO, Nn = len(Om), len(nu)
+    cut_O, cut_1 = cuts[:NO], cuts[NO:NO + Nn]
+    cut_2, cut_3 = cuts[NO + Nn:NO + 2 * Nn], cuts[NO + 2 * Nn:NO + 3 * Nn]
     O_lin = scan(Om, cut_O, p_O[0], p_O[1], p_O[2], p_O[3] * Lam, p_O[4] * Lam)
     n1 = scan(nu, cut_1, p_n[0], p_n[1], p_n[2], p_n[3] * Lam, p_n[4] * Lam)
     n2 = scan(nu, cut_2, p_n[0], p_n[1], p_n[2], p_n[3] * Lam, p_n[4] * Lam)
@@ -140,7 +155,22 @@ def _resample_channel(Om_old, nu_old, ch_old, Om_new, nu_new, ch_new):
 
 def resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m_old: F.Mesh, a_old: A.Action,
                      a_new: A.Action, chi=None) -> F.Mesh:
-    """New meshes at cutoff Λ and the action resampled onto them (Action.jl:483-548)."""
+    """New meshes at cutoff Λ and the action resampled onto them (Action.jl:483-548), on the host."""
+    cuts = [[channel_cuts(ch.q3) for ch in v.channels] for v in a_old.Γ]
+    m_new = new_meshes(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m_old, a_old.Σ, cuts, chi)
+    for k, w in enumerate(m_new.sigma):
+        a_new.Σ[k] = get_sigma(w, m_old.sigma, a_old.Σ)
+    for vo, vn in zip(a_old.Γ, a_new.Γ):
+        _resample_channel(m_old.omega_s, m_old.nu_s, vo.ch_s, m_new.omega_s, m_new.nu_s, vn.ch_s)
+        _resample_channel(m_old.omega_t, m_old.nu_t, vo.ch_t, m_new.omega_t, m_new.nu_t, vn.ch_t)
+        _resample_channel(m_old.omega_s, m_old.nu_s, vo.ch_u, m_new.omega_s, m_new.nu_s, vn.ch_u)
+    return m_new
+
+
+def new_meshes(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m_old: F.Mesh, Sigma, cuts,
+               chi=None) -> F.Mesh:
+    """The meshes of resample_from_to (Action.jl:499-544) from Σ, the cuts of every component's
+    s, t, u channel (cuts[c][ch]) and χ."""
     s_lin = lins[1] * Lam
     Os_lin = lins[2] * Lam
     ns_lin = lins[3] * Lam
@@ -148,14 +178,14 @@ def resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, 
     nt_lin = lins[3] * Lam
     c_lin = lins[4] * Lam
     if Lam < lins[0]:
-        s_lin = p_sigma[1] * m_old.sigma[int(np.argmax(np.abs(a_old.Σ)))]
+        s_lin = p_sigma[1] * m_old.sigma[int(np.argmax(np.abs(Sigma)))]
         Os, ns, Ot, nt = [], [], [], []
-        for v in a_old.Γ:
-            o1, n1 = scan_channel(Lam, p_Os, p_ns, m_old.omega_s, m_old.nu_s, v.ch_s.q3)
-            o2, n2 = scan_channel(Lam, p_Os, p_ns, m_old.omega_s, m_old.nu_s, v.ch_u.q3)
+        for cs in cuts:
+            o1, n1 = scan_cuts(Lam, p_Os, p_ns, m_old.omega_s, m_old.nu_s, cs[0])
+            o2, n2 = scan_cuts(Lam, p_Os, p_ns, m_old.omega_s, m_old.nu_s, cs[2])
             Os.append(min(o1, o2))
             ns.append(min(n1, n2))
-            o3, n3 = scan_channel(Lam, p_Ot, p_nt, m_old.omega_t, m_old.nu_t, v.ch_t.q3)
+            o3, n3 = scan_cuts(Lam, p_Ot, p_nt, m_old.omega_t, m_old.nu_t, cs[1])
             Ot.append(o3)
             nt.append(n3)
         Os_lin, ns_lin, Ot_lin, nt_lin = min(Os), min(ns), min(Ot), min(nt)
@@ -172,14 +202,7 @@ def resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, 
     Ot_m = F.get_mesh(Ot_lin, bounds[2] * b, m_old.num_omega - 1, p_Ot[0]) * p_Ot[5]
     nt_m = F.get_mesh(nt_lin, bounds[3] * b, m_old.num_nu - 1, p_nt[0]) * p_nt[5]
     chi_m = F.get_mesh(c_lin, bounds[4] * b, m_old.num_chi - 1, p_chi[0]) * p_chi[5]
-    m_new = F.Mesh(m_old.num_sigma, m_old.num_omega, m_old.num_nu, m_old.num_chi, sigma, Os_m, ns_m, Ot_m, nt_m, chi_m)
-    for k, w in enumerate(m_new.sigma):
-        a_new.Σ[k] = get_sigma(w, m_old.sigma, a_old.Σ)
-    for vo, vn in zip(a_old.Γ, a_new.Γ):
-        _resample_channel(m_old.omega_s, m_old.nu_s, vo.ch_s, m_new.omega_s, m_new.nu_s, vn.ch_s)
-        _resample_channel(m_old.omega_t, m_old.nu_t, vo.ch_t, m_new.omega_t, m_new.nu_t, vn.ch_t)
-        _resample_channel(m_old.omega_s, m_old.nu_s, vo.ch_u, m_new.omega_s, m_new.nu_s, vn.ch_u)
-    return m_new
+    return F.Mesh(m_old.num_sigma, m_old.num_omega, m_old.num_nu, m_old.num_chi, sigma, Os_m, ns_m, Ot_m, nt_m, chi_m)
 
 
 # ---------------------------------------------------------------------------
@@ -402,9 +425,11 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
             res.dLam.append(dLam)
             res.err.append(err)
             res.abs_max.append(amax)
-            t0 = time.perf_counter()
-            ctx.download(_capi.SLOT_NEXT, a_next)
-            res.timers["transfer"] += time.perf_counter() - t0
+            if measure or out:
+                # the callback and the checkpoints see the accepted state on the host
+                t0 = time.perf_counter()
+                ctx.download(_capi.SLOT_NEXT, a_next)
+                res.timers["transfer"] += time.perf_counter() - t0
             if amax >= 1000.0:
                 res.reason = "vertex has diverged"
                 if chi_tol is not None:
@@ -422,23 +447,28 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
                 if out:
                     out.measure(Lam, dLam, m, a_next, chi, ct=0.0)
                 break
-            # new meshes and resampled state (launcher_1l.jl:177)
+            # new meshes and the resampled state (launcher_1l.jl:177): the scans read Σ and the cuts
+            # through each channel's maximum from the device, the meshes are built on the host and
+            # the action is interpolated onto them on the device
             t0 = time.perf_counter()
-            a_new.buf[:] = a_next.buf
-            m = resample_from_to(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m, a_next, a_new,
-                                 chi if chi_tol is not None else None)
-            t1 = time.perf_counter()
-            res.timers["resample"] += t1 - t0
-            ctx.set_mesh(m)
-            ctx.upload(_capi.SLOT_A, a_new)
-            res.timers["transfer"] += time.perf_counter() - t1
+            sig, _, cuts = ctx.scan_cuts(_capi.SLOT_NEXT)
+            C = len(a.Γ)
+            cut_lists = [[cuts[3 * c + ch] for ch in range(3)] for c in range(C)]
+            m = new_meshes(Lam, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m, sig, cut_lists,
+                           chi if chi_tol is not None else None)
+            ctx.resample(_capi.SLOT_NEXT, _capi.SLOT_A, m)
+            res.timers["resample"] += time.perf_counter() - t0
         else:
             dLam = next_dlam(dLam)
             res.rejected += 1
     else:
         res.finished = True
     res.mesh = m
-    res.action = a_new if res.Lam else a
+    if res.Lam:
+        ctx.download(_capi.SLOT_A, a_new)
+        res.action = a_new
+    else:
+        res.action = a
 
 
 def launch_parquet(ctx: FlowContext, r, m, a: A.Action, Lam: float, max_iter: int, min_eval: int, max_eval: int,

@@ -118,16 +118,22 @@ def test_launch_writes_and_resumes_files(pkg, tmp_path):
     kw = dict(num_sigma=10, num_omega=4, num_nu=3, num_chi=4, initial=5.0, parquet=False, precision="fp64",
               ct=0.0)
     f = str(tmp_path / "run")
-    res = launch(f, "square", 3, "heisenberg", "su2", [[1.0]], final=3.0, **kw)
+    last = {}
+
+    def keep(Lam, dLam, m, a, ctx):
+        last.update(Lam=Lam, m=m, buf=a.buf.copy())
+
+    res = launch(f, "square", 3, "heisenberg", "su2", [[1.0]], final=3.0, measure=keep, **kw)
     assert res.finished
     with H.File(f + "_obs", "r") as o, H.File(f + "_cp", "r") as c:
         assert o.read("finished") is True and c.read("finished") is True
         cut = sorted((float(k) for k in o.keys("χ")), reverse=True)
         assert np.allclose(cut, res.Lam)
         assert o.read("reduced_lattice/model") == "heisenberg"
+        # the last checkpoint holds the accepted state before resampling, on its meshes
         Lam, dLam, m, a = D.read_checkpoint(c, 0.0)
-        assert Lam == res.Lam[-1]
-        assert np.array_equal(a.buf, res.action.buf)
+        assert Lam == res.Lam[-1] == last["Lam"]
+        assert np.array_equal(a.buf, last["buf"]) and np.array_equal(m.omega_s, last["m"].omega_s)
 
     # interrupted after two accepted steps, then resumed
     g = str(tmp_path / "cut")
@@ -166,3 +172,44 @@ def test_sweep_matches_single_runs(pkg):
         single = launch("", i.name, i.size, i.model, i.symmetry, i.J, **kw)
         assert r.Lam == single.Lam
         assert np.array_equal(r.action.buf, single.action.buf)
+
+
+@pytest.mark.parametrize("symmetry", ["su2", "u1-dm"])
+def test_device_resample_matches_host(pkg, symmetry):
+    """Mesh scans from the device cuts and the device resampling (pffrg_scan_cuts, pffrg_resample)
+    against the host restatement of resample_from_to (Action.jl:483-557)."""
+    import pffrg_gb300._capi as C
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300 import frequency as F
+    from pffrg_gb300 import launcher as LA
+    from pffrg_gb300.action import Action
+    from pffrg_gb300.flow import FlowContext
+
+    if symmetry == "su2":
+        w = wl.WORKLOADS["square-L3-1l"]
+    else:
+        w = wl.Workload("t", "kagome", 3, "kagome-xxz-dm", [[1.0, 0.8, 0.2]], 1, 1.0, 10, 5, 4, 0.1, 3,
+                        symmetry="u1-dm")
+    lat, r, m, a = wl.build_state(w, num_sigma=12, num_omega=6, num_nu=5)
+    P = (F.DEFAULT_P_SIGMA, F.DEFAULT_P_OMEGA, F.DEFAULT_P_NU, F.DEFAULT_P_OMEGA, F.DEFAULT_P_NU, F.DEFAULT_P_CHI,
+         F.DEFAULT_LINS, F.DEFAULT_BOUNDS)
+    chi = [np.random.default_rng(5).normal(size=(r.num_sites, m.num_chi))]
+    for Lam in (0.3, 8.0):  # scanned meshes below lins[1], scaled ones above
+        host = Action.empty_like(a)
+        m_host = LA.resample_from_to(Lam, *P, m, a, host, chi)
+        with FlowContext(r, m, symmetry=symmetry, precision="fp64") as ctx:
+            ctx.upload(C.SLOT_NEXT, a)
+            sig, arg, cuts = ctx.scan_cuts(C.SLOT_NEXT)
+            for c, v in enumerate(a.Γ):
+                for ch, chan in enumerate(v.channels):
+                    want = int(np.argmax(np.abs(chan.q3).reshape(-1, order="F")))
+                    assert arg[3 * c + ch] == want
+                    assert np.array_equal(cuts[3 * c + ch], LA.channel_cuts(chan.q3))
+            cl = [[cuts[3 * c + ch] for ch in range(3)] for c in range(len(a.Γ))]
+            m_dev = LA.new_meshes(Lam, *P, m, sig, cl, chi)
+            for name in ("sigma", "omega_s", "nu_s", "omega_t", "nu_t", "chi"):
+                assert np.array_equal(getattr(m_dev, name), getattr(m_host, name))
+            ctx.resample(C.SLOT_NEXT, C.SLOT_A, m_dev)
+            dev = Action.empty_like(a)
+            ctx.download(C.SLOT_A, dev)
+        assert np.max(np.abs(dev.buf - host.buf)) <= 1e-13 * np.max(np.abs(host.buf))
