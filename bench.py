@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
+    p.add_argument("--no-flow", action="store_true", help="skip the full-flow leg")
+    p.add_argument("--flow-final", type=float, default=0.01, help="final cutoff of the full-flow leg")
+    p.add_argument("--flow-precisions", default="mixed,fp64", help="precisions of the full-flow leg")
     return p.parse_args()
 
 
@@ -301,6 +304,9 @@ def ours(args):
         if dist:
             dist.destroy_process_group()
         return 0
+    flow = None
+    if world == 1 and not args.no_flow:
+        flow = flow_leg(args, local)
     # CPU baseline (oracle, all host cores, bounded strided sample), rank 0 at N=1 only
     cpu = None
     if world == 1 and not args.no_cpu:
@@ -325,6 +331,7 @@ def ours(args):
         "fp64": {"value": 1e3 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
                  "mixed_speedup": fp64_ms / ms_step} if fp64_ms else None,
         "mixed_vs_fp64_rel_err": err_mixed,
+        "full_flow": flow,
         "integrand_evals_per_step": evals_step,
         "clocks": clk,
     }
@@ -332,6 +339,47 @@ def ours(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+# the full flow of the square-lattice case: L = 3, nearest-neighbour Heisenberg, 1 loop, 50/15/10
+# frequencies, bare couplings at Λ = 50 (no parquet start), Bogacki-Shampine tolerance 1e-3, χ at
+# every accepted step; both precisions pass the same checkpoints, where their χ(ω = 0) is compared
+FLOW = dict(name="square", size=3, model="heisenberg", symmetry="su2", J=[[1.0]], num_sigma=50, num_omega=15,
+            num_nu=10, num_chi=10, initial=50.0, ode_tol=(1e-3, 1e-3), parquet=False, loops=1)
+FLOW_CPS = [10.0, 5.0, 2.0, 1.0, 0.5, 0.2, 0.1, 0.05, 0.02]
+
+
+def flow_leg(args, dev_index):
+    """Seconds of full flows (ODE steps, χ, resampling) per precision and χ(ω=0) of the mixed flow
+    against the FP64 flow at the shared checkpoints."""
+    from pffrg_gb300.launcher import launch
+
+    runs = {}
+    for prec in [s for s in args.flow_precisions.split(",") if s]:
+        kw = dict(FLOW)
+        name, size, model, sym, J = (kw.pop(k) for k in ("name", "size", "model", "symmetry", "J"))
+        t0 = time.perf_counter()
+        res = launch("", name, size, model, sym, J, final=args.flow_final, cps=FLOW_CPS, precision=prec,
+                     device=dev_index, **kw)
+        runs[prec] = (time.perf_counter() - t0, res)
+    out = {"workload": "square L=3 Heisenberg, 1 loop, 50/15/10, Λ 50 -> %g, ODE tol 1e-3, bare start"
+                       % args.flow_final}
+    for prec, (secs, res) in runs.items():
+        out[prec] = {"seconds": secs, "accepted_steps": len(res.Lam), "rejected_steps": res.rejected,
+                     "final_lambda": res.Lam[-1] if res.Lam else None, "reason": res.reason or "final cutoff",
+                     "timers_s": {k: round(v, 3) for k, v in res.timers.items()},
+                     "rhs_evaluations": res.rhs_evals}
+    if "mixed" in runs and "fp64" in runs:
+        out["speedup_mixed_vs_fp64"] = runs["fp64"][0] / runs["mixed"][0]
+        cm = {round(L, 12): c[:, 0] for (L, mesh, c) in runs["mixed"][1].chi}
+        cf = {round(L, 12): c[:, 0] for (L, mesh, c) in runs["fp64"][1].chi}
+        errs = {}
+        for L in FLOW_CPS:
+            a, b = cm.get(round(L, 12)), cf.get(round(L, 12))
+            if a is not None and b is not None:
+                errs[str(L)] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+        out["chi_static_rel_err_mixed_vs_fp64"] = errs
+    return out
 
 
 def fp64_leg(args, ctx, pkg, C, a, rhs, flush, dev, da_mixed):

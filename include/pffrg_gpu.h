@@ -231,6 +231,28 @@ const char* pffrg_noalloc_last_error(void);
 void* pffrg_host_alloc(int64_t bytes);
 void pffrg_host_free(void* p);
 
+/* Learned parquet warm start.  No counterpart in the reference: a multilayer
+ * perceptron (dense layers, tanh on all but the last, FP32) maps a model's
+ * couplings to the principal-component coordinates of its converged parquet
+ * vertex; a fixed affine decoder (basis[k][d], mean[d]) turns them into the
+ * vertex that starts the parquet iteration of src/Launcher/parquet.jl, which
+ * stays the judge of convergence.  sizes[0..nlayers] are the layer widths;
+ * parameters are stored layer by layer as W[n_in][n_out] then b[n_out].
+ * Training minimises the mean squared error over the whole batch with Adam. */
+typedef struct pffrg_mlp pffrg_mlp;
+pffrg_mlp* pffrg_mlp_create(int nlayers, const int* sizes, unsigned seed);
+void pffrg_mlp_destroy(pffrg_mlp* net);
+const char* pffrg_mlp_last_error(const pffrg_mlp* net);
+int64_t pffrg_mlp_num_params(const pffrg_mlp* net);
+int pffrg_mlp_get_params(pffrg_mlp* net, float* params);
+int pffrg_mlp_set_params(pffrg_mlp* net, const float* params);
+int pffrg_mlp_forward(pffrg_mlp* net, const float* x, int batch, float* y);
+int pffrg_mlp_gradient(pffrg_mlp* net, const float* x, const float* target, int batch, float* grads, float* loss);
+int pffrg_mlp_train(pffrg_mlp* net, const float* x, const float* target, int batch, int epochs, float lr,
+                    float* loss);
+int pffrg_mlp_set_decoder(pffrg_mlp* net, const float* basis, const float* mean, int k, int64_t d);
+int pffrg_mlp_predict(pffrg_mlp* net, const float* x, float* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -11,7 +11,7 @@ CSRC = HERE / "csrc"
 OUT_DIR = HERE / "_build"
 LIB = OUT_DIR / "libpffrg_gpu.so"
 SOURCES = ["pffrg_flow_f64.cu", "pffrg_flow_f32.cu", "pffrg_flow_u1dm_f64.cu", "pffrg_flow_u1dm_f32.cu",
-           "pffrg_sigma.cu", "pffrg_state.cu", "pffrg_capi.cu", "pffrg_noalloc.cu"]
+           "pffrg_sigma.cu", "pffrg_state.cu", "pffrg_capi.cu", "pffrg_noalloc.cu", "pffrg_mlp.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]

@@ -195,7 +195,7 @@ def test_device_resample_matches_host(pkg, symmetry):
          F.DEFAULT_LINS, F.DEFAULT_BOUNDS)
     chi = [np.random.default_rng(5).normal(size=(r.num_sites, m.num_chi))]
     for Lam in (0.3, 8.0):  # scanned meshes below lins[1], scaled ones above
-        host = Action.empty_like(a)
+        host = a.copy()  # the flow resamples a copy of the accepted state (bare couplings kept)
         m_host = LA.resample_from_to(Lam, *P, m, a, host, chi)
         with FlowContext(r, m, symmetry=symmetry, precision="fp64") as ctx:
             ctx.upload(C.SLOT_NEXT, a)
