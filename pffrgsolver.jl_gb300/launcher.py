@@ -289,7 +289,7 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
            loops: int = 1, parquet: bool = True, sigma_corr: bool = True, initial: float = 5.0,
            final: float = 0.05, bmin: float = 1e-4, bmax: float = 0.1, cps=(), overwrite: bool = True,
            wt: float = 23.5, ct: float = 1.0, precision: str = "mixed", device: int = 0, measure=None,
-           correlations: bool = True, verbose: bool = False) -> FlowResult:
+           correlations: bool = True, warm_start=None, verbose: bool = False) -> FlowResult:
     """Run the FRG flow from ``initial`` to ``final`` (launch!, Launcher.jl:565-773).
 
     After every accepted step the static correlations χ of the new state are
@@ -300,7 +300,9 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
 
     With a non-empty ``f`` the run writes the reference's ``f_obs`` / ``f_cp``
     HDF5 files; ``overwrite = False`` resumes from the last checkpoint of
-    existing files (Launcher.jl:704-760).
+    existing files (Launcher.jl:704-760).  ``warm_start`` (a fitted
+    ``warmstart.ParquetWarmStart``) starts the parquet iteration from its
+    predicted vertex instead of the bare couplings.
     """
     t0 = time.perf_counter()
     if symmetry not in A.SYMMETRIES:
@@ -342,6 +344,11 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
     ctx = FlowContext(r, m, symmetry=symmetry, S=S, precision=precision, device=device)
     try:
         if parquet:
+            if warm_start is not None:
+                from .warmstart import coupling_features, vertex_mask
+
+                mask = vertex_mask(a)
+                a.buf[mask] = warm_start.predict(coupling_features(J))
             res.parquet_iterations = launch_parquet(ctx, r, m, a, initial, max_iter, min_eval, max_eval, sigma_tol,
                                                     gamma_tol, parquet_tol, verbose=verbose)
             if out:
