@@ -194,6 +194,8 @@ typedef struct pffrg_stats {
     int64_t launches;           /* all kernel launches since the last reset */
     int64_t chi_evals;          /* χ integrand evaluations (cubature points) of the last pffrg_chi call */
     int64_t chi_regions_max;    /* largest region count of one χ integral in that call */
+    int64_t chi_rounds;         /* refinement rounds of all χ integrals in that call */
+    int64_t chi_rounds_max;     /* most rounds of one χ integral in that call */
 } pffrg_stats;
 int pffrg_set_timing(pffrg_ctx* ctx, int on);
 int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset);

@@ -34,7 +34,8 @@ EXPORTED = [
 class Stats(ctypes.Structure):
     _fields_ = [("integrand_evals", ctypes.c_int64), ("algorithmic_values", ctypes.c_int64),
                 ("pass_ms", ctypes.c_double), ("rhs_ms", ctypes.c_double), ("pass_launches", ctypes.c_int64),
-                ("launches", ctypes.c_int64), ("chi_evals", ctypes.c_int64), ("chi_regions_max", ctypes.c_int64)]
+                ("launches", ctypes.c_int64), ("chi_evals", ctypes.c_int64), ("chi_regions_max", ctypes.c_int64),
+                ("chi_rounds", ctypes.c_int64), ("chi_rounds_max", ctypes.c_int64)]
 
 
 class LatticeView(ctypes.Structure):

@@ -57,7 +57,7 @@ struct pffrg_ctx {
     long long gk_cap = 0, gk_slots = 0;
     int gk_overflow = 0;
     int async_waves = 1;  // device-driven quadrature levels (no host round trip per level)
-    int64_t chi_evals = 0, chi_regions_max = 0;
+    int64_t chi_evals = 0, chi_regions_max = 0, chi_rounds = 0, chi_rounds_max = 0;
     // wave workspace of the passes (device scratch) and its host-visible counters
     void* wave_mem = nullptr;
     size_t wave_bytes = 0;
@@ -519,8 +519,8 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     c.box_out = ctx->chi_box;
     c.chi = ctx->chi_out;
     c.status = ctx->status;
-    c.evals = ctx->counter + 2;  // [2], [3] of the context's counters
-    CK(cudaMemsetAsync(c.evals, 0, 2 * sizeof(unsigned long long), ctx->st));
+    c.evals = ctx->counter + 2;  // [2..5] of the context's counters
+    CK(cudaMemsetAsync(c.evals, 0, 4 * sizeof(unsigned long long), ctx->st));
     const long long cap_max = 10000000 / 34 + 2;
     const size_t budget = (size_t)16 << 30;
     std::vector<int> todo(njobs), over;
@@ -578,11 +578,13 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     }
     CK(cudaMemcpyAsync(chi, ctx->chi_out, sizeof(double) * ncomp * (size_t)Ns * num_chi, cudaMemcpyDeviceToHost,
                        ctx->st));
-    unsigned long long ev[2] = {0, 0};
+    unsigned long long ev[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(ev, c.evals, sizeof(ev), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     ctx->chi_evals = (int64_t)ev[0];
     ctx->chi_regions_max = (int64_t)ev[1];
+    ctx->chi_rounds = (int64_t)ev[2];
+    ctx->chi_rounds_max = (int64_t)ev[3];
     return 0;
 }
 
@@ -772,6 +774,8 @@ int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset) {
     out->launches = ctx->launches;
     out->chi_evals = ctx->chi_evals;
     out->chi_regions_max = ctx->chi_regions_max;
+    out->chi_rounds = ctx->chi_rounds;
+    out->chi_rounds_max = ctx->chi_rounds_max;
     if (reset) {
         ctx->pass_ms = ctx->rhs_ms = 0.0;
         ctx->pass_launches = ctx->launches = 0;
@@ -887,7 +891,7 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
          dalloc((void**)&ctx->corrs_sde, sizeof(double) * 6 * L.NO) &&
          dalloc((void**)&ctx->partial, sizeof(double) * kPartials) &&
          dalloc((void**)&ctx->scalars, sizeof(double) * 4) && dalloc((void**)&ctx->status, sizeof(int)) &&
-         dalloc((void**)&ctx->counter, 4 * sizeof(unsigned long long));
+         dalloc((void**)&ctx->counter, 6 * sizeof(unsigned long long));
     if (!ok) return bail("device allocation failed");
     if (cudaHostAlloc((void**)&ctx->h_scalars, sizeof(double) * 4, cudaHostAllocDefault) != cudaSuccess ||
         cudaHostAlloc((void**)&ctx->h_wave_counters, sizeof(int) * 8, cudaHostAllocDefault) != cudaSuccess)

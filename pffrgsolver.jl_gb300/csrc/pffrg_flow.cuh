@@ -380,8 +380,7 @@ struct Team {
         }
         if constexpr (C == 2) {
             // every team of the warp passes the same two warp barriers, whatever its channel
-            if (X == 1) eval_t_stage(count, g);
-            else eval_su(X, count, g);
+            eval_su2_nodes(X, count, g);
             __syncwarp();
             if (X == 1) eval_t_overlap(count, g);
             __syncwarp();
@@ -452,8 +451,17 @@ struct Team {
         }
     }
 
-    // phase B of the SU(2) s and u channels (flow_su2_s.jl, flow_su2_u.jl): per node and site
-    __device__ void eval_su(int X, int count, R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
+    // phase B of SU(2), node by node (one gather site for all channels keeps the kernel small):
+    // the s and u bubbles (flow_su2_s.jl, flow_su2_u.jl) per site, or for the t channel
+    // (flow_su2_t.jl:46-81) the local part per site and both slots staged in shared memory as
+    // [site][node] (spin, density) pairs for the overlap sums that follow
+    __device__ void eval_su2_nodes(int X, int count, R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
+        constexpr int NB = BatchOf<T, C, SPL>::NB;
+        using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
+        const int Ns = A.L.Ns;
+        constexpr int SS = t_site_stride<R, NB>();
+        R2* tb1 = reinterpret_cast<R2*>(tmp);  // [Ns][SS]
+        R2* tb2 = tb1 + (size_t)Ns * SS;
         const R two = (X == 0) ? (R)-2 : (R)2;
         for (int j = 0; j < count; ++j) {
             const NodeScratch<R, C>& ns = ts.node[j];
@@ -461,30 +469,14 @@ struct Team {
             R v1[C][SPL], v2[C][SPL];
             gather_slot<R, T, SPL, C>(A, ns, 0, tl, site_ex, v1);
             gather_slot<R, T, SPL, C>(A, ns, 1, tl, site_ex, v2);
+            if (X != 1) {
 #pragma unroll
-            for (int k = 0; k < SPL; ++k) {
-                g[j][0][k] = -p * (two * v1[0][k] * v2[0][k] + v1[0][k] * v2[1][k] + v1[1][k] * v2[0][k]);
-                g[j][1][k] = -p * ((R)3 * v1[0][k] * v2[0][k] + v1[1][k] * v2[1][k]);
+                for (int k = 0; k < SPL; ++k) {
+                    g[j][0][k] = -p * (two * v1[0][k] * v2[0][k] + v1[0][k] * v2[1][k] + v1[1][k] * v2[0][k]);
+                    g[j][1][k] = -p * ((R)3 * v1[0][k] * v2[0][k] + v1[1][k] * v2[1][k]);
+                }
+                continue;
             }
-        }
-    }
-
-    // phase B of the SU(2) t channel for the whole batch (flow_su2_t.jl:46-81), first half:
-    // the non-local vertices of every node are gathered, their local part combined, and both
-    // slots staged in shared memory as [site][node] pairs (spin, density)
-    __device__ void eval_t_stage(int count, R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
-        constexpr int NB = BatchOf<T, C, SPL>::NB;
-        using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
-        const int Ns = A.L.Ns;
-        constexpr int SS = t_site_stride<R, NB>();
-        R2* tb1 = reinterpret_cast<R2*>(tmp);  // [Ns][SS]
-        R2* tb2 = tb1 + (size_t)Ns * SS;
-        for (int j = 0; j < count; ++j) {
-            const NodeScratch<R, C>& ns = ts.node[j];
-            const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
-            R v1[C][SPL], v2[C][SPL];
-            gather_slot<R, T, SPL, C>(A, ns, 0, tl, site_ex, v1);
-            gather_slot<R, T, SPL, C>(A, ns, 1, tl, site_ex, v2);
             const R v3s = ns.loc[0], v3d = ns.loc[1], v4s = ns.loc[2], v4d = ns.loc[3];
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {

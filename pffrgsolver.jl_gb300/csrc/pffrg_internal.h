@@ -176,7 +176,7 @@ struct ChiArgs {
     long long cap;           // regions per integral
     double* box_out;         // [ncomp][num_chi][Ns][9]
     double* chi;             // [ncomp][Ns][num_chi], each column-major
-    unsigned long long* evals;  // [0] cubature points evaluated, [1] largest region count
+    unsigned long long* evals;  // [0] cubature points, [1] largest region count, [2] rounds, [3] most rounds
     double* seg;             // Gauss-Kronrod segments of the local term: [num_chi][4][seg_cap]
     long long seg_cap;
     int* status;             // bit 1: GK segments exhausted

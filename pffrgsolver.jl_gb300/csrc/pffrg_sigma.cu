@@ -660,9 +660,11 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, cons
     long long numeval = 17;
     const long long maxevals = 10000000;
     bool over = false;
+    long long rounds = 0;
     auto converged = [&](double err, double val) { return !(err > A.atol && err > fabs(val) * A.rtol); };
     while (numeval < maxevals) {
         if (converged(tot_err, tot_val)) break;
+        ++rounds;
         double ee_err = tot_err;
         const double ee_val = tot_val;
         const int n0 = n;
@@ -738,6 +740,8 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, cons
         if (A.evals && !over) {
             atomicAdd(A.evals, (unsigned long long)numeval);
             atomicMax(A.evals + 1, (unsigned long long)n);
+            atomicAdd(A.evals + 2, (unsigned long long)rounds);
+            atomicMax(A.evals + 3, (unsigned long long)rounds);
         }
     }
 }

@@ -191,6 +191,9 @@ def test_device_resample_matches_host(pkg, symmetry):
         w = wl.Workload("t", "kagome", 3, "kagome-xxz-dm", [[1.0, 0.8, 0.2]], 1, 1.0, 10, 5, 4, 0.1, 3,
                         symmetry="u1-dm")
     lat, r, m, a = wl.build_state(w, num_sigma=12, num_omega=6, num_nu=5)
+    # a smooth self energy (the scans read argmax |Σ|; a noisy one can place it where the reference's
+    # own mesh rule has no valid linear bound)
+    a.Σ[:] = m.sigma / (1.0 + m.sigma ** 2)
     P = (F.DEFAULT_P_SIGMA, F.DEFAULT_P_OMEGA, F.DEFAULT_P_NU, F.DEFAULT_P_OMEGA, F.DEFAULT_P_NU, F.DEFAULT_P_CHI,
          F.DEFAULT_LINS, F.DEFAULT_BOUNDS)
     chi = [np.random.default_rng(5).normal(size=(r.num_sites, m.num_chi))]
