@@ -1357,56 +1357,37 @@ inline void gm_eval(Region2& R, const double* v) {
     R.split = diff[1] > diff[0] ? 1 : 0;
 }
 
-// max-heap of region indices keyed by their error estimate, 32 children per
-// node (children of h at 32 h + 1 .. 32 h + 32).  push sifts up while the
-// parent's key is smaller; pop moves the last entry to the root and sifts it
-// down to the largest child (the first of equal largest keys) while that child
-// is larger.  The GPU kernel uses the same rules (its pops compare the 32
-// children of a node across a warp), so both pop regions in the same order.
-struct RegionHeap {
-    static constexpr int D = 32;
-    std::vector<double> key;
-    std::vector<int> idx;
-    void push(double k, int i) {
-        int h = (int)key.size();
-        key.push_back(k);
-        idx.push_back(i);
-        while (h > 0) {
-            const int p = (h - 1) / D;
-            if (key[p] >= k) break;
-            key[h] = key[p];
-            idx[h] = idx[p];
-            h = p;
-        }
-        key[h] = k;
-        idx[h] = i;
+// regions waiting to be cut, largest error first; equal errors leave in the order
+// they were filed (a counter stamps every push).  The C library's binary heap
+// leaves ties in an order set by its layout; this rule is fixed instead, and the
+// GPU kernel keeps the same order with a sorted list (stable sort of each round's
+// halves, merged after the older entries of equal error).
+struct RegionQueue {
+    struct E {
+        double err;
+        long long stamp;
+        int idx;
+    };
+    std::vector<E> h;
+    long long next = 0;
+    // a has lower priority than b
+    static bool lower(const E& a, const E& b) { return a.err < b.err || (a.err == b.err && a.stamp > b.stamp); }
+    void push(double err, int i) {
+        h.push_back({err, next++, i});
+        std::push_heap(h.begin(), h.end(), lower);
     }
     int pop() {
-        const int top = idx[0];
-        const double k = key.back();
-        const int i = idx.back();
-        key.pop_back();
-        idx.pop_back();
-        const int n = (int)key.size();
-        if (n > 0) {
-            int h = 0;
-            for (;;) {
-                const int c0 = D * h + 1;
-                if (c0 >= n) break;
-                int c = c0;
-                for (int q = c0 + 1; q < std::min(c0 + D, n); ++q)
-                    if (key[q] > key[c]) c = q;
-                if (key[c] <= k) break;
-                key[h] = key[c];
-                idx[h] = idx[c];
-                h = c;
-            }
-            key[h] = k;
-            idx[h] = i;
-        }
-        return top;
+        std::pop_heap(h.begin(), h.end(), lower);
+        const int i = h.back().idx;
+        h.pop_back();
+        return i;
     }
+    bool empty() const { return h.empty(); }
 };
+
+// the final total: 256 consecutive blocks of regions (index order), each summed in
+// order, then the block sums in order (the GPU block's threads sum one block each)
+constexpr int kChiSumBlocks = 256;
 
 template <class F>
 double hcubature2(F& f, const double xmin[2], const double xmax[2], double abstol, double reltol,
@@ -1426,7 +1407,7 @@ double hcubature2(F& f, const double xmin[2], const double xmax[2], double absto
     }
     R0.vol = (2.0 * R0.h[0]) * (2.0 * R0.h[1]);
     eval(R0);
-    RegionHeap heap;
+    RegionQueue heap;
     heap.push(R0.err, 0);
     double tot_val = R0.val, tot_err = R0.err;
     long long numeval = 17;
@@ -1457,7 +1438,7 @@ double hcubature2(F& f, const double xmin[2], const double xmax[2], double absto
             cut.push_back((int)regs.size() - 1);
             numeval += 34;
             if (converged(ee_err, ee_val)) break;
-        } while (!heap.key.empty() && numeval < maxevals);
+        } while (!heap.empty() && numeval < maxevals);
         for (int r : cut) eval(regs[r]);
         for (int r : cut) {
             heap.push(regs[r].err, r);
@@ -1465,9 +1446,14 @@ double hcubature2(F& f, const double xmin[2], const double xmax[2], double absto
             tot_err += regs[r].err;
         }
     }
-    // the total in heap order, as the library sums it
+    const int n = (int)regs.size();
+    const int c = (n + kChiSumBlocks - 1) / kChiSumBlocks;
     double I = 0.0;
-    for (int i : heap.idx) I += regs[i].val;
+    for (int t = 0; t < kChiSumBlocks; ++t) {
+        double p = 0.0;
+        for (int q = std::min(n, t * c); q < std::min(n, (t + 1) * c); ++q) p += regs[q].val;
+        I += p;
+    }
     return I;
 }
 

@@ -527,7 +527,7 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     for (long long j = 0; j < njobs; ++j) todo[j] = (int)j;
     long long cap = 512;
     while (!todo.empty()) {
-        const size_t per_job = (size_t)cap * (8 * sizeof(double) + 2 * sizeof(int));
+        const size_t per_job = (size_t)cap * (10 * sizeof(double) + 4 * sizeof(int));
         const long long batch = std::max<long long>(1, std::min<long long>((long long)todo.size(),
                                                                            (long long)(budget / per_job)));
         if (per_job * (size_t)batch > ctx->chi_reg_bytes) {
@@ -536,8 +536,8 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
             ctx->chi_reg = nullptr;
             ctx->chi_split = nullptr;
             ctx->chi_reg_bytes = 0;
-            CK(cudaMalloc(&ctx->chi_reg, sizeof(double) * 8 * (size_t)cap * batch));
-            CK(cudaMalloc(&ctx->chi_split, sizeof(int) * 2 * (size_t)cap * batch));
+            CK(cudaMalloc(&ctx->chi_reg, sizeof(double) * 10 * (size_t)cap * batch));
+            CK(cudaMalloc(&ctx->chi_split, sizeof(int) * 4 * (size_t)cap * batch));
             ctx->chi_reg_bytes = per_job * (size_t)batch;
         }
         c.reg = ctx->chi_reg;

@@ -171,8 +171,8 @@ struct ChiArgs {
     int ncomp;               // 1 (SU(2)) or 3 (U(1)-DM: xx, zz, xy)
     const int* exch;
     double Lam, atol, rtol, twoS;
-    double* reg;             // [job slot][8][cap] region records and heap keys
-    int* reg_split;          // [job slot][2][cap] split / cut-from words and heap indices
+    double* reg;             // [job slot][10][cap] region records (7) and the keys of three region lists
+    int* reg_split;          // [job slot][4][cap] split dimensions and the entries of three region lists
     long long cap;           // regions per integral
     double* box_out;         // [ncomp][num_chi][Ns][9]
     double* chi;             // [ncomp][Ns][num_chi], each column-major

@@ -373,13 +373,18 @@ cudaError_t launch_corrs(const CorrsArgs<R>& a, cudaStream_t st) {
 // degree-7/5 rule for dim = 2 (17 points, error |R7 - R5|), split along the
 // dimension with the largest fourth difference, and per round the bisection
 // of every largest-error region needed to bring the remaining error under
-// max(atol, rtol |I|).  One warp per (ω, site, box) integral, FP64; the
-// regions live in device scratch (capacity per integral: chi_cap).
+// max(atol, rtol |I|).  One block per (ω, site, component, box) integral;
+// the regions live in device scratch (capacity per integral: ChiArgs::cap),
+// the coordinates, rules and sums in FP64.
 // ---------------------------------------------------------------------------
 constexpr double kGL2 = 0.3585685828003180919906451539079374954541;  // sqrt(9/70)
 constexpr double kGL4 = 0.9486832980505137995996680633298155601160;  // sqrt(9/10)
 constexpr double kGL5 = 0.6882472016116852977216287342936235251269;  // sqrt(9/19)
 
+// Regions of one integral.  The geometry, rule values and errors are indexed by
+// region; the regions waiting to be cut are kept as a list sorted by error
+// (largest first; equal errors in the order they were filed), in three buffers
+// that take turns as the list, the round's new entries and the sort scratch.
 struct ChiRegions {
     double* c0;
     double* c1;
@@ -388,67 +393,152 @@ struct ChiRegions {
     double* vol;
     double* val;
     double* err;
-    int* split;    // bit 0: split dimension; bits 1+: the region the second half of a cut was cut from
-    double* hkey;  // max-heap of region indices keyed by error
-    int* hidx;
+    int* split;                   // split dimension given by the region's last rule
+    unsigned long long* key[3];   // list keys: ~bits(err), ascending = error descending
+    int* idx[3];                  // list entries: region index
 };
 
-// region heap of one integral: 32 children per node, the oracle's sift rules.  push runs on
-// lane 0; pop is warp-collective, one lane per child of the node being sifted.
-constexpr int kHeapD = 32;
+constexpr int kChiThreads = 256;   // one block per integral
+constexpr int kChiChunk = 128;     // regions whose 17 points are evaluated per pass of the block
+constexpr int kChiScan = 1024;     // list entries staged per step of the sequential sums
+constexpr int kChiSumBlocks = 256; // blocks of the final sum (the oracle sums the same blocks)
+constexpr int kSortItems = 8;      // list entries per thread and tile of the radix sort
 
-__device__ __forceinline__ void heap_push(ChiRegions& R, int& hn, double k, int i) {
-    int h = hn++;
-    while (h > 0) {
-        const int p = (h - 1) / kHeapD;
-        if (R.hkey[p] >= k) break;
-        R.hkey[h] = R.hkey[p];
-        R.hidx[h] = R.hidx[p];
-        h = p;
-    }
-    R.hkey[h] = k;
-    R.hidx[h] = i;
+// shared scratch of one integral; the phases of a round use it in turn
+struct ChiScratch {
+    union {
+        double f[kChiChunk * 17];
+        struct {
+            double e[kChiScan];
+            double v[kChiScan];
+        } scan;
+        struct {
+            unsigned hist[8][256];
+            unsigned base[256];
+            unsigned cnt[kChiThreads / 32][256];
+        } sort;
+    };
+    unsigned wsum[kChiThreads / 32];
+    double tot_val, tot_err;
+    long long numeval;
+    int K, done, over;
+};
+
+__device__ __forceinline__ unsigned long long err_key(double e) {
+    return ~(unsigned long long)__double_as_longlong(e);  // e >= 0: bits ascending with e
 }
 
-__device__ __forceinline__ int heap_pop_warp(ChiRegions& R, int& hn) {
-    const int lane = threadIdx.x & 31;
-    const int top = R.hidx[0];
-    const int n = --hn;
-    const double k = R.hkey[n];
-    const int i = R.hidx[n];
-    __syncwarp();
-    int h = 0;
-    if (n > 0) {
-        for (;;) {
-            const int c0 = kHeapD * h + 1;
-            if (c0 >= n) break;
-            const int c = c0 + lane;
-            double best = (c < n) ? R.hkey[c] : -1.0;
-            int bc = (c < n) ? c : 0x7fffffff;
-            // the largest child, the first of equal largest keys
-            for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oc = __shfl_xor_sync(0xffffffffu, bc, o);
-                if (ob > best || (ob == best && oc < bc)) {
-                    best = ob;
-                    bc = oc;
+// Stable LSD radix sort (8-bit digits) of cnt >= 1 (key, index) pairs by the block, from
+// (k0, i0) with (k1, i1) as scratch; digits shared by every key are skipped.  Returns the
+// buffer that holds the result (0: k0/i0, 1: k1/i1).
+__device__ int block_radix_sort(unsigned long long* k0, int* i0, unsigned long long* k1, int* i1, int cnt,
+                                ChiScratch& S) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int q = tid; q < 8 * 256; q += kChiThreads) (&S.sort.hist[0][0])[q] = 0u;
+    __syncthreads();
+    for (int e = tid; e < cnt; e += kChiThreads) {
+        const unsigned long long k = k0[e];
+#pragma unroll
+        for (int d = 0; d < 8; ++d) atomicAdd(&S.sort.hist[d][(unsigned)(k >> (8 * d)) & 255u], 1u);
+    }
+    __syncthreads();
+    int cur = 0;
+    for (int d = 0; d < 8; ++d) {
+        unsigned long long* ks = cur ? k1 : k0;
+        int* is = cur ? i1 : i0;
+        unsigned long long* kd = cur ? k0 : k1;
+        int* id = cur ? i0 : i1;
+        if (S.sort.hist[d][(unsigned)(ks[0] >> (8 * d)) & 255u] == (unsigned)cnt) continue;
+        {  // exclusive prefix of the digit counts
+            const unsigned x = S.sort.hist[d][tid];
+            unsigned inc = x;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            if (lane == 31) S.wsum[warp] = inc;
+            __syncthreads();
+            unsigned off = 0;
+            for (int w = 0; w < warp; ++w) off += S.wsum[w];
+            S.sort.base[tid] = off + inc - x;
+        }
+        __syncthreads();
+        unsigned* cw = S.sort.cnt[warp];
+        for (int t0 = 0; t0 < cnt; t0 += kChiThreads * kSortItems) {
+            for (int q = lane; q < 256; q += 32) cw[q] = 0u;
+            __syncwarp();
+            unsigned long long kk[kSortItems];
+            int ii[kSortItems];
+            unsigned dg[kSortItems], rk[kSortItems];
+            // each warp ranks its 256 consecutive entries of the tile, in order
+#pragma unroll
+            for (int s = 0; s < kSortItems; ++s) {
+                const int e = t0 + (warp * kSortItems + s) * 32 + lane;
+                const bool ok = e < cnt;
+                kk[s] = ok ? ks[e] : 0ull;
+                ii[s] = ok ? is[e] : 0;
+                dg[s] = ok ? ((unsigned)(kk[s] >> (8 * d)) & 255u) : 256u + (unsigned)lane;
+                const unsigned peers = __match_any_sync(0xffffffffu, dg[s]);
+                rk[s] = ok ? cw[dg[s]] + (unsigned)__popc(peers & lt) : 0u;
+                __syncwarp();
+                if (ok && (peers & lt) == 0u) cw[dg[s]] += (unsigned)__popc(peers);
+                __syncwarp();
+            }
+            __syncthreads();
+            {  // each digit's destinations: earlier tiles, then the warps in order
+                unsigned run = S.sort.base[tid];
+                for (int w = 0; w < kChiThreads / 32; ++w) {
+                    const unsigned c = S.sort.cnt[w][tid];
+                    S.sort.cnt[w][tid] = run;
+                    run += c;
+                }
+                S.sort.base[tid] = run;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int s = 0; s < kSortItems; ++s) {
+                const int e = t0 + (warp * kSortItems + s) * 32 + lane;
+                if (e < cnt) {
+                    const unsigned p = cw[dg[s]] + rk[s];
+                    kd[p] = kk[s];
+                    id[p] = ii[s];
                 }
             }
-            if (best <= k) break;
-            if (lane == 0) {
-                R.hkey[h] = best;
-                R.hidx[h] = R.hidx[bc];
-            }
-            __syncwarp();
-            h = bc;
+            __syncthreads();
         }
-        if (lane == 0) {
-            R.hkey[h] = k;
-            R.hidx[h] = i;
+        cur ^= 1;
+    }
+    return cur;
+}
+
+// merge the sorted lists a[0, na) and b[0, nb) into o; equal keys: a's first
+__device__ void block_merge(const unsigned long long* ak, const int* ai, int na, const unsigned long long* bk,
+                            const int* bi, int nb, unsigned long long* ok, int* oi) {
+    const int n = na + nb;
+    const int per = (n + kChiThreads - 1) / kChiThreads;
+    const int d0 = min(n, (int)threadIdx.x * per), d1 = min(n, d0 + per);
+    if (d0 < d1) {
+        int lo = max(0, d0 - nb), hi = min(d0, na);
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (ak[mid] <= bk[d0 - 1 - mid]) lo = mid + 1;
+            else hi = mid;
+        }
+        int i = lo, j = d0 - lo;
+        for (int d = d0; d < d1; ++d) {
+            if (j >= nb || (i < na && ak[i] <= bk[j])) {
+                ok[d] = ak[i];
+                oi[d] = ai[i];
+                ++i;
+            } else {
+                ok[d] = bk[j];
+                oi[d] = bi[j];
+                ++j;
+            }
         }
     }
-    __syncwarp();
-    return top;
+    __syncthreads();
 }
 
 // point k of the 17 Genz-Malik points of region (c, h), the library's order
@@ -565,53 +655,52 @@ struct ChiKernel {
     }
 };
 
-// evaluate the pending regions [first, first + count) of one integral (17 points each over the lanes)
-template <class F>
-__device__ void chi_eval_regions(const F& f, ChiRegions R, const int* idx, int count, double* fbuf) {
-    const int lane = threadIdx.x & 31;
-    for (int base = 0; base < count * 17; base += 32) {
-        const int e = base + lane;
-        if (e < count * 17) {
-            const int r = idx[e / 17], k = e % 17;
+// evaluate regions reg(0 .. count) of one integral with the block: the 17 points of
+// kChiChunk regions at a time, then each region's rule; emit(e, r, err) sees every result
+template <class F, class Reg, class Emit>
+__device__ void chi_eval_block(const F& f, const ChiRegions& R, const Reg& reg, int count, ChiScratch& S,
+                               const Emit& emit) {
+    const int tid = threadIdx.x;
+    for (int cb = 0; cb < count; cb += kChiChunk) {
+        const int cnt = min(kChiChunk, count - cb);
+        for (int p = tid; p < cnt * 17; p += kChiThreads) {
+            const int r = reg(cb + p / 17);
             double x, y;
-            gm_point(k, R.c0[r], R.c1[r], R.h0[r], R.h1[r], x, y);
-            fbuf[e] = f(x, y);
+            gm_point(p % 17, R.c0[r], R.c1[r], R.h0[r], R.h1[r], x, y);
+            S.f[p] = f(x, y);
         }
+        __syncthreads();
+        for (int q = tid; q < cnt; q += kChiThreads) {
+            const int r = reg(cb + q);
+            double val, err;
+            int sp;
+            gm_rule(S.f + 17 * q, R.vol[r], val, err, sp);
+            R.val[r] = val;
+            R.err[r] = err;
+            R.split[r] = sp;
+            emit(cb + q, r, err);
+        }
+        __syncthreads();
     }
-    __syncwarp();
-    for (int q = lane; q < count; q += 32) {
-        const int r = idx[q];
-        double val, err;
-        int sp;
-        gm_rule(fbuf + 17 * q, R.vol[r], val, err, sp);
-        R.val[r] = val;
-        R.err[r] = err;
-        R.split[r] = (R.split[r] & ~1) | sp;
-    }
-    __syncwarp();
 }
 
-constexpr int kChiWarps = 2;
-constexpr int kChiPend = 64;  // regions evaluated per batch
-
-// One warp per (ω, site, component, box) integral of the job list; a job that
-// runs out of region capacity raises its overflow flag and is run again with a
-// larger capacity.
+// One block per (ω, site, component, box) integral of the job list.  A round takes
+// the head of the sorted list (the library's pop order) while the remaining error
+// is above the bound, cuts those regions, evaluates the halves with the whole block,
+// adds them in cut order, sorts them and merges them into the rest of the list.  A
+// job that runs out of region capacity raises its overflow flag and is run again
+// with a larger capacity.
 template <typename RT>
-__global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, const int* __restrict__ jobs, int njobs,
-                                                                  int* overflow) {
+__global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, const int* __restrict__ jobs,
+                                                                   int njobs, int* overflow) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SMesh<RT>& M = *reinterpret_cast<SMesh<RT>*>(smem_raw);
-    double* fb = reinterpret_cast<double*>(smem_raw + sizeof(SMesh<RT>));
-    int* pend = reinterpret_cast<int*>(fb + kChiWarps * kChiPend * 17);
+    ChiScratch& S = *reinterpret_cast<ChiScratch*>(smem_raw + sizeof(SMesh<RT>));
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long slot = (long long)blockIdx.x * kChiWarps + warp;
+    const int tid = threadIdx.x;
+    const long long slot = blockIdx.x;
     if (slot >= njobs) return;
     const long long job = jobs[slot];
-    double* fbuf = fb + warp * kChiPend * 17;
-    int* pidx = pend + warp * kChiPend;
     // job = ((ω index * Ns + site) * ncomp + component) * 9 + box
     const int box = (int)(job % 9);
     const long long rj = job / 9;
@@ -625,120 +714,182 @@ __global__ void __launch_bounds__(kChiWarps * 32) chi_box_kernel(ChiArgs A, cons
     const double lo[3] = {0.0, 0.5 - s, 0.5 + s}, hi[3] = {0.5 - s, 0.5 + s, 1.0};
     const int row = 2 - box / 3, col = box % 3;  // the reference's order: top line first
     ChiRegions R;
-    const size_t cap = A.cap;
-    const size_t off = (size_t)slot * cap;
-    R.c0 = A.reg + off * 8;
-    R.c1 = R.c0 + cap;
-    R.h0 = R.c1 + cap;
-    R.h1 = R.h0 + cap;
-    R.vol = R.h1 + cap;
-    R.val = R.vol + cap;
-    R.err = R.val + cap;
-    R.hkey = R.err + cap;
-    R.split = A.reg_split + off * 2;
-    R.hidx = R.split + cap;
+    const long long cap = A.cap;
+    {
+        double* d = A.reg + (size_t)slot * cap * 10;
+        int* i = A.reg_split + (size_t)slot * cap * 4;
+        R.c0 = d;
+        R.c1 = d + cap;
+        R.h0 = d + 2 * cap;
+        R.h1 = d + 3 * cap;
+        R.vol = d + 4 * cap;
+        R.val = d + 5 * cap;
+        R.err = d + 6 * cap;
+        R.split = i;
+        for (int b = 0; b < 3; ++b) {
+            R.key[b] = reinterpret_cast<unsigned long long*>(d + (7 + b) * cap);
+            R.idx[b] = i + (1 + b) * cap;
+        }
+    }
     const RT* state;
     if constexpr (sizeof(RT) == 8) state = A.a;
     else state = A.af;
     ChiKernel<RT> f{A, M, state, site, k, wv};
-    if (lane == 0) {
+    if (tid == 0) {
         R.c0[0] = 0.5 * (lo[col] + hi[col]);
         R.c1[0] = 0.5 * (lo[row] + hi[row]);
         R.h0[0] = 0.5 * (hi[col] - lo[col]);
         R.h1[0] = 0.5 * (hi[row] - lo[row]);
         R.vol[0] = (2.0 * R.h0[0]) * (2.0 * R.h1[0]);
-        R.split[0] = 0;
-        pidx[0] = 0;
     }
-    __syncwarp();
-    chi_eval_regions(f, R, pidx, 1, fbuf);
-    int n = 1, hn = 0;
-    if (lane == 0) heap_push(R, hn, R.err[0], 0);
-    hn = __shfl_sync(0xffffffffu, hn, 0);  // the heap size is kept uniform across the warp
-    __syncwarp();
-    double tot_val = R.val[0], tot_err = R.err[0];
-    long long numeval = 17;
-    const long long maxevals = 10000000;
-    bool over = false;
+    __syncthreads();  // the mesh and region 0
+    int cur = 0;
+    chi_eval_block(f, R, [](int) { return 0; }, 1, S, [&](int, int r, double e) {
+        R.key[cur][0] = err_key(e);
+        R.idx[cur][0] = r;
+    });
+    // the control state lives in S and is written by thread 0 between barriers
+    int n = 1, m = 1;
     long long rounds = 0;
-    auto converged = [&](double err, double val) { return !(err > A.atol && err > fabs(val) * A.rtol); };
-    while (numeval < maxevals) {
-        if (converged(tot_err, tot_val)) break;
-        ++rounds;
-        double ee_err = tot_err;
-        const double ee_val = tot_val;
-        const int n0 = n;
-        int npend = 0;
-        // pop the largest-error regions (the library's parallel mode) and halve each
-        do {
-            if (n + 1 > (int)cap) {
-                over = true;
-                break;
-            }
-            const int bi = heap_pop_warp(R, hn);
-            const double pv = R.val[bi], pe = R.err[bi];
-            tot_val -= pv;
-            tot_err -= pe;
-            ee_err -= pe;
-            if (lane == 0) {
-                const int d = R.split[bi] & 1;
-                R.c0[n] = R.c0[bi];
-                R.c1[n] = R.c1[bi];
-                R.h0[n] = R.h0[bi];
-                R.h1[n] = R.h1[bi];
-                if (d == 0) {
-                    R.h0[bi] *= 0.5;
-                    R.h0[n] = R.h0[bi];
-                    R.c0[bi] -= R.h0[bi];
-                    R.c0[n] += R.h0[bi];
-                } else {
-                    R.h1[bi] *= 0.5;
-                    R.h1[n] = R.h1[bi];
-                    R.c1[bi] -= R.h1[bi];
-                    R.c1[n] += R.h1[bi];
-                }
-                R.vol[bi] *= 0.5;
-                R.vol[n] = (2.0 * R.h0[n]) * (2.0 * R.h1[n]);
-                R.split[bi] = 0;
-                R.split[n] = bi << 1;
-                pidx[npend] = bi;
-                pidx[npend + 1] = n;
-            }
-            __syncwarp();
-            npend += 2;
-            ++n;
-            numeval += 34;
-            if (converged(ee_err, ee_val)) break;
-            if (npend + 2 > kChiPend) {
-                chi_eval_regions(f, R, pidx, npend, fbuf);
-                npend = 0;
-            }
-        } while (hn > 0 && numeval < maxevals);
-        if (npend) chi_eval_regions(f, R, pidx, npend, fbuf);
-        // the round's regions join the heap, in the order they were cut
-        for (int q = n0; q < n; ++q) {
-            const int tw = R.split[q] >> 1;
-            tot_val += R.val[tw];
-            tot_err += R.err[tw];
-            tot_val += R.val[q];
-            tot_err += R.err[q];
-            if (lane == 0) {
-                heap_push(R, hn, R.err[tw], tw);
-                heap_push(R, hn, R.err[q], q);
-            }
-        }
-        hn = __shfl_sync(0xffffffffu, hn, 0);
-        __syncwarp();
-        if (over) break;
+    if (tid == 0) {
+        S.tot_val = R.val[0];
+        S.tot_err = R.err[0];
+        S.numeval = 17;
+        S.over = 0;
     }
-    // the total in heap order, as the library sums it
-    double I = 0.0;
-    if (lane == 0) {
-        for (int q = 0; q < hn; ++q) I += R.val[R.hidx[q]];
+    __syncthreads();
+    const long long maxevals = 10000000;
+    auto converged = [&](double err, double val) { return !(err > A.atol && err > fabs(val) * A.rtol); };
+    while (S.numeval < maxevals && !converged(S.tot_err, S.tot_val)) {
+        ++rounds;
+        // 1. the pops: list head while the remaining error is above the bound
+        const int n0 = n;
+        double ee_err = S.tot_err;
+        const double ee_val = S.tot_val;
+        int K = 0;
+        for (int b0 = 0;; b0 += kChiScan) {
+            const int nb = min(kChiScan, m - b0);
+            for (int t = tid; t < nb; t += kChiThreads) {
+                const int q = R.idx[cur][b0 + t];
+                S.scan.e[t] = R.err[q];
+                S.scan.v[t] = R.val[q];
+            }
+            __syncthreads();
+            if (tid == 0) {
+                int done = 0;
+                double tv = S.tot_val, te = S.tot_err;
+                long long ne = S.numeval;
+                for (int t = 0; t < nb; ++t) {
+                    if (n0 + K + 1 > cap) {
+                        S.over = 1;
+                        done = 1;
+                        break;
+                    }
+                    tv -= S.scan.v[t];
+                    te -= S.scan.e[t];
+                    ee_err -= S.scan.e[t];
+                    ++K;
+                    ne += 34;
+                    if (converged(ee_err, ee_val) || K >= m || ne >= maxevals) {
+                        done = 1;
+                        break;
+                    }
+                }
+                S.tot_val = tv;
+                S.tot_err = te;
+                S.numeval = ne;
+                S.K = K;
+                S.done = done;
+            }
+            __syncthreads();
+            if (S.done) break;
+        }
+        K = S.K;
+        if (S.over) break;
+        // 2. cut: the first half keeps the index, the second half is region n0 + j
+        for (int j = tid; j < K; j += kChiThreads) {
+            const int bi = R.idx[cur][j], q = n0 + j;
+            const int d = R.split[bi];
+            double c0 = R.c0[bi], c1 = R.c1[bi], h0 = R.h0[bi], h1 = R.h1[bi];
+            double cq0 = c0, cq1 = c1;
+            if (d == 0) {
+                h0 *= 0.5;
+                c0 -= h0;
+                cq0 += h0;
+            } else {
+                h1 *= 0.5;
+                c1 -= h1;
+                cq1 += h1;
+            }
+            R.c0[bi] = c0;
+            R.c1[bi] = c1;
+            R.h0[bi] = h0;
+            R.h1[bi] = h1;
+            R.vol[bi] *= 0.5;
+            R.c0[q] = cq0;
+            R.c1[q] = cq1;
+            R.h0[q] = h0;
+            R.h1[q] = h1;
+            R.vol[q] = (2.0 * h0) * (2.0 * h1);
+        }
+        __syncthreads();
+        // 3. evaluate the halves in cut order (j's first half, j's second half, ...) into list b1
+        const int b1 = (cur + 1) % 3, b2 = (cur + 2) % 3;
+        const int* head = R.idx[cur];
+        auto cut = [head, n0](int e) { return (e & 1) ? n0 + (e >> 1) : head[e >> 1]; };
+        unsigned long long* nk = R.key[b1];
+        int* ni = R.idx[b1];
+        chi_eval_block(f, R, cut, 2 * K, S, [&](int e, int r, double err) {
+            nk[e] = err_key(err);
+            ni[e] = r;
+        });
+        // 4. the new regions join the totals in cut order
+        for (int b0 = 0; b0 < 2 * K; b0 += kChiScan) {
+            const int nb = min(kChiScan, 2 * K - b0);
+            for (int t = tid; t < nb; t += kChiThreads) {
+                const int r = cut(b0 + t);
+                S.scan.e[t] = R.err[r];
+                S.scan.v[t] = R.val[r];
+            }
+            __syncthreads();
+            if (tid == 0) {
+                double tv = S.tot_val, te = S.tot_err;
+                for (int t = 0; t < nb; ++t) {
+                    tv += S.scan.v[t];
+                    te += S.scan.e[t];
+                }
+                S.tot_val = tv;
+                S.tot_err = te;
+            }
+            __syncthreads();
+        }
+        // 5. sort them and merge them after equal errors of the rest of the list
+        const int in_b2 = block_radix_sort(nk, ni, R.key[b2], R.idx[b2], 2 * K, S);
+        const int bs = in_b2 ? b2 : b1, bo = in_b2 ? b1 : b2;
+        block_merge(R.key[cur] + K, R.idx[cur] + K, m - K, R.key[bs], R.idx[bs], 2 * K, R.key[bo], R.idx[bo]);
+        cur = bo;
+        m += K;
+        n = n0 + K;
+    }
+    // the total: kChiSumBlocks consecutive blocks of regions, each summed in index order
+    const int over = S.over;
+    __syncthreads();
+    static_assert(kChiSumBlocks == kChiThreads, "one block of the sum per thread");
+    {
+        const int c = (n + kChiSumBlocks - 1) / kChiSumBlocks;
+        const int q0 = min(n, tid * c), q1 = min(n, q0 + c);
+        double p = 0.0;
+        for (int q = q0; q < q1; ++q) p += R.val[q];
+        S.f[tid] = p;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double I = 0.0;
+        for (int t = 0; t < kChiSumBlocks; ++t) I += S.f[t];
         A.box_out[job] = I;
-        overflow[slot] = over ? 1 : 0;
+        overflow[slot] = over;
         if (A.evals && !over) {
-            atomicAdd(A.evals, (unsigned long long)numeval);
+            atomicAdd(A.evals, (unsigned long long)S.numeval);
             atomicMax(A.evals + 1, (unsigned long long)n);
             atomicAdd(A.evals + 2, (unsigned long long)rounds);
             atomicMax(A.evals + 3, (unsigned long long)rounds);
@@ -790,11 +941,10 @@ __global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
 
 template <typename R>
 static cudaError_t launch_chi_boxes_r(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st) {
-    const size_t smem = sizeof(SMesh<R>) + sizeof(double) * kChiWarps * kChiPend * 17 + sizeof(int) * kChiWarps * kChiPend;
+    const size_t smem = sizeof(SMesh<R>) + sizeof(ChiScratch);
     cudaError_t e = cudaFuncSetAttribute(chi_box_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    chi_box_kernel<R><<<(unsigned)((njobs + kChiWarps - 1) / kChiWarps), kChiWarps * 32, smem, st>>>(a, jobs, njobs,
-                                                                                                      overflow);
+    chi_box_kernel<R><<<(unsigned)njobs, kChiThreads, smem, st>>>(a, jobs, njobs, overflow);
     return cudaGetLastError();
 }
 
