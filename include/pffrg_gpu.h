@@ -166,6 +166,14 @@ int pffrg_resample(pffrg_ctx* ctx, int src_slot, int dst_slot, const pffrg_mesh_
  * level).  Both give identical results.  No counterpart in the reference. */
 int pffrg_set_async_waves(pffrg_ctx* ctx, int on);
 
+/* Team shape of the quadrature passes: `lanes` threads share a batch of nodes
+ * and each holds `sites_per_lane` sites (built: 8x1, 16x1, 16x3, 16x4, 32x1,
+ * 32x2, 32x4, 32x8; 0x0 = chosen from the number of sites).  A shape that
+ * does not cover the sites is ignored.  Results agree to rounding (the
+ * t-channel overlap sums are split over the lanes differently).  No
+ * counterpart in the reference. */
+int pffrg_set_team_shape(pffrg_ctx* ctx, int lanes, int sites_per_lane);
+
 /* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86,
  * correlation_u1_dm.jl:152-190): static spin correlations χ[i, w] of the
  * action `a` at Λ on the frequencies chi_mesh[0..num_chi), written

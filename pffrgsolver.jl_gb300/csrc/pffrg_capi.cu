@@ -57,6 +57,7 @@ struct pffrg_ctx {
     long long gk_cap = 0, gk_slots = 0;
     int gk_overflow = 0;
     int async_waves = 1;  // device-driven quadrature levels (no host round trip per level)
+    int team_T = 0, team_SPL = 0;  // requested team shape of the passes (0: chosen by Ns)
     int64_t chi_evals = 0, chi_regions_max = 0, chi_rounds = 0, chi_rounds_max = 0;
     // wave workspace of the passes (device scratch) and its host-visible counters
     void* wave_mem = nullptr;
@@ -83,6 +84,7 @@ struct pffrg_ctx {
     size_t chi_reg_bytes = 0;
     int* chi_jobs = nullptr;  // job list of a cubature launch
     int* chi_over = nullptr;  // per-job overflow flags
+    int* chi_ctl = nullptr;   // per-job round orders of a cluster
     double* chi_box = nullptr;
     double* chi_out = nullptr;
     double* chi_mesh = nullptr;
@@ -332,6 +334,8 @@ PassArgs<R> base_pass(pffrg_ctx* ctx, double Lam, int eval, double atol, double 
     p.chan_of_y[2] = 2;
     p.node_counter = ctx->counter;
     p.async_waves = ctx->async_waves;
+    p.team_T = ctx->team_T;
+    p.team_SPL = ctx->team_SPL;
     p.status = ctx->status;
     return p;
 }
@@ -485,7 +489,7 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
             CK(stream_free(ctx->st, *p));
             *p = nullptr;
         }
-        for (int** p : {&ctx->chi_jobs, &ctx->chi_over}) {
+        for (int** p : {&ctx->chi_jobs, &ctx->chi_over, &ctx->chi_ctl}) {
             CK(stream_free(ctx->st, *p));
             *p = nullptr;
         }
@@ -494,6 +498,7 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
         CK(cudaMalloc(&ctx->chi_out, sizeof(double) * 3 * (size_t)Ns * num_chi));
         CK(cudaMalloc(&ctx->chi_jobs, sizeof(int) * 9 * 3 * (size_t)Ns * num_chi));
         CK(cudaMalloc(&ctx->chi_over, sizeof(int) * 9 * 3 * (size_t)Ns * num_chi));
+        CK(cudaMalloc(&ctx->chi_ctl, sizeof(int) * 4 * 9 * 3 * (size_t)Ns * num_chi));
         ctx->chi_n = num_chi;
     }
     CK(cudaMemcpyAsync(ctx->chi_mesh, chi_mesh, sizeof(double) * num_chi, cudaMemcpyHostToDevice, ctx->st));
@@ -542,13 +547,16 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
         }
         c.reg = ctx->chi_reg;
         c.reg_split = ctx->chi_split;
+        c.ctl = ctx->chi_ctl;
         c.cap = cap;
         std::vector<int> next;
         for (size_t s = 0; s < todo.size(); s += (size_t)batch) {
             const int nb = (int)std::min<size_t>((size_t)batch, todo.size() - s);
             CK(cudaMemcpyAsync(ctx->chi_jobs, todo.data() + s, sizeof(int) * nb, cudaMemcpyHostToDevice, ctx->st));
             ++ctx->launches;
-            CK(launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, ctx->st));
+            // the integrals that outgrew the first capacities are few and long: a cluster of
+            // blocks evaluates each round's regions of one integral
+            CK(launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, cap >= 32768 ? 8 : 1, ctx->st));
             over.resize(nb);
             CK(cudaMemcpyAsync(over.data(), ctx->chi_over, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->st));
             CK(cudaStreamSynchronize(ctx->st));
@@ -558,7 +566,8 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
         todo.swap(next);
         if (!todo.empty()) {
             if (cap >= cap_max) return ctx->fail(PFFRG_E_LIMIT, "cubature of χ needs more than %lld regions", cap_max);
-            cap = std::min(cap * 8, cap_max);
+            // a job that outgrows 8x would restart close to the cap: take the cap at once
+            cap = cap * 64 > cap_max ? cap_max : cap * 8;
         }
     }
     for (;;) {
@@ -791,7 +800,7 @@ void pffrg_destroy(pffrg_ctx* ctx) {
                     ctx->mesh, ctx->log_bounds, ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig, ctx->sig_tmp, ctx->f_a, ctx->f_da,
                     ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
                     ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red, ctx->chi_reg, ctx->chi_split,
-                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over, ctx->gk_seg,
+                    ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over, ctx->chi_ctl, ctx->gk_seg,
                     ctx->mesh_new, ctx->scan_arg, ctx->scan_cuts};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -1267,6 +1276,18 @@ int pffrg_set_async_waves(pffrg_ctx* ctx, int on) {
     if (!ctx) return PFFRG_E_ARGS;
     ctx->async_waves = on ? 1 : 0;
     return 0;
+}
+
+int pffrg_set_team_shape(pffrg_ctx* ctx, int lanes, int sites_per_lane) {
+    if (!ctx) return PFFRG_E_ARGS;
+    static const int shapes[][2] = {{0, 0}, {8, 1}, {16, 1}, {16, 3}, {16, 4}, {32, 1}, {32, 2}, {32, 4}, {32, 8}};
+    for (const auto& sh : shapes)
+        if (sh[0] == lanes && sh[1] == sites_per_lane) {
+            ctx->team_T = lanes;
+            ctx->team_SPL = sites_per_lane;
+            return 0;
+        }
+    return ctx->fail(PFFRG_E_ARGS, "team shape %dx%d is not built", lanes, sites_per_lane);
 }
 
 void* pffrg_host_alloc(int64_t bytes) {

@@ -1136,6 +1136,18 @@ cudaError_t launch_pass_impl(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counte
     const int Ns = a.L.Ns;
     if (a.ntasks == 0) return cudaSuccess;
     const int cap = 152 * 32;
+    // a requested team shape that covers the sites
+    if (a.team_T > 0 && a.team_T * a.team_SPL >= Ns) {
+        const int T = a.team_T, S = a.team_SPL;
+        if (T == 8 && S == 1) return PassLauncher<R, C>::template run<8, 1>(a, Wsp, h_counters, st, cap);
+        if (T == 16 && S == 1) return PassLauncher<R, C>::template run<16, 1>(a, Wsp, h_counters, st, cap);
+        if (T == 16 && S == 3) return PassLauncher<R, C>::template run<16, 3>(a, Wsp, h_counters, st, cap);
+        if (T == 16 && S == 4) return PassLauncher<R, C>::template run<16, 4>(a, Wsp, h_counters, st, cap);
+        if (T == 32 && S == 1) return PassLauncher<R, C>::template run<32, 1>(a, Wsp, h_counters, st, cap);
+        if (T == 32 && S == 2) return PassLauncher<R, C>::template run<32, 2>(a, Wsp, h_counters, st, cap);
+        if (T == 32 && S == 4) return PassLauncher<R, C>::template run<32, 4>(a, Wsp, h_counters, st, cap);
+        if (T == 32 && S == 8) return PassLauncher<R, C>::template run<32, 8>(a, Wsp, h_counters, st, cap);
+    }
     if (Ns <= 8) return PassLauncher<R, C>::template run<8, 1>(a, Wsp, h_counters, st, cap);
     if (Ns <= 16) return PassLauncher<R, C>::template run<16, 1>(a, Wsp, h_counters, st, cap);
     if (Ns <= 32) return PassLauncher<R, C>::template run<32, 1>(a, Wsp, h_counters, st, cap);

@@ -48,6 +48,7 @@ struct PassArgs {
     double twoS;
     int reduced;          // reduced s bubble of the SDE (U(1)-DM keeps xx, zz, dd only)
     int async_waves;      // levels without host round trips; overflow reported in *status (bit 3)
+    int team_T, team_SPL; // team shape (lanes per node batch, sites per lane); 0: chosen by Ns
     int* status;
     unsigned long long* node_counter;  // optional: [0] integrand evaluations, [1] algorithmic values read
 };
@@ -174,6 +175,7 @@ struct ChiArgs {
     double* reg;             // [job slot][10][cap] region records (7) and the keys of three region lists
     int* reg_split;          // [job slot][4][cap] split dimensions and the entries of three region lists
     long long cap;           // regions per integral
+    int* ctl;                // [job slot][4] a round's orders from a cluster's block 0 to the others
     double* box_out;         // [ncomp][num_chi][Ns][9]
     double* chi;             // [ncomp][Ns][num_chi], each column-major
     unsigned long long* evals;  // [0] cubature points, [1] largest region count, [2] rounds, [3] most rounds
@@ -181,8 +183,10 @@ struct ChiArgs {
     long long seg_cap;
     int* status;             // bit 1: GK segments exhausted
 };
-// the box integrals of the listed jobs (overflow[slot] = 1: region capacity exhausted)
-cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st);
+// the box integrals of the listed jobs (overflow[slot] = 1: region capacity exhausted), one block
+// per integral, or a cluster of blocks per integral (cluster > 1)
+cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, int cluster,
+                             cudaStream_t st);
 // the local term and the sums of the boxes into χ
 cudaError_t launch_chi_sum(const ChiArgs& a, cudaStream_t st);
 

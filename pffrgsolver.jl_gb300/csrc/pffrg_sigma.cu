@@ -403,6 +403,7 @@ constexpr int kChiChunk = 128;     // regions whose 17 points are evaluated per 
 constexpr int kChiScan = 1024;     // list entries staged per step of the sequential sums
 constexpr int kChiSumBlocks = 256; // blocks of the final sum (the oracle sums the same blocks)
 constexpr int kSortItems = 8;      // list entries per thread and tile of the radix sort
+constexpr int kChiCluster = 8;     // blocks per integral of the large-capacity passes
 
 // shared scratch of one integral; the phases of a round use it in turn
 struct ChiScratch {
@@ -428,7 +429,8 @@ __device__ __forceinline__ unsigned long long err_key(double e) {
     return ~(unsigned long long)__double_as_longlong(e);  // e >= 0: bits ascending with e
 }
 
-// Stable LSD radix sort (8-bit digits) of cnt >= 1 (key, index) pairs by the block, from
+// Stable LSD radix sort (8-bit digits) of cnt >= 1 (key, index) pairs by the block (entries
+// read through L2: other blocks of a cluster may have written them), from
 // (k0, i0) with (k1, i1) as scratch; digits shared by every key are skipped.  Returns the
 // buffer that holds the result (0: k0/i0, 1: k1/i1).
 __device__ int block_radix_sort(unsigned long long* k0, int* i0, unsigned long long* k1, int* i1, int cnt,
@@ -438,7 +440,7 @@ __device__ int block_radix_sort(unsigned long long* k0, int* i0, unsigned long l
     for (int q = tid; q < 8 * 256; q += kChiThreads) (&S.sort.hist[0][0])[q] = 0u;
     __syncthreads();
     for (int e = tid; e < cnt; e += kChiThreads) {
-        const unsigned long long k = k0[e];
+        const unsigned long long k = __ldcg(k0 + e);
 #pragma unroll
         for (int d = 0; d < 8; ++d) atomicAdd(&S.sort.hist[d][(unsigned)(k >> (8 * d)) & 255u], 1u);
     }
@@ -449,7 +451,7 @@ __device__ int block_radix_sort(unsigned long long* k0, int* i0, unsigned long l
         int* is = cur ? i1 : i0;
         unsigned long long* kd = cur ? k0 : k1;
         int* id = cur ? i0 : i1;
-        if (S.sort.hist[d][(unsigned)(ks[0] >> (8 * d)) & 255u] == (unsigned)cnt) continue;
+        if (S.sort.hist[d][(unsigned)(__ldcg(ks) >> (8 * d)) & 255u] == (unsigned)cnt) continue;
         {  // exclusive prefix of the digit counts
             const unsigned x = S.sort.hist[d][tid];
             unsigned inc = x;
@@ -476,8 +478,8 @@ __device__ int block_radix_sort(unsigned long long* k0, int* i0, unsigned long l
             for (int s = 0; s < kSortItems; ++s) {
                 const int e = t0 + (warp * kSortItems + s) * 32 + lane;
                 const bool ok = e < cnt;
-                kk[s] = ok ? ks[e] : 0ull;
-                ii[s] = ok ? is[e] : 0;
+                kk[s] = ok ? __ldcg(ks + e) : 0ull;
+                ii[s] = ok ? __ldcg(is + e) : 0;
                 dg[s] = ok ? ((unsigned)(kk[s] >> (8 * d)) & 255u) : 256u + (unsigned)lane;
                 const unsigned peers = __match_any_sync(0xffffffffu, dg[s]);
                 rk[s] = ok ? cw[dg[s]] + (unsigned)__popc(peers & lt) : 0u;
@@ -512,7 +514,7 @@ __device__ int block_radix_sort(unsigned long long* k0, int* i0, unsigned long l
     return cur;
 }
 
-// merge the sorted lists a[0, na) and b[0, nb) into o; equal keys: a's first
+// merge the sorted lists a[0, na) and b[0, nb) into o; equal keys: a's first (reads through L2)
 __device__ void block_merge(const unsigned long long* ak, const int* ai, int na, const unsigned long long* bk,
                             const int* bi, int nb, unsigned long long* ok, int* oi) {
     const int n = na + nb;
@@ -522,18 +524,18 @@ __device__ void block_merge(const unsigned long long* ak, const int* ai, int na,
         int lo = max(0, d0 - nb), hi = min(d0, na);
         while (lo < hi) {
             const int mid = (lo + hi) >> 1;
-            if (ak[mid] <= bk[d0 - 1 - mid]) lo = mid + 1;
+            if (__ldcg(ak + mid) <= __ldcg(bk + d0 - 1 - mid)) lo = mid + 1;
             else hi = mid;
         }
         int i = lo, j = d0 - lo;
         for (int d = d0; d < d1; ++d) {
-            if (j >= nb || (i < na && ak[i] <= bk[j])) {
-                ok[d] = ak[i];
-                oi[d] = ai[i];
+            if (j >= nb || (i < na && __ldcg(ak + i) <= __ldcg(bk + j))) {
+                ok[d] = __ldcg(ak + i);
+                oi[d] = __ldcg(ai + i);
                 ++i;
             } else {
-                ok[d] = bk[j];
-                oi[d] = bi[j];
+                ok[d] = __ldcg(bk + j);
+                oi[d] = __ldcg(bi + j);
                 ++j;
             }
         }
@@ -655,18 +657,20 @@ struct ChiKernel {
     }
 };
 
-// evaluate regions reg(0 .. count) of one integral with the block: the 17 points of
-// kChiChunk regions at a time, then each region's rule; emit(e, r, err) sees every result
+// evaluate regions reg(e) of one integral, e in [0, count), the block taking every CL-th
+// chunk of kChiChunk regions from chunk `first`: the 17 points of a chunk over all threads,
+// then each region's rule; emit(e, r, err) sees every result.  Region records are read
+// through L2 (other blocks of the cluster write them).
 template <class F, class Reg, class Emit>
-__device__ void chi_eval_block(const F& f, const ChiRegions& R, const Reg& reg, int count, ChiScratch& S,
-                               const Emit& emit) {
+__device__ void chi_eval_block(const F& f, const ChiRegions& R, const Reg& reg, int count, int first, int stride,
+                               ChiScratch& S, const Emit& emit) {
     const int tid = threadIdx.x;
-    for (int cb = 0; cb < count; cb += kChiChunk) {
+    for (int cb = first * kChiChunk; cb < count; cb += stride * kChiChunk) {
         const int cnt = min(kChiChunk, count - cb);
         for (int p = tid; p < cnt * 17; p += kChiThreads) {
             const int r = reg(cb + p / 17);
             double x, y;
-            gm_point(p % 17, R.c0[r], R.c1[r], R.h0[r], R.h1[r], x, y);
+            gm_point(p % 17, __ldcg(R.c0 + r), __ldcg(R.c1 + r), __ldcg(R.h0 + r), __ldcg(R.h1 + r), x, y);
             S.f[p] = f(x, y);
         }
         __syncthreads();
@@ -674,7 +678,7 @@ __device__ void chi_eval_block(const F& f, const ChiRegions& R, const Reg& reg, 
             const int r = reg(cb + q);
             double val, err;
             int sp;
-            gm_rule(S.f + 17 * q, R.vol[r], val, err, sp);
+            gm_rule(S.f + 17 * q, __ldcg(R.vol + r), val, err, sp);
             R.val[r] = val;
             R.err[r] = err;
             R.split[r] = sp;
@@ -684,13 +688,18 @@ __device__ void chi_eval_block(const F& f, const ChiRegions& R, const Reg& reg, 
     }
 }
 
-// One block per (ω, site, component, box) integral of the job list.  A round takes
-// the head of the sorted list (the library's pop order) while the remaining error
-// is above the bound, cuts those regions, evaluates the halves with the whole block,
-// adds them in cut order, sorts them and merges them into the rest of the list.  A
-// job that runs out of region capacity raises its overflow flag and is run again
-// with a larger capacity.
-template <typename RT>
+// all threads of the cluster; writes before it are seen by every block of the cluster after it
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// One integral of the job list per cluster of CL blocks (CL = 1: a single block).  A round
+// takes the head of the sorted list (the library's pop order) while the remaining error is
+// above the bound, cuts those regions, evaluates the halves with all blocks of the cluster,
+// adds them in cut order, sorts them and merges them into the rest of the list.  Block 0 of
+// the cluster keeps the list and the totals; the others only evaluate.  A job that runs out
+// of region capacity raises its overflow flag and is run again with a larger capacity.
+template <typename RT, int CL>
 __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, const int* __restrict__ jobs,
                                                                    int njobs, int* overflow) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -698,8 +707,9 @@ __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, cons
     ChiScratch& S = *reinterpret_cast<ChiScratch*>(smem_raw + sizeof(SMesh<RT>));
     load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     const int tid = threadIdx.x;
-    const long long slot = blockIdx.x;
-    if (slot >= njobs) return;
+    const long long slot = blockIdx.x / CL;
+    const int rank = (int)(blockIdx.x % CL);  // the cluster's blocks are consecutive in x
+    const bool lead = rank == 0;
     const long long job = jobs[slot];
     // job = ((ω index * Ns + site) * ncomp + component) * 9 + box
     const int box = (int)(job % 9);
@@ -731,11 +741,12 @@ __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, cons
             R.idx[b] = i + (1 + b) * cap;
         }
     }
+    int* ctl = A.ctl + slot * 4;  // the round's orders to the cluster: stop, K, first new region, list
     const RT* state;
     if constexpr (sizeof(RT) == 8) state = A.a;
     else state = A.af;
     ChiKernel<RT> f{A, M, state, site, k, wv};
-    if (tid == 0) {
+    if (lead && tid == 0) {
         R.c0[0] = 0.5 * (lo[col] + hi[col]);
         R.c1[0] = 0.5 * (lo[row] + hi[row]);
         R.h0[0] = 0.5 * (hi[col] - lo[col]);
@@ -744,112 +755,136 @@ __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, cons
     }
     __syncthreads();  // the mesh and region 0
     int cur = 0;
-    chi_eval_block(f, R, [](int) { return 0; }, 1, S, [&](int, int r, double e) {
-        R.key[cur][0] = err_key(e);
-        R.idx[cur][0] = r;
-    });
-    // the control state lives in S and is written by thread 0 between barriers
-    int n = 1, m = 1;
+    int n = 1, m = 1;  // regions; list length (every region is on the list between rounds)
     long long rounds = 0;
-    if (tid == 0) {
-        S.tot_val = R.val[0];
-        S.tot_err = R.err[0];
-        S.numeval = 17;
-        S.over = 0;
-    }
-    __syncthreads();
     const long long maxevals = 10000000;
     auto converged = [&](double err, double val) { return !(err > A.atol && err > fabs(val) * A.rtol); };
-    while (S.numeval < maxevals && !converged(S.tot_err, S.tot_val)) {
-        ++rounds;
-        // 1. the pops: list head while the remaining error is above the bound
-        const int n0 = n;
-        double ee_err = S.tot_err;
-        const double ee_val = S.tot_val;
-        int K = 0;
-        for (int b0 = 0;; b0 += kChiScan) {
-            const int nb = min(kChiScan, m - b0);
-            for (int t = tid; t < nb; t += kChiThreads) {
-                const int q = R.idx[cur][b0 + t];
-                S.scan.e[t] = R.err[q];
-                S.scan.v[t] = R.val[q];
-            }
-            __syncthreads();
-            if (tid == 0) {
-                int done = 0;
-                double tv = S.tot_val, te = S.tot_err;
-                long long ne = S.numeval;
-                for (int t = 0; t < nb; ++t) {
-                    if (n0 + K + 1 > cap) {
-                        S.over = 1;
-                        done = 1;
-                        break;
-                    }
-                    tv -= S.scan.v[t];
-                    te -= S.scan.e[t];
-                    ee_err -= S.scan.e[t];
-                    ++K;
-                    ne += 34;
-                    if (converged(ee_err, ee_val) || K >= m || ne >= maxevals) {
-                        done = 1;
-                        break;
-                    }
-                }
-                S.tot_val = tv;
-                S.tot_err = te;
-                S.numeval = ne;
-                S.K = K;
-                S.done = done;
-            }
-            __syncthreads();
-            if (S.done) break;
-        }
-        K = S.K;
-        if (S.over) break;
-        // 2. cut: the first half keeps the index, the second half is region n0 + j
-        for (int j = tid; j < K; j += kChiThreads) {
-            const int bi = R.idx[cur][j], q = n0 + j;
-            const int d = R.split[bi];
-            double c0 = R.c0[bi], c1 = R.c1[bi], h0 = R.h0[bi], h1 = R.h1[bi];
-            double cq0 = c0, cq1 = c1;
-            if (d == 0) {
-                h0 *= 0.5;
-                c0 -= h0;
-                cq0 += h0;
-            } else {
-                h1 *= 0.5;
-                c1 -= h1;
-                cq1 += h1;
-            }
-            R.c0[bi] = c0;
-            R.c1[bi] = c1;
-            R.h0[bi] = h0;
-            R.h1[bi] = h1;
-            R.vol[bi] *= 0.5;
-            R.c0[q] = cq0;
-            R.c1[q] = cq1;
-            R.h0[q] = h0;
-            R.h1[q] = h1;
-            R.vol[q] = (2.0 * h0) * (2.0 * h1);
+    if (lead) {
+        chi_eval_block(f, R, [](int) { return 0; }, 1, 0, 1, S, [&](int, int r, double e) {
+            R.key[cur][0] = err_key(e);
+            R.idx[cur][0] = r;
+        });
+        if (tid == 0) {
+            S.tot_val = __ldcg(R.val);
+            S.tot_err = __ldcg(R.err);
+            S.numeval = 17;
+            S.over = 0;
         }
         __syncthreads();
+    }
+    for (;;) {
+        int stop = 0, K = 0, n0 = n;
+        if (lead) {
+            stop = S.numeval >= maxevals || converged(S.tot_err, S.tot_val);
+            if (!stop) {
+                ++rounds;
+                // 1. the pops: list head while the remaining error is above the bound
+                double ee_err = S.tot_err;
+                const double ee_val = S.tot_val;
+                for (int b0 = 0;; b0 += kChiScan) {
+                    const int nb = min(kChiScan, m - b0);
+                    for (int t = tid; t < nb; t += kChiThreads) {
+                        const int q = R.idx[cur][b0 + t];
+                        S.scan.e[t] = __ldcg(R.err + q);
+                        S.scan.v[t] = __ldcg(R.val + q);
+                    }
+                    __syncthreads();
+                    if (tid == 0) {
+                        int done = 0;
+                        double tv = S.tot_val, te = S.tot_err;
+                        long long ne = S.numeval;
+                        for (int t = 0; t < nb; ++t) {
+                            if (n0 + K + 1 > cap) {
+                                S.over = 1;
+                                done = 1;
+                                break;
+                            }
+                            tv -= S.scan.v[t];
+                            te -= S.scan.e[t];
+                            ee_err -= S.scan.e[t];
+                            ++K;
+                            ne += 34;
+                            if (converged(ee_err, ee_val) || K >= m || ne >= maxevals) {
+                                done = 1;
+                                break;
+                            }
+                        }
+                        S.tot_val = tv;
+                        S.tot_err = te;
+                        S.numeval = ne;
+                        S.K = K;
+                        S.done = done;
+                    }
+                    __syncthreads();
+                    if (S.done) break;
+                }
+                K = S.K;
+                stop = S.over;
+            }
+            if (!stop) {
+                // 2. cut: the first half keeps the index, the second half is region n0 + j
+                for (int j = tid; j < K; j += kChiThreads) {
+                    const int bi = R.idx[cur][j], q = n0 + j;
+                    const int d = __ldcg(R.split + bi);
+                    double c0 = R.c0[bi], c1 = R.c1[bi], h0 = R.h0[bi], h1 = R.h1[bi];
+                    double cq0 = c0, cq1 = c1;
+                    if (d == 0) {
+                        h0 *= 0.5;
+                        c0 -= h0;
+                        cq0 += h0;
+                    } else {
+                        h1 *= 0.5;
+                        c1 -= h1;
+                        cq1 += h1;
+                    }
+                    R.c0[bi] = c0;
+                    R.c1[bi] = c1;
+                    R.h0[bi] = h0;
+                    R.h1[bi] = h1;
+                    R.vol[bi] *= 0.5;
+                    R.c0[q] = cq0;
+                    R.c1[q] = cq1;
+                    R.h0[q] = h0;
+                    R.h1[q] = h1;
+                    R.vol[q] = (2.0 * h0) * (2.0 * h1);
+                }
+            }
+            if (CL > 1 && tid == 0) {
+                ctl[0] = stop;
+                ctl[1] = K;
+                ctl[2] = n0;
+                ctl[3] = cur;
+            }
+        }
+        if constexpr (CL > 1) {
+            cluster_barrier();
+            stop = __ldcg(ctl);
+            K = __ldcg(ctl + 1);
+            n0 = __ldcg(ctl + 2);
+            cur = __ldcg(ctl + 3);
+        } else {
+            __syncthreads();
+        }
+        if (stop) break;
         // 3. evaluate the halves in cut order (j's first half, j's second half, ...) into list b1
         const int b1 = (cur + 1) % 3, b2 = (cur + 2) % 3;
         const int* head = R.idx[cur];
-        auto cut = [head, n0](int e) { return (e & 1) ? n0 + (e >> 1) : head[e >> 1]; };
+        auto cut = [head, n0](int e) { return (e & 1) ? n0 + (e >> 1) : __ldcg(head + (e >> 1)); };
         unsigned long long* nk = R.key[b1];
         int* ni = R.idx[b1];
-        chi_eval_block(f, R, cut, 2 * K, S, [&](int e, int r, double err) {
+        chi_eval_block(f, R, cut, 2 * K, rank, CL, S, [&](int e, int r, double err) {
             nk[e] = err_key(err);
             ni[e] = r;
         });
+        if constexpr (CL > 1) cluster_barrier();
+        if (!lead) continue;
         // 4. the new regions join the totals in cut order
         for (int b0 = 0; b0 < 2 * K; b0 += kChiScan) {
             const int nb = min(kChiScan, 2 * K - b0);
             for (int t = tid; t < nb; t += kChiThreads) {
                 const int r = cut(b0 + t);
-                S.scan.e[t] = R.err[r];
-                S.scan.v[t] = R.val[r];
+                S.scan.e[t] = __ldcg(R.err + r);
+                S.scan.v[t] = __ldcg(R.val + r);
             }
             __syncthreads();
             if (tid == 0) {
@@ -871,6 +906,7 @@ __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, cons
         m += K;
         n = n0 + K;
     }
+    if (!lead) return;
     // the total: kChiSumBlocks consecutive blocks of regions, each summed in index order
     const int over = S.over;
     __syncthreads();
@@ -879,7 +915,7 @@ __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, cons
         const int c = (n + kChiSumBlocks - 1) / kChiSumBlocks;
         const int q0 = min(n, tid * c), q1 = min(n, q0 + c);
         double p = 0.0;
-        for (int q = q0; q < q1; ++q) p += R.val[q];
+        for (int q = q0; q < q1; ++q) p += __ldcg(R.val + q);
         S.f[tid] = p;
     }
     __syncthreads();
@@ -939,18 +975,34 @@ __global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
     }
 }
 
-template <typename R>
+template <typename R, int CL>
 static cudaError_t launch_chi_boxes_r(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st) {
     const size_t smem = sizeof(SMesh<R>) + sizeof(ChiScratch);
-    cudaError_t e = cudaFuncSetAttribute(chi_box_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = chi_box_kernel<R, CL>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    chi_box_kernel<R><<<(unsigned)njobs, kChiThreads, smem, st>>>(a, jobs, njobs, overflow);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)njobs * CL);
+    cfg.blockDim = dim3(kChiThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a, jobs, njobs, overflow);
 }
 
-cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st) {
-    return a.af ? launch_chi_boxes_r<float>(a, jobs, njobs, overflow, st)
-                : launch_chi_boxes_r<double>(a, jobs, njobs, overflow, st);
+cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, int cluster,
+                             cudaStream_t st) {
+    if (cluster > 1)
+        return a.af ? launch_chi_boxes_r<float, kChiCluster>(a, jobs, njobs, overflow, st)
+                    : launch_chi_boxes_r<double, kChiCluster>(a, jobs, njobs, overflow, st);
+    return a.af ? launch_chi_boxes_r<float, 1>(a, jobs, njobs, overflow, st)
+                : launch_chi_boxes_r<double, 1>(a, jobs, njobs, overflow, st);
 }
 
 cudaError_t launch_chi_sum(const ChiArgs& a, cudaStream_t st) {

@@ -152,6 +152,11 @@ class FlowContext:
         """Device-driven quadrature levels (default) or the host-driven loop; same results."""
         self._check(self.lib.pffrg_set_async_waves(self.h, int(bool(on))), "set_async_waves")
 
+    def set_team_shape(self, lanes: int = 0, sites_per_lane: int = 0) -> None:
+        """Team shape of the quadrature passes (lanes x sites per lane; 0, 0: chosen from the
+        number of sites).  Results agree to rounding."""
+        self._check(self.lib.pffrg_set_team_shape(self.h, int(lanes), int(sites_per_lane)), "set_team_shape")
+
     # ---- device-resident interface ----
     def upload(self, slot: int, a: Action) -> None:
         v = _capi.action_view(a)
