@@ -10,8 +10,13 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 OUT_DIR = HERE / "_build"
 LIB = OUT_DIR / "libpffrg_gpu.so"
-SOURCES = ["pffrg_flow_f64.cu", "pffrg_flow_f32.cu", "pffrg_flow_u1dm_f64.cu", "pffrg_flow_u1dm_f32.cu",
-           "pffrg_sigma.cu", "pffrg_state.cu", "pffrg_capi.cu", "pffrg_noalloc.cu", "pffrg_mlp.cu"]
+# (source, object, defines): the pass kernels are compiled once per precision, component count and
+# group of team shapes so that the longest objects build in parallel
+SOURCES = [(s, s + ".o", []) for s in ["pffrg_passes.cu", "pffrg_sigma.cu", "pffrg_state.cu", "pffrg_capi.cu",
+                                       "pffrg_noalloc.cu", "pffrg_mlp.cu"]]
+SOURCES += [("pffrg_shapes.cu", f"pffrg_shapes_{r}_c{c}_g{g}.o",
+             [f"-DPFFRG_R={r}", f"-DPFFRG_C={c}", f"-DPFFRG_GROUP={g}"])
+            for r in ("double", "float") for c in (2, 6) for g in (0, 1, 2)]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -29,15 +34,15 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     OUT_DIR.mkdir(parents=True, exist_ok=True)
     procs = []
     objs = []
-    for s in SOURCES:
+    for s, o, defs in SOURCES:
         src = CSRC / s
-        obj = OUT_DIR / (s + ".o")
+        obj = OUT_DIR / o
         objs.append(obj)
         if force or _stale(obj, src):
-            cmd = [NVCC, *ARCH, *FLAGS, "-c", str(src), "-o", str(obj)]
+            cmd = [NVCC, *ARCH, *FLAGS, *defs, "-c", str(src), "-o", str(obj)]
             if verbose:
                 print(" ".join(cmd), flush=True)
-            procs.append((s, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+            procs.append((o, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     failed = []
     for s, p in procs:
         out, _ = p.communicate()

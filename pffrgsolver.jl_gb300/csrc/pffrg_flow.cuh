@@ -1131,29 +1131,41 @@ struct PassLauncher {
     }
 };
 
+// one team shape of one precision and component count; instantiated explicitly in
+// pffrg_shapes.cu (one object per group of shapes, so the kernels compile in parallel)
+template <typename R, int C, int T, int SPL>
+cudaError_t run_shape(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st, int grid_cap) {
+    return PassLauncher<R, C>::template run<T, SPL>(a, Wsp, h_counters, st, grid_cap);
+}
+
+// the team shapes built: lanes per node batch x sites per lane
+#define PFFRG_TEAM_SHAPES(X) X(8, 1) X(16, 1) X(32, 1) X(16, 3) X(16, 4) X(32, 2) X(32, 4) X(32, 8)
+
+// the default shape for Ns sites: the narrowest team (more teams per warp, smaller node
+// batches and staging) whose lanes hold at most four sites each
+__host__ __device__ inline void default_team_shape(int Ns, int& T, int& SPL) {
+    if (Ns <= 8) T = 8, SPL = 1;
+    else if (Ns <= 16) T = 16, SPL = 1;
+    else if (Ns <= 32) T = 32, SPL = 1;
+    else if (Ns <= 48) T = 16, SPL = 3;
+    else if (Ns <= 64) T = 16, SPL = 4;
+    else if (Ns <= 128) T = 32, SPL = 4;
+    else T = 32, SPL = 8;
+}
+
 template <typename R, int C>
 cudaError_t launch_pass_impl(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st) {
     const int Ns = a.L.Ns;
     if (a.ntasks == 0) return cudaSuccess;
+    if (Ns > 256) return cudaErrorInvalidValue;
     const int cap = 152 * 32;
-    // a requested team shape that covers the sites
-    if (a.team_T > 0 && a.team_T * a.team_SPL >= Ns) {
-        const int T = a.team_T, S = a.team_SPL;
-        if (T == 8 && S == 1) return PassLauncher<R, C>::template run<8, 1>(a, Wsp, h_counters, st, cap);
-        if (T == 16 && S == 1) return PassLauncher<R, C>::template run<16, 1>(a, Wsp, h_counters, st, cap);
-        if (T == 16 && S == 3) return PassLauncher<R, C>::template run<16, 3>(a, Wsp, h_counters, st, cap);
-        if (T == 16 && S == 4) return PassLauncher<R, C>::template run<16, 4>(a, Wsp, h_counters, st, cap);
-        if (T == 32 && S == 1) return PassLauncher<R, C>::template run<32, 1>(a, Wsp, h_counters, st, cap);
-        if (T == 32 && S == 2) return PassLauncher<R, C>::template run<32, 2>(a, Wsp, h_counters, st, cap);
-        if (T == 32 && S == 4) return PassLauncher<R, C>::template run<32, 4>(a, Wsp, h_counters, st, cap);
-        if (T == 32 && S == 8) return PassLauncher<R, C>::template run<32, 8>(a, Wsp, h_counters, st, cap);
-    }
-    if (Ns <= 8) return PassLauncher<R, C>::template run<8, 1>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 16) return PassLauncher<R, C>::template run<16, 1>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 32) return PassLauncher<R, C>::template run<32, 1>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 64) return PassLauncher<R, C>::template run<32, 2>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 128) return PassLauncher<R, C>::template run<32, 4>(a, Wsp, h_counters, st, cap);
-    if (Ns <= 256) return PassLauncher<R, C>::template run<32, 8>(a, Wsp, h_counters, st, cap);
+    int T, S;
+    default_team_shape(Ns, T, S);
+    if (a.team_T > 0 && a.team_T * a.team_SPL >= Ns) T = a.team_T, S = a.team_SPL;  // a requested shape
+#define PFFRG_DISPATCH(t, s) \
+    if (T == t && S == s) return run_shape<R, C, t, s>(a, Wsp, h_counters, st, cap);
+    PFFRG_TEAM_SHAPES(PFFRG_DISPATCH)
+#undef PFFRG_DISPATCH
     return cudaErrorInvalidValue;
 }
 

@@ -107,11 +107,9 @@ inline void wave_space_carve(WaveSpace& W, void* base, long long nsub, int Ns, l
     W.qcap = (int)qcap;
 }
 
+// one pass of channel tasks (SU(2) or U(1)-DM by a.L.C)
 template <typename R>
 cudaError_t launch_pass(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st);
-// the U(1)-DM (C = 6) instantiation, in its own translation unit
-template <typename R>
-cudaError_t launch_pass_u1dm(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cudaStream_t st);
 
 // GK integrals of the self energy / corrections (QuadGK-equivalent)
 enum SigmaKind { SIG_FLOW = 0, SIG_CORR1 = 1, SIG_CORR2 = 2, SIG_SDE = 3 };
