@@ -174,6 +174,14 @@ int pffrg_set_async_waves(pffrg_ctx* ctx, int on);
  * counterpart in the reference. */
 int pffrg_set_team_shape(pffrg_ctx* ctx, int lanes, int sites_per_lane);
 
+/* Mixed path: a Simpson subdomain whose convergence test is closer to its
+ * bounds than eps (the relative rounding allowed for the FP32 node values)
+ * could be decided the other way in FP64; such subdomains are evaluated again
+ * in FP64 on the FP64 actions, so every adaptive decision of the mixed path is
+ * the FP64 path's and the two differ by FP32 arithmetic only.  Default 1e-5;
+ * 0 turns the hand-off off (FP32 decisions).  No counterpart in the reference. */
+int pffrg_set_fp64_handoff(pffrg_ctx* ctx, double eps);
+
 /* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86,
  * correlation_u1_dm.jl:152-190): static spin correlations χ[i, w] of the
  * action `a` at Λ on the frequencies chi_mesh[0..num_chi), written

@@ -41,6 +41,10 @@ struct pffrg_ctx {
     float* f_da = nullptr;
     float* f_dal = nullptr;
     float* f_dtemp = nullptr;
+    // the FP64 action each FP32 copy was last made from (the FP64 pass of the mixed path reads it)
+    const float* f_copy[4] = {nullptr, nullptr, nullptr, nullptr};
+    const double* f_src[4] = {nullptr, nullptr, nullptr, nullptr};
+    double esc_eps = 1e-5;  // FP64 hand-off margin of the mixed path (0: off)
     std::vector<double> h_mesh;    // host copy of [σ|Ωs|νs|Ωt|νt]
     double* log_bounds = nullptr;  // [2][NO][eval+1]
     int bounds_cap = 0;            // eval the buffer holds
@@ -278,12 +282,48 @@ cudaError_t launch_waves(pffrg_ctx* ctx, const PassArgs<R>& p) {
     return e;
 }
 
+// the FP64 action an FP32 copy of the mixed path was made from
+const double* fp64_source(const pffrg_ctx* ctx, const float* y) {
+    if (!y) return nullptr;
+    for (int k = 0; k < 4; ++k)
+        if (ctx->f_copy[k] == y) return ctx->f_src[k];
+    return nullptr;
+}
+
+// One pass; on the mixed path the FP32 waves hand the subdomains whose Simpson decisions FP32
+// rounding could flip to the same pass in FP64 on the FP64 actions, which also sums the results.
+template <typename R>
+cudaError_t launch_pass_all(pffrg_ctx* ctx, const PassArgs<R>& p) {
+    if constexpr (sizeof(R) == 4) {
+        if (ctx->esc_eps > 0.0) {
+            static_assert(sizeof(PassArgs<float>) == sizeof(PassArgs<double>), "R appears only in pointers");
+            PassArgs<float> p32 = p;
+            p32.esc_mode = 1;
+            p32.esc_eps = ctx->esc_eps;
+            PassArgs<double> p64;
+            std::memcpy(&p64, &p32, sizeof(p64));
+            for (int k = 0; k < 4; ++k) {
+                p64.src[k] = fp64_source(ctx, p32.src[k]);
+                if (p32.src[k] && !p64.src[k]) return cudaErrorInvalidValue;
+            }
+            p64.prop_a = fp64_source(ctx, p32.prop_a);
+            p64.prop_da = fp64_source(ctx, p32.prop_da);
+            if ((p32.prop_a && !p64.prop_a) || (p32.prop_da && !p64.prop_da)) return cudaErrorInvalidValue;
+            p64.esc_mode = 2;
+            cudaError_t e = launch_waves<float>(ctx, p32);
+            if (e != cudaSuccess) return e;
+            return launch_waves<double>(ctx, p64);
+        }
+    }
+    return launch_waves<R>(ctx, p);
+}
+
 // pass launch, bracketed by CUDA events on the context's stream when timing is on
 template <typename R>
 cudaError_t run_pass(pffrg_ctx* ctx, const PassArgs<R>& p) {
     ++ctx->launches;
     ++ctx->pass_launches;
-    if (!ctx->timing) return launch_waves<R>(ctx, p);
+    if (!ctx->timing) return launch_pass_all<R>(ctx, p);
     while ((int)ctx->ev.size() < 2 * (ctx->ev_used + 1)) {
         cudaEvent_t e;
         cudaError_t er = cudaEventCreate(&e);
@@ -294,7 +334,7 @@ cudaError_t run_pass(pffrg_ctx* ctx, const PassArgs<R>& p) {
     ++ctx->ev_used;
     cudaError_t er = cudaEventRecord(e0, ctx->st);
     if (er != cudaSuccess) return er;
-    er = launch_waves<R>(ctx, p);
+    er = launch_pass_all<R>(ctx, p);
     if (er != cudaSuccess) return er;
     return cudaEventRecord(e1, ctx->st);
 }
@@ -455,6 +495,12 @@ int sigma_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* aux, do
 }
 
 int to_f(pffrg_ctx* ctx, const double* x, float* y) {
+    for (int k = 0; k < 4; ++k)
+        if (ctx->f_copy[k] == y || !ctx->f_copy[k]) {
+            ctx->f_copy[k] = y;
+            ctx->f_src[k] = x;
+            break;
+        }
     ++ctx->launches;
     CK(launch_to_float(x, y, ctx->L.total, ctx->st));
     return 0;
@@ -1275,6 +1321,13 @@ int pffrg_resample(pffrg_ctx* ctx, int src_slot, int dst_slot, const pffrg_mesh_
 int pffrg_set_async_waves(pffrg_ctx* ctx, int on) {
     if (!ctx) return PFFRG_E_ARGS;
     ctx->async_waves = on ? 1 : 0;
+    return 0;
+}
+
+int pffrg_set_fp64_handoff(pffrg_ctx* ctx, double eps) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (!(eps >= 0.0) || eps >= 1.0) return ctx->fail(PFFRG_E_ARGS, "hand-off margin must be in [0, 1)");
+    ctx->esc_eps = eps;
     return 0;
 }
 

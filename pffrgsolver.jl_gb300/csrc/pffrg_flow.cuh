@@ -782,6 +782,57 @@ __device__ __forceinline__ int simps_test(const double s_old[C][SPL], const doub
     return (adiff < atol || rdiff < rtol || 2 * n > (1ll << 20)) ? 1 : 0;
 }
 
+// The same test on the FP32 pass of the mixed path: 1 done, 0 next level, 2 hand the subdomain to
+// the FP64 pass.  sa_old / sa_new bound the norms of the Simpson sums taken over |node values|
+// with |weights|; with node values rounded by at most eps of their magnitude the FP64 sums lie
+// within eps sa of the FP32 ones, so when the test is closer to one of its bounds than that
+// margin the FP64 evaluation of the same nodes could decide the other way, and the subdomain is
+// evaluated again in FP64 from its first level (all its decisions then are the FP64 path's).
+template <int T, int SPL, int C>
+__device__ __forceinline__ int simps_decide(const double s_old[C][SPL], const double s_new[C][SPL], long long n,
+                                            double atol, double rtol, double eps, double sa_old, double sa_new) {
+    double ss_r = 0.0, ss_n = 0.0, ss_d = 0.0;
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+#pragma unroll
+        for (int k = 0; k < SPL; ++k) {
+            const double rich = s_old[c][k] * (-1.0 / 15.0) + (16.0 / 15.0) * s_new[c][k];
+            const double dd = rich - s_new[c][k];
+            ss_r += rich * rich;
+            ss_n += s_new[c][k] * s_new[c][k];
+            ss_d += dd * dd;
+        }
+    ss_r = in_team_sum<T>(ss_r);
+    ss_n = in_team_sum<T>(ss_n);
+    ss_d = in_team_sum<T>(ss_d);
+    const double adiff = sqrt(ss_d);
+    const double den = fmax(sqrt(ss_r), sqrt(ss_n));
+    if (2 * n > (1ll << 20)) return 1;
+    const int done = (adiff < atol || adiff / den < rtol) ? 1 : 0;
+    const double E = eps * (sa_new + sa_old) / 15.0;          // |Δ64 - Δ32|
+    const double Es = eps * (16.0 * sa_new + sa_old) / 15.0;  // change of the norms in the bound
+    const bool can_done = adiff - E < atol || adiff - E < rtol * (den + Es);
+    const bool can_go = adiff + E >= atol && adiff + E >= rtol * fmax(den - Es, 0.0);
+    return (can_done && can_go) ? 2 : done;
+}
+
+// norm of a team's per-site values
+template <int T, int SPL, int C>
+__device__ __forceinline__ double team_norm(const double v[C][SPL]) {
+    double ss = 0.0;
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+#pragma unroll
+        for (int k = 0; k < SPL; ++k) ss += v[c][k] * v[c][k];
+    return sqrt(in_team_sum<T>(ss));
+}
+
+// hand a subdomain from the FP32 pass to the FP64 pass (team lane 0)
+__device__ __forceinline__ void hand_off(WaveSpace& Wsp, int sub) {
+    Wsp.subs[sub].n = 0;
+    Wsp.esc[atomicAdd(&Wsp.counters[5], 1)] = sub;
+}
+
 // ---- wave 0: first five nodes of every subdomain, boundary nodes, first test ----
 template <typename R, int T, int SPL, int C>
 __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveSpace Wsp) {
@@ -796,9 +847,11 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
     const int jobs = 4 * A.eval + 1;
     const long long nwarps = (long long)gridDim.x * kWarps;
     constexpr int NB = BatchOf<T, C, SPL>::NB;
-    for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < Wsp.nsub; base += nwarps * NPW) {
-        const int sub = (int)(base + team);
-        const bool valid = sub < Wsp.nsub;
+    // the FP64 pass of the mixed path starts only the subdomains the FP32 pass handed to it
+    const int nwork = A.esc_mode == 2 ? Wsp.counters[5] : Wsp.nsub;
+    for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < nwork; base += nwarps * NPW) {
+        const bool valid = base + team < nwork;
+        const int sub = !valid ? 0 : (A.esc_mode == 2 ? Wsp.esc[base + team] : (int)(base + team));
         TaskInfo ti{0, 1, 0, 0, 0};
         int job = 0, cnt = 0;
         double x[8], lo = 0, hi = 0, sgn = 1;
@@ -860,8 +913,33 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
                 s_new[c][k] = 0.5 * s_old[c][k] + wn * f_new[c][k] + wo * (double)g[2][c][k];
             }
         // every lane takes part in the test's team reductions
-        const int done = simps_test<T, SPL, C>(s_old, s_new, 2, A.atol, A.rtol, team, false);
+        int done;
+        double sa_new = 0.0, fab = 0.0;
+        if (A.esc_mode == 1) {
+            double a_old[C][SPL], a_new[C][SPL], a_f[C][SPL];
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) {
+                    a_old[c][k] = a_new[c][k] = a_f[c][k] = 0.0;
+                    if (!simpson) continue;
+                    a_old[c][k] = we * fabs((double)g[0][c][k]) + wm * fabs((double)g[2][c][k]) +
+                                  we * fabs((double)g[4][c][k]);
+                    a_f[c][k] = fabs((double)g[1][c][k]) + fabs((double)g[3][c][k]);
+                    a_new[c][k] = 0.5 * a_old[c][k] + fabs(wn) * a_f[c][k] + fabs(wo) * fabs((double)g[2][c][k]);
+                }
+            const double sa_old = team_norm<T, SPL, C>(a_old);
+            sa_new = team_norm<T, SPL, C>(a_new);
+            fab = team_norm<T, SPL, C>(a_f);
+            done = simps_decide<T, SPL, C>(s_old, s_new, 2, A.atol, A.rtol, A.esc_eps, sa_old, sa_new);
+        } else {
+            done = simps_test<T, SPL, C>(s_old, s_new, 2, A.atol, A.rtol, team, false);
+        }
         if (!valid) continue;
+        if (simpson && done == 2) {
+            if (tl == 0) hand_off(Wsp, sub);
+            continue;
+        }
         double* sA = Wsp.stA + (size_t)sub * C * Ns;
         double* sB = Wsp.stB + (size_t)sub * C * Ns;
         if (!simpson) {
@@ -894,6 +972,8 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
             S.lo = lo;
             S.hi = hi;
             S.sgn = sgn;
+            S.sa = sa_new;
+            S.fab = fab;
             if (done) S.n = 0;
             else enqueue(Wsp, 1, sub, 4);
         }
@@ -949,10 +1029,14 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
 #pragma unroll
         for (int o = T; o < 32; o <<= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
         Acc<R> acc[C][SPL];
+        R aab[C][SPL];  // FP32 pass of the mixed path: sums of |node values|
 #pragma unroll
         for (int c = 0; c < C; ++c)
 #pragma unroll
-            for (int k = 0; k < SPL; ++k) acc[c][k] = Acc<R>{(R)0, (R)0};
+            for (int k = 0; k < SPL; ++k) {
+                acc[c][k] = Acc<R>{(R)0, (R)0};
+                aab[c][k] = (R)0;
+            }
         for (int b = 0; b < mx; b += NB) {
             double x[NB];
             const int nb = max(0, min(NB, cnt - b));
@@ -965,7 +1049,21 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
 #pragma unroll
                 for (int c = 0; c < C; ++c)
 #pragma unroll
-                    for (int k = 0; k < SPL; ++k) acc_add(acc[c][k], g[j][c][k]);
+                    for (int k = 0; k < SPL; ++k) {
+                        acc_add(acc[c][k], g[j][c][k]);
+                        if constexpr (sizeof(R) == 4) aab[c][k] += fabsf(g[j][c][k]);
+                    }
+        }
+        if constexpr (sizeof(R) == 4) {
+            if (A.esc_mode == 1) {
+                double ad[C][SPL];
+#pragma unroll
+                for (int c = 0; c < C; ++c)
+#pragma unroll
+                    for (int k = 0; k < SPL; ++k) ad[c][k] = (double)aab[c][k];
+                const double nrm = team_norm<T, SPL, C>(ad);  // every lane of the warp takes part
+                if (valid && tl == 0) Wsp.part_abs[chunk] = nrm;
+            }
         }
         if (!valid) continue;
         double* P = Wsp.part + (size_t)chunk * C * Ns;
@@ -985,7 +1083,8 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
 
 // ---- wave k >= 1: per subdomain, next Simpson sum, test, result or next level ----
 template <int T, int SPL, int C>
-__global__ void __launch_bounds__(kWarps * 32) decide_kernel(WaveSpace Wsp, int Ns, double atol, double rtol, int par) {
+__global__ void __launch_bounds__(kWarps * 32) decide_kernel(WaveSpace Wsp, int Ns, double atol, double rtol, int par,
+                                                             int esc_mode, double esc_eps) {
     constexpr int NPW = 32 / T;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
@@ -1016,8 +1115,21 @@ __global__ void __launch_bounds__(kWarps * 32) decide_kernel(WaveSpace Wsp, int 
                 s_old[c][k] = sA[c * Ns + i];
                 s_new[c][k] = 0.5 * s_old[c][k] + wn * f + wo * sB[c * Ns + i];
             }
-        const int done = simps_test<T, SPL, C>(s_old, s_new, S.n, atol, rtol, team, false);
+        int done;
+        double sa_new = 0.0, fa_new = 0.0;
+        if (esc_mode == 1) {
+            for (int q = 0; q < S.nchunk; ++q) fa_new += Wsp.part_abs[S.chunk0 + q];  // triangle bound
+            const double sa_old = valid ? S.sa : 0.0;
+            sa_new = 0.5 * sa_old + fabs(wn) * fa_new + fabs(wo) * (valid ? S.fab : 0.0);
+            done = simps_decide<T, SPL, C>(s_old, s_new, S.n, atol, rtol, esc_eps, sa_old, sa_new);
+        } else {
+            done = simps_test<T, SPL, C>(s_old, s_new, S.n, atol, rtol, team, false);
+        }
         if (!valid) continue;
+        if (done == 2) {
+            if (tl == 0) hand_off(Wsp, sub);
+            continue;
+        }
 #pragma unroll
         for (int c = 0; c < C; ++c)
 #pragma unroll
@@ -1032,8 +1144,13 @@ __global__ void __launch_bounds__(kWarps * 32) decide_kernel(WaveSpace Wsp, int 
                 }
             }
         if (tl == 0) {
-            if (done) Wsp.subs[sub].n = 0;
-            else enqueue(Wsp, par ^ 1, sub, 2 * S.n);
+            if (done) {
+                Wsp.subs[sub].n = 0;
+            } else {
+                Wsp.subs[sub].sa = sa_new;
+                Wsp.subs[sub].fab = fa_new;
+                enqueue(Wsp, par ^ 1, sub, 2 * S.n);
+            }
         }
     }
 }
@@ -1085,7 +1202,8 @@ struct PassLauncher {
             return e;
         constexpr int NPW = 32 / T;
         const int teams_per_block = kWarps * NPW;
-        if ((e = cudaMemsetAsync(Wsp.counters, 0, sizeof(int) * 5, st))) return e;
+        // the FP64 pass of the mixed path keeps the count of handed subdomains (counters[5])
+        if ((e = cudaMemsetAsync(Wsp.counters, 0, sizeof(int) * (a.esc_mode == 2 ? 5 : 6), st))) return e;
         int g0 = (Wsp.nsub + teams_per_block - 1) / teams_per_block;
         wave0_kernel<R, T, SPL, C><<<g0 < grid_cap ? g0 : grid_cap, kWarps * 32, smem, st>>>(a, Wsp);
         if ((e = cudaGetLastError())) return e;
@@ -1098,12 +1216,14 @@ struct PassLauncher {
             for (int wave = 1; wave <= 21; ++wave) {
                 eval_kernel<R, T, SPL, C><<<grid_cap, kWarps * 32, smem, st>>>(a, Wsp, par);
                 if ((e = cudaGetLastError())) return e;
-                decide_kernel<T, SPL, C><<<gd, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol, par);
+                decide_kernel<T, SPL, C><<<gd, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol, par, a.esc_mode,
+                                                                     a.esc_eps);
                 if ((e = cudaGetLastError())) return e;
                 par ^= 1;
             }
             wave_status_kernel<<<1, 32, 0, st>>>(Wsp.counters, a.status);
             if ((e = cudaGetLastError())) return e;
+            if (a.esc_mode == 1) return cudaSuccess;  // the FP64 pass finishes and reduces
             reduce_kernel<R, C><<<a.ntasks * a.nchan, 128, 0, st>>>(a, Wsp);
             return cudaGetLastError();
         }
@@ -1122,10 +1242,11 @@ struct PassLauncher {
             if ((e = cudaGetLastError())) return e;
             int gd = (nact + teams_per_block - 1) / teams_per_block;
             decide_kernel<T, SPL, C><<<gd < grid_cap ? gd : grid_cap, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol,
-                                                                                           par);
+                                                                                           par, a.esc_mode, a.esc_eps);
             if ((e = cudaGetLastError())) return e;
             par ^= 1;
         }
+        if (a.esc_mode == 1) return cudaSuccess;  // the FP64 pass finishes and reduces
         reduce_kernel<R, C><<<a.ntasks * a.nchan, 128, 0, st>>>(a, Wsp);
         return cudaGetLastError();
     }

@@ -49,6 +49,11 @@ struct PassArgs {
     int reduced;          // reduced s bubble of the SDE (U(1)-DM keeps xx, zz, dd only)
     int async_waves;      // levels without host round trips; overflow reported in *status (bit 3)
     int team_T, team_SPL; // team shape (lanes per node batch, sites per lane); 0: chosen by Ns
+    // FP64 hand-off of the mixed path: 1 = FP32 pass that hands every subdomain whose Simpson test
+    // is closer to its bounds than esc_eps (relative rounding of the FP32 node values) allows to
+    // an FP64 pass, 2 = that FP64 pass over the handed subdomains (then the reduction), 0 = off
+    int esc_mode;
+    double esc_eps;
     int* status;
     unsigned long long* node_counter;  // optional: [0] integrand evaluations, [1] algorithmic values read
 };
@@ -61,6 +66,8 @@ struct SubRec {
     long long n;  // new nodes of the pending level (0: finished)
     int chunk0;   // first chunk of the pending level in the wave queue
     int nchunk;
+    double sa;    // FP32 pass: bound of |weights| x |node values| of the last Simpson sum (norm)
+    double fab;   // and of the last level's new nodes
 };
 
 struct WaveSpace {
@@ -70,7 +77,9 @@ struct WaveSpace {
     int4* queue[2];  // chunk records (sub, first node, count, -) of the current / next level
     int* active[2];  // subdomains with chunks in the current / next level
     double* part;    // [qcap][C Ns] chunk partial node sums
-    int* counters;   // [0..1] chunks, [2..3] active subdomains per parity, [4] queue overflow
+    double* part_abs;  // [qcap] FP32 pass: norm of the chunk's sums of |node values|
+    int* esc;        // [nsub] subdomains handed from the FP32 pass to the FP64 pass
+    int* counters;   // [0..1] chunks, [2..3] active subdomains per parity, [4] queue overflow, [5] handed
     int nsub, qcap;
 };
 
@@ -80,7 +89,8 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 inline size_t wave_space_bytes(long long nsub, int Ns, long long qcap, int C) {
     const size_t vec = sizeof(double) * C * (size_t)Ns;
     return align256(sizeof(SubRec) * nsub) + 2 * align256(vec * nsub) + 2 * align256(sizeof(int4) * qcap) +
-           2 * align256(sizeof(int) * nsub) + align256(vec * qcap) + align256(sizeof(int) * 8);
+           2 * align256(sizeof(int) * nsub) + align256(vec * qcap) + align256(sizeof(double) * qcap) +
+           align256(sizeof(int) * nsub) + align256(sizeof(int) * 8);
 }
 
 inline void wave_space_carve(WaveSpace& W, void* base, long long nsub, int Ns, long long qcap, int C) {
@@ -102,6 +112,10 @@ inline void wave_space_carve(WaveSpace& W, void* base, long long nsub, int Ns, l
     }
     W.part = reinterpret_cast<double*>(p);
     p += align256(vec * qcap);
+    W.part_abs = reinterpret_cast<double*>(p);
+    p += align256(sizeof(double) * qcap);
+    W.esc = reinterpret_cast<int*>(p);
+    p += align256(sizeof(int) * nsub);
     W.counters = reinterpret_cast<int*>(p);
     W.nsub = (int)nsub;
     W.qcap = (int)qcap;

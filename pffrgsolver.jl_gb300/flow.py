@@ -152,6 +152,11 @@ class FlowContext:
         """Device-driven quadrature levels (default) or the host-driven loop; same results."""
         self._check(self.lib.pffrg_set_async_waves(self.h, int(bool(on))), "set_async_waves")
 
+    def set_fp64_handoff(self, eps: float = 1e-5) -> None:
+        """Mixed path: Simpson subdomains whose test FP32 rounding (relative eps) could flip are
+        evaluated again in FP64, so the adaptive decisions are the FP64 path's (0: off)."""
+        self._check(self.lib.pffrg_set_fp64_handoff(self.h, float(eps)), "set_fp64_handoff")
+
     def set_team_shape(self, lanes: int = 0, sites_per_lane: int = 0) -> None:
         """Team shape of the quadrature passes (lanes x sites per lane; 0, 0: chosen from the
         number of sites).  Results agree to rounding."""
