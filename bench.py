@@ -244,6 +244,8 @@ def ours(args):
 
     ctx = FlowContext(r, m, precision="mixed", device=local)
     ctx.upload(C.SLOT_A, a)
+    # the team shape of the quadrature passes, picked by timing one right-hand side per candidate
+    team = ctx.autotune_team_shape(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
 
     def rhs():
         ctx.rhs(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
@@ -319,7 +321,8 @@ def ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 integrand / f64 quadrature bookkeeping", "data": "synthetic",
-        "config": config(args, w, {"precision": "mixed", "wall_ms_per_step": t_wall * 1e3 / args.steps}),
+        "config": config(args, w, {"precision": "mixed", "wall_ms_per_step": t_wall * 1e3 / args.steps,
+                                   "team_shape": "%dx%d" % team}),
         "e2e": e2e,
         "gpu_launches": int(round(launches_step * args.steps)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -174,6 +174,15 @@ int pffrg_set_async_waves(pffrg_ctx* ctx, int on);
  * counterpart in the reference. */
 int pffrg_set_team_shape(pffrg_ctx* ctx, int lanes, int sites_per_lane);
 
+/* Autotuner of the team shape: times one right-hand side (as pffrg_rhs on
+ * a_slot into da_slot, without Σ corrections) for every built shape that
+ * covers the sites with at most twice as many lane slots as sites, keeps the
+ * fastest as the context's shape and returns it.  da_slot is overwritten.
+ * No counterpart in the reference. */
+int pffrg_autotune_team_shape(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, int eval,
+                              double gamma_atol, double gamma_rtol, double sigma_atol, double sigma_rtol,
+                              int* lanes, int* sites_per_lane);
+
 /* Mixed path: a Simpson subdomain whose convergence test is closer to its
  * bounds than eps (the relative rounding allowed for the FP32 node values)
  * could be decided the other way in FP64; such subdomains are evaluated again

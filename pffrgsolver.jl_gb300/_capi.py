@@ -27,7 +27,8 @@ EXPORTED = [
     "pffrg_dsigma", "pffrg_dgamma", "pffrg_sde", "pffrg_bse", "pffrg_action_size", "pffrg_upload",
     "pffrg_download", "pffrg_rhs", "pffrg_bs_step", "pffrg_accept", "pffrg_last_integrand_evals",
     "pffrg_host_alloc", "pffrg_host_free", "pffrg_set_timing", "pffrg_read_stats", "pffrg_chi", "pffrg_chi_slot",
-    "pffrg_set_async_waves", "pffrg_set_team_shape", "pffrg_set_fp64_handoff", "pffrg_scan_cuts",
+    "pffrg_set_async_waves", "pffrg_set_team_shape", "pffrg_autotune_team_shape", "pffrg_set_fp64_handoff",
+    "pffrg_scan_cuts",
     "pffrg_resample",
 ]
 
@@ -97,6 +98,9 @@ def load():
     L.pffrg_set_async_waves.argtypes = [vp, ctypes.c_int]
     L.pffrg_set_team_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.pffrg_set_fp64_handoff.argtypes = [vp, ctypes.c_double]
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.pffrg_autotune_team_shape.argtypes = [vp, ctypes.c_int, d, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d, d, d,
+                                            ip, ip]
     L.pffrg_scan_cuts.argtypes = [vp, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int64), dp]
     L.pffrg_resample.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(MeshView)]
     L.pffrg_chi.argtypes = [vp, d, AV, dp, ctypes.c_int, d, d, dp]

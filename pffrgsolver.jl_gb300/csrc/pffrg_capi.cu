@@ -643,17 +643,11 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     return 0;
 }
 
-// compute_dΣ! on device actions
-template <typename R>
+// compute_dΣ! on device actions.  The Gauss-Kronrod integrals run in FP64 on both paths: their
+// adaptive bisection stops on |K15 - G7|, which FP32 rounding of the integrand keeps above the
+// tolerance at small Λ (the segments then grow to the capacity limit)
 int dsigma_dev(pffrg_ctx* ctx, double Lam, const double* a, double* da, double atol, double rtol) {
-    const R* ra;
-    if constexpr (sizeof(R) == 8) {
-        ra = (const R*)a;
-    } else {
-        if (int rc = to_f(ctx, a, ctx->f_a)) return rc;
-        ra = (const R*)ctx->f_a;
-    }
-    return sigma_run<R>(ctx, SIG_FLOW, Lam, ra, nullptr, da, atol, rtol);
+    return sigma_run<double>(ctx, SIG_FLOW, Lam, a, nullptr, da, atol, rtol);
 }
 
 // compute_dΓ_{1l,2l,ml}! (+ compute_dΣ_corr!) on device actions
@@ -678,7 +672,7 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
     CK(cudaMemsetAsync(ctx->counter, 0, 2 * sizeof(unsigned long long), ctx->st));
     if (int rc = upload_log_bounds(ctx, Lam, eval)) return rc;
     // 1 loop (compute.jl:57-112)
-    if (int rc = corrs_run<R>(ctx, PROP_KAT, Lam, s.a, s.da, gatol, grtol, ctx->corrs)) return rc;
+    if (int rc = corrs_run<double>(ctx, PROP_KAT, Lam, a, da, gatol, grtol, ctx->corrs)) return rc;
     {
         PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
         set_tasks(p, ctx, false);
@@ -695,7 +689,7 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
         if constexpr (sizeof(R) == 4) {
             if (int rc = to_f(ctx, da, ctx->f_da)) return rc;
         }
-        if (int rc = corrs_run<R>(ctx, PROP_PLAIN, Lam, s.a, s.a, gatol, grtol, ctx->corrs)) return rc;
+        if (int rc = corrs_run<double>(ctx, PROP_PLAIN, Lam, a, a, gatol, grtol, ctx->corrs)) return rc;
         PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
         set_tasks(p, ctx, true);
         set_slots<R>(p, s.da, s.a, s.da, s.a, kMaskLeft);
@@ -744,20 +738,10 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
             CK((++ctx->launches, launch_axpby)(L, 1.0, ctx->da_temp, 1.0, da, false, true, ctx->st));
         }
         if (sigma_corr) {
-            // compute_dΣ_corr! (flow_self.jl:23-51)
-            const R* sig_src;
-            if constexpr (sizeof(R) == 8) {
-                sig_src = (const R*)ctx->da_sig;
-            } else {
-                if (int rc = to_f(ctx, ctx->da_sig, ctx->f_dtemp)) return rc;
-                sig_src = (const R*)ctx->f_dtemp;
-            }
-            if (int rc = sigma_run<R>(ctx, SIG_CORR1, Lam, s.a, sig_src, ctx->da_sig, satol, srtol)) return rc;
-            if constexpr (sizeof(R) == 4) {
-                if (int rc = to_f(ctx, ctx->da_sig, ctx->f_dtemp)) return rc;
-            }
+            // compute_dΣ_corr! (flow_self.jl:23-51), in FP64 on both paths
+            if (int rc = sigma_run<double>(ctx, SIG_CORR1, Lam, a, ctx->da_sig, ctx->da_sig, satol, srtol)) return rc;
             CK(cudaMemsetAsync(ctx->sig_tmp, 0, sizeof(double) * L.Nsig, ctx->st));
-            if (int rc = sigma_run<R>(ctx, SIG_CORR2, Lam, s.a, sig_src, ctx->sig_tmp, satol, srtol)) return rc;
+            if (int rc = sigma_run<double>(ctx, SIG_CORR2, Lam, a, ctx->da_sig, ctx->sig_tmp, satol, srtol)) return rc;
             // da.Σ += da_Σ.Σ + corr2 (index 0 included: both are zero there)
             CK((++ctx->launches, launch_axpby)(L, 1.0, ctx->da_sig, 1.0, da, true, false, ctx->st));
             CK((++ctx->launches, launch_axpby)(L, 1.0, ctx->sig_tmp, 1.0, da, true, false, ctx->st));
@@ -768,15 +752,11 @@ int dgamma_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* d
 
 int rhs_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* da, int eval, double gatol,
             double grtol, double satol, double srtol, int sigma_corr) {
-    int rc;
-    if (ctx->precision == PFFRG_FP64) {
-        rc = dsigma_dev<double>(ctx, Lam, a, da, satol, srtol);
-        if (!rc) rc = dgamma_dev<double>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
-    } else {
-        rc = dsigma_dev<float>(ctx, Lam, a, da, satol, srtol);
-        if (!rc) rc = dgamma_dev<float>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
-    }
-    return rc;
+    int rc = dsigma_dev(ctx, Lam, a, da, satol, srtol);
+    if (rc) return rc;
+    if (ctx->precision == PFFRG_FP64)
+        return dgamma_dev<double>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
+    return dgamma_dev<float>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
 }
 
 int read_evals(pffrg_ctx* ctx) {
@@ -1019,9 +999,7 @@ static int dsigma_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, p
     CK(cudaSetDevice(ctx->device));
     if (int rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_A], a, true)) return rc;
     if (int rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, true)) return rc;
-    int rc = ctx->precision == PFFRG_FP64
-                 ? dsigma_dev<double>(ctx, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], atol, rtol)
-                 : dsigma_dev<float>(ctx, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], atol, rtol);
+    int rc = dsigma_dev(ctx, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], atol, rtol);
     if (rc) return rc;
     if ((rc = check_status(ctx))) return rc;
     if ((rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, false))) return rc;
@@ -1090,6 +1068,52 @@ int pffrg_rhs(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, in
     return gk_retry(ctx, [&] { return rhs_once(ctx, loops, Lam, a_slot, da_slot, eval, gatol, grtol, satol, srtol, sigma_corr); });
 }
 
+int pffrg_autotune_team_shape(pffrg_ctx* ctx, int loops, double Lam, int a_slot, int da_slot, int eval, double gatol,
+                              double grtol, double satol, double srtol, int* lanes, int* sites_per_lane) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    const int Ns = ctx->L.Ns;
+    static const int shapes[][2] = {{8, 1}, {16, 1}, {32, 1}, {16, 3}, {16, 4}, {32, 2}, {32, 4}, {32, 8}};
+    cudaEvent_t ev[2];
+    CK(cudaEventCreate(&ev[0]));
+    if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+        cudaEventDestroy(ev[0]);
+        return ctx->fail(PFFRG_E_CUDA, "cudaEventCreate failed");
+    }
+    float best = 0.f;
+    int bT = 0, bS = 0, rc = 0;
+    for (const auto& sh : shapes) {
+        const int cover = sh[0] * sh[1];
+        if (cover < Ns || cover > std::max(2 * Ns, 8)) continue;  // shapes that leave at most half the lanes idle
+        ctx->team_T = sh[0];
+        ctx->team_SPL = sh[1];
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && !rc; ++rep) {  // the first right-hand side loads the shape's kernels
+            cudaError_t e = cudaEventRecord(ev[0], ctx->st);
+            if (e == cudaSuccess) rc = pffrg_rhs(ctx, loops, Lam, a_slot, da_slot, eval, gatol, grtol, satol, srtol, 0);
+            if (e == cudaSuccess && !rc) e = cudaEventRecord(ev[1], ctx->st);
+            if (e == cudaSuccess && !rc) e = cudaEventSynchronize(ev[1]);
+            if (e == cudaSuccess && !rc) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            if (e != cudaSuccess && !rc) rc = ctx->fail(PFFRG_E_CUDA, "timing failed: %s", cudaGetErrorString(e));
+        }
+        if (rc) break;
+        if (!bT || ms < best) {
+            best = ms;
+            bT = sh[0];
+            bS = sh[1];
+        }
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    ctx->team_T = rc ? 0 : bT;
+    ctx->team_SPL = rc ? 0 : bS;
+    if (rc) return rc;
+    if (!bT) return ctx->fail(PFFRG_E_ARGS, "no team shape is built for %d sites", Ns);
+    if (lanes) *lanes = bT;
+    if (sites_per_lane) *sites_per_lane = bS;
+    return 0;
+}
+
 static int sde_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
               double grtol, double satol, double srtol) {
     if (!ctx) return PFFRG_E_ARGS;
@@ -1101,16 +1125,13 @@ static int sde_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pff
     auto run = [&](auto tag) -> int {
         using R = decltype(tag);
         const R* r1;
-        const R* r2;
         if constexpr (sizeof(R) == 8) {
             r1 = (const R*)d1;
-            r2 = (const R*)d2;
         } else {
             if (int rc = to_f(ctx, d1, ctx->f_a)) return rc;
             r1 = (const R*)ctx->f_a;
-            r2 = (const R*)ctx->f_da;
         }
-        if (int rc = corrs_run<R>(ctx, PROP_PLAIN, Lam, r1, r1, gatol, grtol, ctx->corrs_sde)) return rc;
+        if (int rc = corrs_run<double>(ctx, PROP_PLAIN, Lam, d1, d1, gatol, grtol, ctx->corrs_sde)) return rc;
         if (int rc = upload_log_bounds(ctx, Lam, eval)) return rc;
         // reduced s bubble (SDE.jl:2-56): slot 1 is the bare vertex
         PassArgs<R> p = base_pass<R>(ctx, Lam, eval, gatol, grtol);
@@ -1126,10 +1147,7 @@ static int sde_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pff
         p.prop_da = r1;
         p.out = d2;
         CK_PASS(run_pass<R>(ctx, p));
-        if constexpr (sizeof(R) == 4) {
-            if (int rc = to_f(ctx, d2, ctx->f_da)) return rc;
-        }
-        return sigma_run<R>(ctx, SIG_SDE, Lam, r1, r2, d2, satol, srtol);
+        return sigma_run<double>(ctx, SIG_SDE, Lam, d1, d2, d2, satol, srtol);
     };
     int rc = ctx->precision == PFFRG_FP64 ? run(double{}) : run(float{});
     if (rc) return rc;

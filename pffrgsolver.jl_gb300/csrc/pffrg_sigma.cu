@@ -1014,8 +1014,6 @@ cudaError_t launch_chi_sum(const ChiArgs& a, cudaStream_t st) {
 }
 
 template cudaError_t launch_sigma<double>(const SigmaArgs<double>&, cudaStream_t);
-template cudaError_t launch_sigma<float>(const SigmaArgs<float>&, cudaStream_t);
 template cudaError_t launch_corrs<double>(const CorrsArgs<double>&, cudaStream_t);
-template cudaError_t launch_corrs<float>(const CorrsArgs<float>&, cudaStream_t);
 
 }  // namespace pffrg

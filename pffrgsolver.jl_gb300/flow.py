@@ -157,6 +157,16 @@ class FlowContext:
         evaluated again in FP64, so the adaptive decisions are the FP64 path's (0: off)."""
         self._check(self.lib.pffrg_set_fp64_handoff(self.h, float(eps)), "set_fp64_handoff")
 
+    def autotune_team_shape(self, Lam: float, eval_: int, loops: int = 1, a_slot: int = _capi.SLOT_A,
+                            da_slot: int = _capi.SLOT_DA, gamma_tol=(1e-8, 1e-4), sigma_tol=(1e-8, 1e-4)):
+        """Time one right-hand side per candidate team shape on the device-resident action in
+        a_slot (da_slot is overwritten), keep the fastest and return it as (lanes, sites per lane)."""
+        t, s = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.pffrg_autotune_team_shape(self.h, loops, Lam, a_slot, da_slot, eval_, gamma_tol[0],
+                                                       gamma_tol[1], sigma_tol[0], sigma_tol[1], ctypes.byref(t),
+                                                       ctypes.byref(s)), "autotune_team_shape")
+        return t.value, s.value
+
     def set_team_shape(self, lanes: int = 0, sites_per_lane: int = 0) -> None:
         """Team shape of the quadrature passes (lanes x sites per lane; 0, 0: chosen from the
         number of sites).  Results agree to rounding."""
