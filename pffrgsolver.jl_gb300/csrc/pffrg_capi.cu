@@ -172,9 +172,10 @@ int upload_mesh(pffrg_ctx* ctx, const pffrg_mesh_view* m) {
     h.insert(h.end(), m->nu_s, m->nu_s + m->num_nu);
     h.insert(h.end(), m->omega_t, m->omega_t + m->num_omega);
     h.insert(h.end(), m->nu_t, m->nu_t + m->num_nu);
+    ctx->h_mesh = h;
+    append_inverse_spacings(h, ctx->L.Nsig, ctx->L.NO, ctx->L.Nn);
     CK(cudaMemcpyAsync(ctx->mesh, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
-    ctx->h_mesh = h;
     return 0;
 }
 
@@ -293,7 +294,17 @@ const double* fp64_source(const pffrg_ctx* ctx, const float* y) {
 // One pass; on the mixed path the FP32 waves hand the subdomains whose Simpson decisions FP32
 // rounding could flip to the same pass in FP64 on the FP64 actions, which also sums the results.
 template <typename R>
-cudaError_t launch_pass_all(pffrg_ctx* ctx, const PassArgs<R>& p) {
+cudaError_t launch_pass_all(pffrg_ctx* ctx, const PassArgs<R>& p0) {
+    PassArgs<R> p = p0;
+    // the FP64 Σ and dΣ of the propagators (node setup in FP64)
+    if constexpr (sizeof(R) == 8) {
+        p.prop_a64 = p.prop_a;
+        p.prop_da64 = p.prop_da;
+    } else {
+        p.prop_a64 = fp64_source(ctx, p.prop_a);
+        p.prop_da64 = fp64_source(ctx, p.prop_da);
+        if ((p.prop_a && !p.prop_a64) || (p.prop_da && !p.prop_da64)) return cudaErrorInvalidValue;
+    }
     if constexpr (sizeof(R) == 4) {
         if (ctx->esc_eps > 0.0) {
             static_assert(sizeof(PassArgs<float>) == sizeof(PassArgs<double>), "R appears only in pointers");
@@ -306,9 +317,8 @@ cudaError_t launch_pass_all(pffrg_ctx* ctx, const PassArgs<R>& p) {
                 p64.src[k] = fp64_source(ctx, p32.src[k]);
                 if (p32.src[k] && !p64.src[k]) return cudaErrorInvalidValue;
             }
-            p64.prop_a = fp64_source(ctx, p32.prop_a);
-            p64.prop_da = fp64_source(ctx, p32.prop_da);
-            if ((p32.prop_a && !p64.prop_a) || (p32.prop_da && !p64.prop_da)) return cudaErrorInvalidValue;
+            p64.prop_a = p32.prop_a64;
+            p64.prop_da = p32.prop_da64;
             p64.esc_mode = 2;
             cudaError_t e = launch_waves<float>(ctx, p32);
             if (e != cudaSuccess) return e;
@@ -909,7 +919,7 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
     bool ok = dalloc((void**)&ctx->lat.exch, sizeof(int) * Ns) && dalloc((void**)&ctx->lat.mult, sizeof(int) * Ns) &&
               dalloc((void**)&ctx->lat.ov_off, sizeof(int) * (Ns + 1)) &&
               dalloc((void**)&ctx->lat.ov_rows, sizeof(unsigned) * rows.size()) &&
-              dalloc((void**)&ctx->mesh, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
+              dalloc((void**)&ctx->mesh, 2 * sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
               dalloc((void**)&ctx->mesh_new, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
               dalloc((void**)&ctx->scan_arg, sizeof(long long) * 3 * L.C) &&
               dalloc((void**)&ctx->scan_cuts, sizeof(double) * 3 * L.C * (L.NO + 3 * L.Nn));

@@ -55,6 +55,31 @@ struct SMesh {
     R nt[kMaxMesh], int_[kMaxMesh];
 };
 
+// Meshes read from the FP64 device block in global memory (L1-resident): the node setup of the
+// quadrature passes (arguments, interval searches, weights, propagators) runs in FP64 on both
+// paths with these.  The block holds [σ | Ωs | νs | Ωt | νt] and then the inverse spacings
+// 1 / (x[k+1] - x[k]) of the same arrays (0 at the last entry).
+template <typename R>
+struct MeshG {
+    const R *sig, *isig, *Os, *iOs, *ns, *ins, *Ot, *iOt, *nt, *int_;
+};
+
+__device__ __forceinline__ MeshG<double> mesh_view(const double* mesh, int Nsig, int NO, int Nn) {
+    const int n = Nsig + 2 * NO + 2 * Nn;
+    MeshG<double> M;
+    M.sig = mesh;
+    M.Os = M.sig + Nsig;
+    M.ns = M.Os + NO;
+    M.Ot = M.ns + Nn;
+    M.nt = M.Ot + NO;
+    M.isig = M.sig + n;
+    M.iOs = M.Os + n;
+    M.ins = M.ns + n;
+    M.iOt = M.Ot + n;
+    M.int_ = M.nt + n;
+    return M;
+}
+
 // device mesh block written by the host: [σ | Ωs | νs | Ωt | νt] (FP64)
 template <typename R>
 __device__ inline void load_mesh(SMesh<R>& M, const double* mesh, int Nsig, int NO, int Nn) {
@@ -135,27 +160,29 @@ struct Plan {
     int off[8];
 };
 
-template <typename R>
-__device__ __forceinline__ void make_plan(Plan<R>& P, int chan, R w, R v, R vp, const SMesh<R>& M, int Ns,
-                                          int NO, int Nn) {
+// The interval search and the weights run in the arguments' type S (FP64 for the node setup of
+// both paths); the plan stores the weights in R.
+template <typename R, typename S, typename MV>
+__device__ __forceinline__ void make_plan(Plan<R>& P, int chan, S w, S v, S vp, const MV& M, int Ns, int NO,
+                                          int Nn) {
     bool ex = false, mp = false, smn = false, sm = false, sn = false;
     if (chan == 0) {  // get_buffer_s (buffer.jl:87-124)
-        if (w < (R)0) { w = -w; ex = !ex; }
-        if (v < (R)0) { v = -v; ex = !ex; mp = !mp; sm = !sm; }
-        if (vp < (R)0) { vp = -vp; mp = !mp; sn = !sn; }
+        if (w < (S)0) { w = -w; ex = !ex; }
+        if (v < (S)0) { v = -v; ex = !ex; mp = !mp; sm = !sm; }
+        if (vp < (S)0) { vp = -vp; mp = !mp; sn = !sn; }
     } else if (chan == 1) {  // get_buffer_t (buffer.jl:126-160)
-        if (w < (R)0) { w = -w; smn = !smn; }
-        if (v < (R)0) { v = -v; sm = !sm; }
-        if (vp < (R)0) { vp = -vp; sn = !sn; }
+        if (w < (S)0) { w = -w; smn = !smn; }
+        if (v < (S)0) { v = -v; sm = !sm; }
+        if (vp < (S)0) { vp = -vp; sn = !sn; }
     } else {  // get_buffer_u (buffer.jl:162-199)
-        if (w < (R)0) { w = -w; ex = !ex; smn = !smn; }
-        if (v < (R)0) { v = -v; ex = !ex; mp = !mp; sn = !sn; }
-        if (vp < (R)0) { vp = -vp; mp = !mp; sn = !sn; }
+        if (w < (S)0) { w = -w; ex = !ex; smn = !smn; }
+        if (v < (S)0) { v = -v; ex = !ex; mp = !mp; sn = !sn; }
+        if (vp < (S)0) { vp = -vp; mp = !mp; sn = !sn; }
     }
-    const R* Om = chan == 1 ? M.Ot : M.Os;
-    const R* iOm = chan == 1 ? M.iOt : M.iOs;
-    const R* nu = chan == 1 ? M.nt : M.ns;
-    const R* inu = chan == 1 ? M.int_ : M.ins;
+    const S* Om = chan == 1 ? M.Ot : M.Os;
+    const S* iOm = chan == 1 ? M.iOt : M.iOs;
+    const S* nu = chan == 1 ? M.nt : M.ns;
+    const S* inu = chan == 1 ? M.int_ : M.ins;
     if (Om[NO - 1] < fabs(w)) {  // get_buffer (buffer.jl:51-84): beyond the bosonic mesh
         P.kernel = 0;
         return;
@@ -164,39 +191,39 @@ __device__ __forceinline__ void make_plan(Plan<R>& P, int chan, R w, R v, R vp, 
     P.flags = (smn ? 1 : 0) | (sm ? 2 : 0) | (sn ? 4 : 0);
     P.src_ch = (chan == 1) ? 1 : ((chan == 0) == mp ? 2 : 0);
     P.sgn_d = ((sm ? -1 : 1) * (sn ? -1 : 1)) < 0 ? (R)-1 : (R)1;
-    const Param<R> p1 = get_param(w, Om, iOm, NO);
+    const Param<S> p1 = get_param(w, Om, iOm, NO);
     const bool vin = !(nu[Nn - 1] < fabs(v));
     const bool vpin = !(nu[Nn - 1] < fabs(vp));
     if (!vin && !vpin) {
         P.kernel = 1;
-        P.w[0] = p1.wl;
-        P.w[1] = p1.wu;
+        P.w[0] = (R)(p1.wl);
+        P.w[1] = (R)(p1.wu);
         P.off[0] = Ns * p1.lo;
         P.off[1] = Ns * p1.hi;
     } else if (vin != vpin) {
         P.kernel = vin ? 2 : 3;
-        const Param<R> pb = get_param(vin ? v : vp, nu, inu, Nn);
-        P.w[0] = p1.wl * pb.wl;
-        P.w[1] = p1.wu * pb.wl;
-        P.w[2] = p1.wl * pb.wu;
-        P.w[3] = p1.wu * pb.wu;
+        const Param<S> pb = get_param(vin ? v : vp, nu, inu, Nn);
+        P.w[0] = (R)(p1.wl * pb.wl);
+        P.w[1] = (R)(p1.wu * pb.wl);
+        P.w[2] = (R)(p1.wl * pb.wu);
+        P.w[3] = (R)(p1.wu * pb.wu);
         P.off[0] = Ns * (p1.lo + NO * pb.lo);
         P.off[1] = Ns * (p1.hi + NO * pb.lo);
         P.off[2] = Ns * (p1.lo + NO * pb.hi);
         P.off[3] = Ns * (p1.hi + NO * pb.hi);
     } else {
         P.kernel = 4;
-        const Param<R> p2 = get_param(v, nu, inu, Nn);
-        const Param<R> p3 = get_param(vp, nu, inu, Nn);
+        const Param<S> p2 = get_param(v, nu, inu, Nn);
+        const Param<S> p3 = get_param(vp, nu, inu, Nn);
         const int NON = NO * Nn;
-        P.w[0] = p1.wl * p2.wl * p3.wl;
-        P.w[1] = p1.wu * p2.wl * p3.wl;
-        P.w[2] = p1.wl * p2.wu * p3.wl;
-        P.w[3] = p1.wu * p2.wu * p3.wl;
-        P.w[4] = p1.wl * p2.wl * p3.wu;
-        P.w[5] = p1.wu * p2.wl * p3.wu;
-        P.w[6] = p1.wl * p2.wu * p3.wu;
-        P.w[7] = p1.wu * p2.wu * p3.wu;
+        P.w[0] = (R)(p1.wl * p2.wl * p3.wl);
+        P.w[1] = (R)(p1.wu * p2.wl * p3.wl);
+        P.w[2] = (R)(p1.wl * p2.wu * p3.wl);
+        P.w[3] = (R)(p1.wu * p2.wu * p3.wl);
+        P.w[4] = (R)(p1.wl * p2.wl * p3.wu);
+        P.w[5] = (R)(p1.wu * p2.wl * p3.wu);
+        P.w[6] = (R)(p1.wl * p2.wu * p3.wu);
+        P.w[7] = (R)(p1.wu * p2.wu * p3.wu);
         P.off[0] = Ns * (p1.lo + NO * p2.lo + NON * p3.lo);
         P.off[1] = Ns * (p1.hi + NO * p2.lo + NON * p3.lo);
         P.off[2] = Ns * (p1.lo + NO * p2.hi + NON * p3.lo);
@@ -274,8 +301,8 @@ __device__ __forceinline__ R jl_sign(R x) {
 }
 
 // get_Σ (Action.jl:8-26): Σ values of an action read from global memory
-template <typename R>
-__device__ __forceinline__ R get_sigma(const SMesh<R>& M, int Nsig, const R* __restrict__ Sig, R w) {
+template <typename R, typename MV>
+__device__ __forceinline__ R get_sigma(const MV& M, int Nsig, const R* __restrict__ Sig, R w) {
     if (fabs(w) <= M.sig[Nsig - 1]) {
         Param<R> p = get_param((R)fabs(w), M.sig, M.isig, Nsig);
         return jl_sign(w) * (p.wl * ldg(Sig + p.lo) + p.wu * ldg(Sig + p.hi));
@@ -294,8 +321,8 @@ __device__ __forceinline__ R G_bare(R L, R w) {
     return (R)0;
 }
 
-template <typename R>
-__device__ __forceinline__ R G_full(const SMesh<R>& M, int Nsig, const R* Sig, R L, R w) {
+template <typename R, typename MV>
+__device__ __forceinline__ R G_full(const MV& M, int Nsig, const R* Sig, R L, R w) {
     if (fabs(w) > (R)1e-8) {
         R s = get_sigma(M, Nsig, Sig, w);
         R g0 = G_bare(L, w);
@@ -305,8 +332,8 @@ __device__ __forceinline__ R G_full(const SMesh<R>& M, int Nsig, const R* Sig, R
     return (R)0;
 }
 
-template <typename R>
-__device__ __forceinline__ R S_single(const SMesh<R>& M, int Nsig, const R* Sig, R L, R w) {
+template <typename R, typename MV>
+__device__ __forceinline__ R S_single(const MV& M, int Nsig, const R* Sig, R L, R w) {
     if (fabs(w) > (R)1e-8) {
         R g = G_full(M, Nsig, Sig, L, w);
         R g0 = G_bare(L, w);
@@ -322,8 +349,8 @@ __device__ __forceinline__ R two_pi() {
 }
 
 // get_propagator_kat (bubbles.jl:64-80)
-template <typename R>
-__device__ __forceinline__ R prop_kat(const SMesh<R>& M, int Nsig, const R* Sig, const R* dSig, R L, R w1, R w2) {
+template <typename R, typename MV>
+__device__ __forceinline__ R prop_kat(const MV& M, int Nsig, const R* Sig, const R* dSig, R L, R w1, R w2) {
     R ds = get_sigma(M, Nsig, dSig, w1);
     R s1 = S_single(M, Nsig, Sig, L, w1);
     R g1 = G_full(M, Nsig, Sig, L, w1);
@@ -332,8 +359,8 @@ __device__ __forceinline__ R prop_kat(const SMesh<R>& M, int Nsig, const R* Sig,
 }
 
 // get_propagator (bubbles.jl:83-96)
-template <typename R>
-__device__ __forceinline__ R prop_plain(const SMesh<R>& M, int Nsig, const R* Sig, R L, R w1, R w2) {
+template <typename R, typename MV>
+__device__ __forceinline__ R prop_plain(const MV& M, int Nsig, const R* Sig, R L, R w1, R w2) {
     R g1 = G_full(M, Nsig, Sig, L, w1);
     R g2 = G_full(M, Nsig, Sig, L, w2);
     return g1 * g2 / two_pi<R>();
@@ -341,8 +368,8 @@ __device__ __forceinline__ R prop_plain(const SMesh<R>& M, int Nsig, const R* Si
 
 // one half of the bubble propagator of channel ch at node v and transfer W
 // (flow_su2_{s,t,u}.jl: first lines of every kernel, bubbles.jl:99-221)
-template <typename R>
-__device__ __forceinline__ R prop_half(int kind, int half, int ch, const SMesh<R>& M, int Nsig, const R* Sig,
+template <typename R, typename MV>
+__device__ __forceinline__ R prop_half(int kind, int half, int ch, const MV& M, int Nsig, const R* Sig,
                                        const R* dSig, R L, R v, R W) {
     R w1, w2;
     const R hW = (R)0.5 * W;

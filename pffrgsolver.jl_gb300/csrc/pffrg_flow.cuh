@@ -313,7 +313,7 @@ __device__ __forceinline__ TaskInfo task_of(const PassArgs<R>& A, int sub, int j
 template <typename R, int T, int SPL, int C>
 struct Team {
     const PassArgs<R>& A;
-    const SMesh<R>& M;
+    const MeshG<double>& M;  // FP64 meshes of the node setup
     TeamScratch<R, T, C, SPL>& ts;
     R* tmp;                 // t channel: [2 C][Ns] slot values of the current node
     const unsigned* rows;   // packed overlap rows (shared or global)
@@ -325,7 +325,7 @@ struct Team {
     // Evaluate the integrand of channel X at up to NB nodes x[0..count) of one task:
     // g[j][c][k] = Γ_c(site tl + k T; x_j).  Team-collective: all lanes of the warp call it
     // together (inactive teams with count = 0).
-    __device__ void eval(const TaskInfo& ti, R W, R V, R VP, const double* x, int count,
+    __device__ void eval(const TaskInfo& ti, double W, double V, double VP, const double* x, int count,
                          R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
         const int X = ti.X;
         const int Ns = A.L.Ns;
@@ -342,16 +342,17 @@ struct Team {
         for (int it = tl; it < count * nitems; it += T) {
             const int j = it / nitems, item = it - j * nitems;
             NodeScratch<R, C>& ns = ts.node[j];
-            const R v = (R)x[j];
+            const double v = x[j];
             if (item < nprop) {
-                ns.p_half[item] = prop_half<R>(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a, A.prop_da, (R)A.Lam, v, W);
+                ns.p_half[item] =
+                    (R)prop_half<double>(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a64, A.prop_da64, A.Lam, v, W);
             } else {
                 const int k = item - nprop;
                 const int slot = k / 3, ch = k - 3 * slot;
                 Plan<R>& P = ns.plan[slot][ch];
                 if (A.mask[X][slot] & (1 << ch)) {
-                    R a0, a1, a2;
-                    slot_arg<R>(X, slot, ch, v, W, V, VP, a0, a1, a2);
+                    double a0, a1, a2;
+                    slot_arg<double>(X, slot, ch, v, W, V, VP, a0, a1, a2);
                     make_plan<R>(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
                 } else {
                     P.kernel = 0;
@@ -656,11 +657,11 @@ __device__ __forceinline__ void enqueue(WaveSpace& Wsp, int par, int sub, long l
 }
 
 template <typename R>
-__device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const SMesh<R>& M, const TaskInfo& ti, R& W, R& V,
-                                           R& VP) {
-    const R* Om = (ti.X == 1) ? M.Ot : M.Os;
-    const R* nu = (ti.X == 1) ? M.nt : M.ns;
-    const R inf = (R)INFINITY;
+__device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const MeshG<double>& M, const TaskInfo& ti, double& W,
+                                           double& V, double& VP) {
+    const double* Om = (ti.X == 1) ? M.Ot : M.Os;
+    const double* nu = (ti.X == 1) ? M.nt : M.ns;
+    const double inf = INFINITY;
     W = Om[ti.w1];
     V = (ti.kernel == 2 || ti.kernel == 4) ? nu[ti.w2] : inf;
     VP = (ti.kernel == 3 || ti.kernel == 4) ? nu[ti.w3] : inf;
@@ -677,8 +678,8 @@ struct SmemLayout {
     }
     size_t mesh, teams, tmp, rows, total;
     __host__ __device__ SmemLayout(int Ns, long long R_rows, bool rows_in_smem) {
-        mesh = 0;
-        teams = mesh + sizeof(SMesh<R>);
+        mesh = 0;  // the meshes are read from global memory
+        teams = 0;
         tmp = (teams + sizeof(TeamScratch<R, T, C, SPL>) * kWarps * NPW + 15) & ~(size_t)15;  // 16-byte loads
         rows = tmp + ((sizeof(R) * (size_t)kWarps * NPW * tmp_per_team(Ns) + 15) & ~(size_t)15);
         total = rows + (rows_in_smem ? sizeof(unsigned) * (size_t)(R_rows + Ns + 1) : 0);
@@ -687,7 +688,7 @@ struct SmemLayout {
 
 template <typename R, int T, int SPL, int C>
 __device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, unsigned char* smem,
-                                                        const SMesh<R>& M, int warp, int team, int tl) {
+                                                        const MeshG<double>& M, int warp, int team, int tl) {
     constexpr int NPW = 32 / T;
     const int Ns = A.L.Ns;
     SmemLayout<R, T, C, SPL> lay(Ns, A.rows_total, A.rows_in_smem);
@@ -713,8 +714,6 @@ __device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, un
 
 template <typename R, int T, int C, int SPL>
 __device__ __forceinline__ void load_common(const PassArgs<R>& A, unsigned char* smem) {
-    SMesh<R>& M = *reinterpret_cast<SMesh<R>*>(smem);
-    load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     if (A.rows_in_smem) {
         SmemLayout<R, T, C, SPL> lay(A.L.Ns, A.rows_total, true);
         unsigned* rows = reinterpret_cast<unsigned*>(smem + lay.rows);
@@ -839,7 +838,7 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
     load_common<R, T, C, SPL>(A, smem);
-    const SMesh<R>& M = *reinterpret_cast<const SMesh<R>*>(smem);
+    const MeshG<double> M = mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
     Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
@@ -880,7 +879,7 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
                 cnt = 5;
             }
         }
-        R W = 0, V = 0, VP = 0;
+        double W = 0, V = 0, VP = 0;
         if (valid) task_freqs(A, M, ti, W, V, VP);
         // all teams of the warp evaluate together (cnt = 0 for idle teams), NB nodes at a time
         R g[5][C][SPL];
@@ -997,7 +996,7 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
     // blocks without a chunk leave before staging the meshes and rows
     if ((long long)blockIdx.x * kWarps * NPW >= Wsp.counters[par]) return;
     load_common<R, T, C, SPL>(A, smem);
-    const SMesh<R>& M = *reinterpret_cast<const SMesh<R>*>(smem);
+    const MeshG<double> M = mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
     Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
@@ -1013,7 +1012,7 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
         int4 cr = make_int4(0, 0, 0, 0);
         TaskInfo ti{0, 1, 0, 0, 0};
         double lo = 0, h = 0, sgn = 1;
-        R W = 0, V = 0, VP = 0;
+        double W = 0, V = 0, VP = 0;
         if (valid) {
             cr = Wsp.queue[par][chunk];
             const SubRec S = Wsp.subs[cr.x];

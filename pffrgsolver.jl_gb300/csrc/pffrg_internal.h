@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "pffrg_device.cuh"
 
 namespace pffrg {
@@ -30,13 +32,15 @@ struct PassArgs {
     int prop_kind;
     const R* prop_a;   // Σ of the propagators
     const R* prop_da;  // dΣ of the Katanin propagator
+    const double* prop_a64;   // the same in FP64: the node setup (propagators, plans) is FP64
+    const double* prop_da64;
     double* out;       // FP64 output action
     const int* exch;
     const int* ov_off;       // [Ns+1]
     const unsigned* ov_rows; // [R] site a | site b << 8 | multiplicity << 16
     long long rows_total;
     int rows_in_smem;        // stage the rows in shared memory
-    const double* mesh;
+    const double* mesh;   // [σ | Ωs | νs | Ωt | νt] then their inverse spacings (FP64)
     const double* corrs;  // [2,3,NO]
     const double* log_bounds;  // [mesh s/u = 0, t = 1][w1][k = 0..eval]: ξ^k a of integrate_log!
     const int4* tasks;    // (kernel 1..4, w1, w2, w3), 0-based frequency indices
@@ -84,6 +88,17 @@ struct WaveSpace {
 };
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// append the inverse spacings 1 / (x[k+1] - x[k]) (0 at the last entry) of the five meshes of a
+// device mesh block [σ | Ωs | νs | Ωt | νt] to the block
+inline void append_inverse_spacings(std::vector<double>& h, int Nsig, int NO, int Nn) {
+    const int len[5] = {Nsig, NO, Nn, NO, Nn};
+    size_t o = 0;
+    for (int a = 0; a < 5; ++a) {
+        for (int k = 0; k < len[a]; ++k) h.push_back(k + 1 < len[a] ? 1.0 / (h[o + k + 1] - h[o + k]) : 0.0);
+        o += len[a];
+    }
+}
 
 // bytes of the wave workspace for nsub subdomains, C components on Ns sites and qcap chunks
 inline size_t wave_space_bytes(long long nsub, int Ns, long long qcap, int C) {

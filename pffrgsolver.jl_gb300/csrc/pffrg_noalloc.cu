@@ -123,6 +123,7 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     hmesh.insert(hmesh.end(), mesh->nu_s, mesh->nu_s + Nn);
     hmesh.insert(hmesh.end(), mesh->omega_t, mesh->omega_t + NO);
     hmesh.insert(hmesh.end(), mesh->nu_t, mesh->nu_t + Nn);
+    append_inverse_spacings(hmesh, L.Nsig, NO, Nn);
     // channel tasks with w2 >= w3 (compute.jl:73-107), 0-based
     std::vector<int4> tasks;
     for (int w1 = 0; w1 < NO; ++w1) {
@@ -215,6 +216,8 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     p.prop_kind = PROP_KAT;
     p.prop_a = a_dev;
     p.prop_da = da_dev;
+    p.prop_a64 = a_dev;
+    p.prop_da64 = da_dev;
     p.out = da_dev;
     p.exch = reinterpret_cast<const int*>(base + o_exch);
     p.ov_off = reinterpret_cast<const int*>(base + o_off);
