@@ -29,6 +29,7 @@ struct pffrg_ctx {
     DevLattice lat;
     double* mesh = nullptr;  // [σ|Ωs|νs|Ωt|νt]
     double* mesh_new = nullptr;  // the next step's meshes during a resampling
+    float* mesh_ff = nullptr;    // float-float meshes of the mixed path's node setup
     long long* scan_arg = nullptr;  // [3 C] argmax of |q3| per component and channel
     double* scan_cuts = nullptr;    // [3 C][NO + 3 Nn] cuts through the maxima
     double* slot[PFFRG_NUM_SLOTS] = {};
@@ -45,6 +46,7 @@ struct pffrg_ctx {
     const float* f_copy[4] = {nullptr, nullptr, nullptr, nullptr};
     const double* f_src[4] = {nullptr, nullptr, nullptr, nullptr};
     double esc_eps = 1e-5;  // FP64 hand-off margin of the mixed path (0: off)
+    long long chi_cluster_min = 32768;  // χ region capacity from which a cluster runs each integral
     std::vector<double> h_mesh;    // host copy of [σ|Ωs|νs|Ωt|νt]
     double* log_bounds = nullptr;  // [2][NO][eval+1]
     int bounds_cap = 0;            // eval the buffer holds
@@ -173,8 +175,10 @@ int upload_mesh(pffrg_ctx* ctx, const pffrg_mesh_view* m) {
     h.insert(h.end(), m->omega_t, m->omega_t + m->num_omega);
     h.insert(h.end(), m->nu_t, m->nu_t + m->num_nu);
     ctx->h_mesh = h;
+    const std::vector<float> hf = mesh_block_ff(h, ctx->L.Nsig, ctx->L.NO, ctx->L.Nn);
     append_inverse_spacings(h, ctx->L.Nsig, ctx->L.NO, ctx->L.Nn);
     CK(cudaMemcpyAsync(ctx->mesh, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->mesh_ff, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return 0;
 }
@@ -371,6 +375,7 @@ PassArgs<R> base_pass(pffrg_ctx* ctx, double Lam, int eval, double atol, double 
     p.rows_total = ctx->lat.rows;
     p.rows_in_smem = 0;
     p.mesh = ctx->mesh;
+    p.mesh_ff = ctx->mesh_ff;
     p.log_bounds = ctx->log_bounds;
     p.corrs = ctx->corrs;
     p.Lam = Lam;
@@ -612,7 +617,7 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
             ++ctx->launches;
             // the integrals that outgrew the first capacities are few and long: a cluster of
             // blocks evaluates each round's regions of one integral
-            CK(launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, cap >= 32768 ? 8 : 1, ctx->st));
+            CK(launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, cap >= ctx->chi_cluster_min ? 8 : 1, ctx->st));
             over.resize(nb);
             CK(cudaMemcpyAsync(over.data(), ctx->chi_over, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->st));
             CK(cudaStreamSynchronize(ctx->st));
@@ -837,7 +842,7 @@ void pffrg_destroy(pffrg_ctx* ctx) {
                     ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
                     ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red, ctx->chi_reg, ctx->chi_split,
                     ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over, ctx->chi_ctl, ctx->gk_seg,
-                    ctx->mesh_new, ctx->scan_arg, ctx->scan_cuts};
+                    ctx->mesh_new, ctx->mesh_ff, ctx->scan_arg, ctx->scan_cuts};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
@@ -920,6 +925,7 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
               dalloc((void**)&ctx->lat.ov_off, sizeof(int) * (Ns + 1)) &&
               dalloc((void**)&ctx->lat.ov_rows, sizeof(unsigned) * rows.size()) &&
               dalloc((void**)&ctx->mesh, 2 * sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
+              dalloc((void**)&ctx->mesh_ff, 3 * sizeof(float) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
               dalloc((void**)&ctx->mesh_new, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
               dalloc((void**)&ctx->scan_arg, sizeof(long long) * 3 * L.C) &&
               dalloc((void**)&ctx->scan_cuts, sizeof(double) * 3 * L.C * (L.NO + 3 * L.Nn));
@@ -1356,6 +1362,13 @@ int pffrg_set_fp64_handoff(pffrg_ctx* ctx, double eps) {
     if (!ctx) return PFFRG_E_ARGS;
     if (!(eps >= 0.0) || eps >= 1.0) return ctx->fail(PFFRG_E_ARGS, "hand-off margin must be in [0, 1)");
     ctx->esc_eps = eps;
+    return 0;
+}
+
+int pffrg_set_chi_cluster(pffrg_ctx* ctx, int64_t min_regions) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (min_regions < 0) return ctx->fail(PFFRG_E_ARGS, "negative region count");
+    ctx->chi_cluster_min = min_regions;
     return 0;
 }
 

@@ -389,4 +389,212 @@ __device__ __forceinline__ R prop_half(int kind, int half, int ch, const MV& M, 
     return -prop_plain(M, Nsig, Sig, L, w1, w2);
 }
 
+// ---------------------------------------------------------------------------
+// Node setup of the mixed path in float-float arithmetic.  An interpolation weight is
+// (x[k+1] - arg) / (x[k+1] - x[k]); with arg and x rounded to FP32 its error is the FP32 rounding
+// of |arg| divided by the mesh spacing, up to ~N ulps on a mesh of N points — the dominant error
+// of an FP32 integrand (measured 2e-6 of max|dΓ|).  The mixed path therefore carries the node,
+// the transfer frequencies and the meshes as unevaluated sums h + l of two floats (error-free
+// two-sum additions), searches the interval on the pair and forms the weight from the pairwise
+// difference: weights accurate to FP32 rounding of the weight itself, in FP32 instructions only
+// (FP64 arithmetic is slow on this GPU).
+// ---------------------------------------------------------------------------
+struct FF {
+    float h, l;
+    FF() = default;
+    __host__ __device__ constexpr FF(float hi, float lo) : h(hi), l(lo) {}
+    // the pair nearest to x (infinities keep l = 0)
+    __device__ explicit FF(double x) : h((float)x), l(isinf((float)x) ? 0.f : (float)(x - (double)(float)x)) {}
+};
+
+__device__ __forceinline__ FF ff_norm(float s, float t) {  // fast two-sum of s + t, |s| >= |t|
+    const float h = __fadd_rn(s, t);
+    return FF{h, __fsub_rn(t, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ FF operator+(FF a, FF b) {
+    const float s = __fadd_rn(a.h, b.h);
+    if (isinf(s)) return FF{s, 0.f};
+    const float bb = __fsub_rn(s, a.h);
+    const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    return ff_norm(s, __fadd_rn(__fadd_rn(e, a.l), b.l));
+}
+__device__ __forceinline__ FF operator-(FF a) { return FF{-a.h, -a.l}; }
+__device__ __forceinline__ FF operator-(FF a, FF b) { return a + (-b); }
+// scaling by a power of two (the 1/2 of the argument formulas): exact
+__device__ __forceinline__ FF operator*(FF s, FF a) { return FF{s.h * a.h, s.h * a.l}; }
+__device__ __forceinline__ bool operator<(FF a, FF b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+__device__ __forceinline__ bool operator<(FF a, float b) { return a.h < b || (a.h == b && a.l < 0.f); }
+__device__ __forceinline__ FF ff_abs(FF a) { return a < 0.f ? -a : a; }
+
+// Mesh block of the mixed path (floats): [h | l | inverse spacing], each [σ | Ωs | νs | Ωt | νt]
+struct MeshFF {
+    const float* h;
+    const float* l;
+    const float* inv;
+    int Nsig, NO, Nn;
+    __device__ __forceinline__ int sig() const { return 0; }
+    __device__ __forceinline__ int Os() const { return Nsig; }
+    __device__ __forceinline__ int ns() const { return Nsig + NO; }
+    __device__ __forceinline__ int Ot() const { return Nsig + NO + Nn; }
+    __device__ __forceinline__ int nt() const { return Nsig + 2 * NO + Nn; }
+    __device__ __forceinline__ FF at(int o, int k) const { return FF{h[o + k], l[o + k]}; }
+};
+
+__device__ __forceinline__ MeshFF mesh_view_ff(const float* block, int Nsig, int NO, int Nn) {
+    const int n = Nsig + 2 * NO + 2 * Nn;
+    return MeshFF{block, block + n, block + 2 * n, Nsig, NO, Nn};
+}
+
+// get_indices + get_param (param.jl:26-87) on the mesh at offset o of length n, as get_param
+__device__ __forceinline__ Param<float> get_param_ff(FF val, const MeshFF& M, int o, int n) {
+    Param<float> p;
+    if (!(val < M.at(o, n - 1))) {
+        p.lo = p.hi = n - 1;
+        p.wl = 1.f;
+        p.wu = 0.f;
+        return p;
+    }
+    int lo = 0, hi = n - 1;
+    if (!(val.h == val.h)) hi = 0;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (!(M.at(o, mid) < val)) hi = mid;
+        else lo = mid + 1;
+    }
+    p.hi = lo;
+    p.lo = (val < M.at(o, lo)) ? lo - 1 : lo;
+    if (p.lo < 0) p.lo = 0;
+    if (p.lo < p.hi) {
+        const float d = M.inv[o + p.lo];
+        const FF xh = M.at(o, p.hi), xl = M.at(o, p.lo);
+        p.wl = d * __fadd_rn(__fsub_rn(xh.h, val.h), __fsub_rn(xh.l, val.l));
+        p.wu = d * __fadd_rn(__fsub_rn(val.h, xl.h), __fsub_rn(val.l, xl.l));
+    } else {
+        p.wl = 1.f;
+        p.wu = 0.f;
+    }
+    return p;
+}
+
+// make_plan with float-float arguments (same sign folding, kernel choice and corner order)
+__device__ __forceinline__ void make_plan_ff(Plan<float>& P, int chan, FF w, FF v, FF vp, const MeshFF& M, int Ns,
+                                             int NO, int Nn) {
+    bool ex = false, mp = false, smn = false, sm = false, sn = false;
+    if (chan == 0) {  // get_buffer_s (buffer.jl:87-124)
+        if (w < 0.f) { w = -w; ex = !ex; }
+        if (v < 0.f) { v = -v; ex = !ex; mp = !mp; sm = !sm; }
+        if (vp < 0.f) { vp = -vp; mp = !mp; sn = !sn; }
+    } else if (chan == 1) {  // get_buffer_t (buffer.jl:126-160)
+        if (w < 0.f) { w = -w; smn = !smn; }
+        if (v < 0.f) { v = -v; sm = !sm; }
+        if (vp < 0.f) { vp = -vp; sn = !sn; }
+    } else {  // get_buffer_u (buffer.jl:162-199)
+        if (w < 0.f) { w = -w; ex = !ex; smn = !smn; }
+        if (v < 0.f) { v = -v; ex = !ex; mp = !mp; sn = !sn; }
+        if (vp < 0.f) { vp = -vp; mp = !mp; sn = !sn; }
+    }
+    const int oO = chan == 1 ? M.Ot() : M.Os();
+    const int on = chan == 1 ? M.nt() : M.ns();
+    if (M.at(oO, NO - 1) < w) {  // get_buffer (buffer.jl:51-84): beyond the bosonic mesh
+        P.kernel = 0;
+        return;
+    }
+    P.exch = ex ? 1 : 0;
+    P.flags = (smn ? 1 : 0) | (sm ? 2 : 0) | (sn ? 4 : 0);
+    P.src_ch = (chan == 1) ? 1 : ((chan == 0) == mp ? 2 : 0);
+    P.sgn_d = ((sm ? -1 : 1) * (sn ? -1 : 1)) < 0 ? -1.f : 1.f;
+    const Param<float> p1 = get_param_ff(w, M, oO, NO);
+    const FF numax = M.at(on, Nn - 1);
+    const bool vin = !(numax < v);
+    const bool vpin = !(numax < vp);
+    if (!vin && !vpin) {
+        P.kernel = 1;
+        P.w[0] = p1.wl;
+        P.w[1] = p1.wu;
+        P.off[0] = Ns * p1.lo;
+        P.off[1] = Ns * p1.hi;
+    } else if (vin != vpin) {
+        P.kernel = vin ? 2 : 3;
+        const Param<float> pb = get_param_ff(vin ? v : vp, M, on, Nn);
+        P.w[0] = p1.wl * pb.wl;
+        P.w[1] = p1.wu * pb.wl;
+        P.w[2] = p1.wl * pb.wu;
+        P.w[3] = p1.wu * pb.wu;
+        P.off[0] = Ns * (p1.lo + NO * pb.lo);
+        P.off[1] = Ns * (p1.hi + NO * pb.lo);
+        P.off[2] = Ns * (p1.lo + NO * pb.hi);
+        P.off[3] = Ns * (p1.hi + NO * pb.hi);
+    } else {
+        P.kernel = 4;
+        const Param<float> p2 = get_param_ff(v, M, on, Nn);
+        const Param<float> p3 = get_param_ff(vp, M, on, Nn);
+        const int NON = NO * Nn;
+        P.w[0] = p1.wl * p2.wl * p3.wl;
+        P.w[1] = p1.wu * p2.wl * p3.wl;
+        P.w[2] = p1.wl * p2.wu * p3.wl;
+        P.w[3] = p1.wu * p2.wu * p3.wl;
+        P.w[4] = p1.wl * p2.wl * p3.wu;
+        P.w[5] = p1.wu * p2.wl * p3.wu;
+        P.w[6] = p1.wl * p2.wu * p3.wu;
+        P.w[7] = p1.wu * p2.wu * p3.wu;
+        P.off[0] = Ns * (p1.lo + NO * p2.lo + NON * p3.lo);
+        P.off[1] = Ns * (p1.hi + NO * p2.lo + NON * p3.lo);
+        P.off[2] = Ns * (p1.lo + NO * p2.hi + NON * p3.lo);
+        P.off[3] = Ns * (p1.hi + NO * p2.hi + NON * p3.lo);
+        P.off[4] = Ns * (p1.lo + NO * p2.lo + NON * p3.hi);
+        P.off[5] = Ns * (p1.hi + NO * p2.lo + NON * p3.hi);
+        P.off[6] = Ns * (p1.lo + NO * p2.hi + NON * p3.hi);
+        P.off[7] = Ns * (p1.hi + NO * p2.hi + NON * p3.hi);
+    }
+}
+
+// get_Σ with the interval weight from the float-float frequency
+__device__ __forceinline__ float get_sigma_ff(const MeshFF& M, int Nsig, const float* __restrict__ Sig, FF w) {
+    const FF aw = ff_abs(w);
+    const FF smax = M.at(M.sig(), Nsig - 1);
+    if (!(smax < aw)) {
+        const Param<float> p = get_param_ff(aw, M, M.sig(), Nsig);
+        return jl_sign(w.h) * (p.wl * ldg(Sig + p.lo) + p.wu * ldg(Sig + p.hi));
+    }
+    return smax.h * ldg(Sig + Nsig - 1) / w.h;
+}
+
+__device__ __forceinline__ float G_full_ff(const MeshFF& M, int Nsig, const float* Sig, float L, FF w) {
+    if (fabsf(w.h) > 1e-8f) {
+        const float s = get_sigma_ff(M, Nsig, Sig, w);
+        const float g0 = G_bare(L, w.h);
+        const float den = (w.h * s >= 0.f) ? 1.f / g0 + s : 1.f / g0;
+        return 1.f / den;
+    }
+    return 0.f;
+}
+
+// prop_half with float-float frequencies (bubbles.jl:64-96)
+__device__ __forceinline__ float prop_half_ff(int kind, int half, int ch, const MeshFF& M, int Nsig, const float* Sig,
+                                              const float* dSig, float L, FF v, FF W) {
+    const FF hW = FF{0.5f, 0.f} * W;
+    FF w1, w2;
+    if (ch == 0) {
+        w1 = v + hW;
+        w2 = hW - v;
+    } else if (ch == 1) {
+        w1 = v + hW;
+        w2 = v - hW;
+    } else {
+        w1 = v - hW;
+        w2 = v + hW;
+    }
+    if (kind == 0) {
+        const FF a = half == 0 ? w1 : w2, b = half == 0 ? w2 : w1;
+        const float ds = get_sigma_ff(M, Nsig, dSig, a);
+        const float g1 = G_full_ff(M, Nsig, Sig, L, a);
+        const float g0 = G_bare(L, a.h);
+        const float r = g1 / g0;
+        const float s1 = fabsf(a.h) > 1e-8f ? r * r * expf(-(a.h * a.h) / (L * L)) * 2.f * a.h / (L * L * L) : 0.f;
+        const float g2 = G_full_ff(M, Nsig, Sig, L, b);
+        return (s1 + g1 * g1 * ds) * g2 / two_pi<float>();
+    }
+    return -(G_full_ff(M, Nsig, Sig, L, w1) * G_full_ff(M, Nsig, Sig, L, w2)) / two_pi<float>();
+}
+
 }  // namespace pffrg

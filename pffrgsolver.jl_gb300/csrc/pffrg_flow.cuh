@@ -313,7 +313,10 @@ __device__ __forceinline__ TaskInfo task_of(const PassArgs<R>& A, int sub, int j
 template <typename R, int T, int SPL, int C>
 struct Team {
     const PassArgs<R>& A;
-    const MeshG<double>& M;  // FP64 meshes of the node setup
+    // node setup: FP64 on the FP64 path, float-float on the mixed path
+    using SetupT = typename std::conditional<sizeof(R) == 4, FF, double>::type;
+    using SetupMesh = typename std::conditional<sizeof(R) == 4, MeshFF, MeshG<double>>::type;
+    const SetupMesh& M;
     TeamScratch<R, T, C, SPL>& ts;
     R* tmp;                 // t channel: [2 C][Ns] slot values of the current node
     const unsigned* rows;   // packed overlap rows (shared or global)
@@ -325,7 +328,7 @@ struct Team {
     // Evaluate the integrand of channel X at up to NB nodes x[0..count) of one task:
     // g[j][c][k] = Γ_c(site tl + k T; x_j).  Team-collective: all lanes of the warp call it
     // together (inactive teams with count = 0).
-    __device__ void eval(const TaskInfo& ti, double W, double V, double VP, const double* x, int count,
+    __device__ void eval(const TaskInfo& ti, SetupT W, SetupT V, SetupT VP, const double* x, int count,
                          R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
         const int X = ti.X;
         const int Ns = A.L.Ns;
@@ -342,18 +345,23 @@ struct Team {
         for (int it = tl; it < count * nitems; it += T) {
             const int j = it / nitems, item = it - j * nitems;
             NodeScratch<R, C>& ns = ts.node[j];
-            const double v = x[j];
+            const SetupT v = SetupT(x[j]);
             if (item < nprop) {
-                ns.p_half[item] =
-                    (R)prop_half<double>(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a64, A.prop_da64, A.Lam, v, W);
+                if constexpr (sizeof(R) == 4)
+                    ns.p_half[item] = prop_half_ff(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a, A.prop_da,
+                                                   (float)A.Lam, v, W);
+                else
+                    ns.p_half[item] = prop_half<double>(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a64, A.prop_da64,
+                                                        A.Lam, v, W);
             } else {
                 const int k = item - nprop;
                 const int slot = k / 3, ch = k - 3 * slot;
                 Plan<R>& P = ns.plan[slot][ch];
                 if (A.mask[X][slot] & (1 << ch)) {
-                    double a0, a1, a2;
-                    slot_arg<double>(X, slot, ch, v, W, V, VP, a0, a1, a2);
-                    make_plan<R>(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
+                    SetupT a0, a1, a2;
+                    slot_arg<SetupT>(X, slot, ch, v, W, V, VP, a0, a1, a2);
+                    if constexpr (sizeof(R) == 4) make_plan_ff(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
+                    else make_plan<R>(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
                 } else {
                     P.kernel = 0;
                 }
@@ -656,6 +664,24 @@ __device__ __forceinline__ void enqueue(WaveSpace& Wsp, int par, int sub, long l
     Wsp.active[par][a] = sub;
 }
 
+// the meshes of the node setup: FP64 for the FP64 path, float-float pairs for the mixed path
+template <typename R>
+__device__ __forceinline__ auto setup_mesh(const PassArgs<R>& A) {
+    if constexpr (sizeof(R) == 4) return mesh_view_ff(A.mesh_ff, A.L.Nsig, A.L.NO, A.L.Nn);
+    else return mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+}
+
+template <typename R>
+__device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const MeshFF& M, const TaskInfo& ti, FF& W, FF& V,
+                                           FF& VP) {
+    const int oO = (ti.X == 1) ? M.Ot() : M.Os();
+    const int on = (ti.X == 1) ? M.nt() : M.ns();
+    const FF inf{INFINITY, 0.f};
+    W = M.at(oO, ti.w1);
+    V = (ti.kernel == 2 || ti.kernel == 4) ? M.at(on, ti.w2) : inf;
+    VP = (ti.kernel == 3 || ti.kernel == 4) ? M.at(on, ti.w3) : inf;
+}
+
 template <typename R>
 __device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const MeshG<double>& M, const TaskInfo& ti, double& W,
                                            double& V, double& VP) {
@@ -688,7 +714,8 @@ struct SmemLayout {
 
 template <typename R, int T, int SPL, int C>
 __device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, unsigned char* smem,
-                                                        const MeshG<double>& M, int warp, int team, int tl) {
+                                                        const typename Team<R, T, SPL, C>::SetupMesh& M, int warp,
+                                                        int team, int tl) {
     constexpr int NPW = 32 / T;
     const int Ns = A.L.Ns;
     SmemLayout<R, T, C, SPL> lay(Ns, A.rows_total, A.rows_in_smem);
@@ -838,7 +865,7 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
     load_common<R, T, C, SPL>(A, smem);
-    const MeshG<double> M = mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+    const auto M = setup_mesh(A);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
     Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
@@ -879,7 +906,7 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
                 cnt = 5;
             }
         }
-        double W = 0, V = 0, VP = 0;
+        typename Team<R, T, SPL, C>::SetupT W(0.0), V(0.0), VP(0.0);
         if (valid) task_freqs(A, M, ti, W, V, VP);
         // all teams of the warp evaluate together (cnt = 0 for idle teams), NB nodes at a time
         R g[5][C][SPL];
@@ -984,8 +1011,9 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
 }
 
 // ---- wave k >= 1: evaluate queued chunks, one partial node sum per chunk ----
+// (FP32 kernels held to 128 registers: four blocks of 128 threads per SM)
 template <typename R, int T, int SPL, int C>
-__global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
+__global__ void __launch_bounds__(kWarps * 32, sizeof(R) == 4 ? 4 : 1) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -996,7 +1024,7 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
     // blocks without a chunk leave before staging the meshes and rows
     if ((long long)blockIdx.x * kWarps * NPW >= Wsp.counters[par]) return;
     load_common<R, T, C, SPL>(A, smem);
-    const MeshG<double> M = mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+    const auto M = setup_mesh(A);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
     Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
@@ -1012,7 +1040,7 @@ __global__ void __launch_bounds__(kWarps * 32) eval_kernel(PassArgs<R> A, WaveSp
         int4 cr = make_int4(0, 0, 0, 0);
         TaskInfo ti{0, 1, 0, 0, 0};
         double lo = 0, h = 0, sgn = 1;
-        double W = 0, V = 0, VP = 0;
+        typename Team<R, T, SPL, C>::SetupT W(0.0), V(0.0), VP(0.0);
         if (valid) {
             cr = Wsp.queue[par][chunk];
             const SubRec S = Wsp.subs[cr.x];

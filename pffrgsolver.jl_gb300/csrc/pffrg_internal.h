@@ -41,6 +41,7 @@ struct PassArgs {
     long long rows_total;
     int rows_in_smem;        // stage the rows in shared memory
     const double* mesh;   // [σ | Ωs | νs | Ωt | νt] then their inverse spacings (FP64)
+    const float* mesh_ff; // the same as float pairs h, l and FP32 inverse spacings (mixed path)
     const double* corrs;  // [2,3,NO]
     const double* log_bounds;  // [mesh s/u = 0, t = 1][w1][k = 0..eval]: ξ^k a of integrate_log!
     const int4* tasks;    // (kernel 1..4, w1, w2, w3), 0-based frequency indices
@@ -88,6 +89,26 @@ struct WaveSpace {
 };
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// float-float form of a mesh block [σ | Ωs | νs | Ωt | νt] (without inverses): the high floats,
+// the low floats (x - h) and the FP32 inverse spacings
+inline std::vector<float> mesh_block_ff(const std::vector<double>& x, int Nsig, int NO, int Nn) {
+    const int len[5] = {Nsig, NO, Nn, NO, Nn};
+    const size_t n = (size_t)Nsig + 2 * NO + 2 * Nn;
+    std::vector<float> f(3 * n);
+    size_t o = 0;
+    for (int a = 0; a < 5; ++a) {
+        for (int k = 0; k < len[a]; ++k) {
+            const double v = x[o + k];
+            const float h = (float)v;
+            f[o + k] = h;
+            f[n + o + k] = (float)(v - (double)h);
+            f[2 * n + o + k] = k + 1 < len[a] ? (float)(1.0 / (x[o + k + 1] - v)) : 0.f;
+        }
+        o += len[a];
+    }
+    return f;
+}
 
 // append the inverse spacings 1 / (x[k+1] - x[k]) (0 at the last entry) of the five meshes of a
 // device mesh block [σ | Ωs | νs | Ωt | νt] to the block
