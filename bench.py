@@ -54,6 +54,10 @@ def parse():
     p.add_argument("--no-flow", action="store_true", help="skip the full-flow leg")
     p.add_argument("--flow-final", type=float, default=0.01, help="final cutoff of the full-flow leg")
     p.add_argument("--flow-precisions", default="mixed,fp64", help="precisions of the full-flow leg")
+    p.add_argument("--sweep", type=int, default=0,
+                   help="instances of the coupling-sweep leg (square J1-J2, L in 3,4,5,6,8; 0: skip)")
+    p.add_argument("--warm-start", default="",
+                   help="train,test counts of the learned parquet warm-start leg (honeycomb J1-J2-J3; empty: skip)")
     return p.parse_args()
 
 
@@ -309,6 +313,8 @@ def ours(args):
     flow = None
     if world == 1 and not args.no_flow:
         flow = flow_leg(args, local)
+    sweep = sweep_leg(args, local) if world == 1 and args.sweep > 0 else None
+    warm = warm_start_leg(args, local) if world == 1 and args.warm_start else None
     # CPU baseline (oracle, all host cores, bounded strided sample), rank 0 at N=1 only
     cpu = None
     if world == 1 and not args.no_cpu:
@@ -335,6 +341,8 @@ def ours(args):
                  "mixed_speedup": fp64_ms / ms_step} if fp64_ms else None,
         "mixed_vs_fp64_rel_err": err_mixed,
         "full_flow": flow,
+        "sweep": sweep,
+        "warm_start": warm,
         "integrand_evals_per_step": evals_step,
         "clocks": clk,
     }
@@ -383,6 +391,74 @@ def flow_leg(args, dev_index):
                 errs[str(L)] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
         out["chi_static_rel_err_mixed_vs_fp64"] = errs
     return out
+
+
+SWEEP = dict(num_sigma=30, num_omega=10, num_nu=8, num_chi=6, initial=50.0, final=0.1, ode_tol=(1e-3, 1e-3),
+             parquet=False)
+
+
+def sweep_leg(args, dev_index):
+    """Config 3: n square-lattice J1-J2 Heisenberg flows (J2 ~ U[0, 1], seed 2; L = 3, 4, 5, 6, 8 round
+    robin), mixed precision, all on one GPU from concurrent streams; against the same instances run one
+    after the other, with the on-site χ(ω=0) of each concurrent run against its single run."""
+    from pffrg_gb300.launcher import launch
+    from pffrg_gb300.sweep import launch_sweep, square_j1j2_sweep
+
+    inst = square_j1j2_sweep(args.sweep)
+    t0 = time.perf_counter()
+    res = launch_sweep(inst, workers=16, device=dev_index, precision="mixed", **SWEEP)
+    t_sweep = time.perf_counter() - t0
+    n_ref = min(len(inst), 8)
+    t0 = time.perf_counter()
+    ref = [launch("", i.name, i.size, i.model, i.symmetry, i.J, device=dev_index, precision="mixed", **SWEEP)
+           for i in inst[:n_ref]]
+    t_one = (time.perf_counter() - t0) / n_ref
+    errs = [float(np.max(np.abs(a.chi[-1][2][0] - b.chi[-1][2][0])) / np.max(np.abs(b.chi[-1][2][0])))
+            for a, b in zip(res, ref)]
+    return {"workload": "square J1-J2 (J2 ~ U[0,1], seed 2), L in 3,4,5,6,8, 1 loop, 30/10/8, Λ 50 -> 0.1, "
+                        "mixed, %d instances" % len(inst),
+            "seconds": t_sweep, "instances_per_s": len(inst) / t_sweep,
+            "serial_seconds_per_instance": t_one, "speedup_vs_serial": t_one * len(inst) / t_sweep,
+            "max_chi_rel_diff_vs_single_runs": max(errs) if errs else None}
+
+
+def warm_start_leg(args, dev_index):
+    """Config 4: the learned parquet warm start on honeycomb J1-J2-J3 (L=5, (J2, J3) ~ U[0, 0.5]^2, seed 3):
+    fit on `train` converged parquet vertices, then parquet iterations to the residual from the bare
+    couplings and from the prediction on `test` held-out couplings (FP64)."""
+    from pffrg_gb300.launcher import launch
+    from pffrg_gb300.warmstart import ParquetWarmStart, coupling_features, vertex_mask
+
+    n_train, n_test = (int(x) for x in args.warm_start.split(","))
+    kw = dict(num_sigma=20, num_omega=8, num_nu=6, num_chi=4, initial=5.0, final=5.0, parquet=True,
+              parquet_tol=(1e-8, 1e-8), max_iter=200, precision="fp64", correlations=False, device=dev_index)
+    rng = np.random.default_rng(3)
+    J = [[[1.0], [float(a)], [float(b)]] for a, b in rng.uniform(0.0, 0.5, size=(n_train + n_test, 2))]
+    t0 = time.perf_counter()
+    feats, verts, it_train = [], [], []
+    for j in J[:n_train]:
+        res = launch("", "honeycomb", 5, "heisenberg", "su2", j, **kw)
+        feats.append(coupling_features(j))
+        verts.append(res.action.buf[vertex_mask(res.action)].copy())
+        it_train.append(res.parquet_iterations)
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ws = ParquetWarmStart(k=16, hidden=(64, 64))
+    loss = ws.fit(feats, verts, epochs=4000, lr=3e-3)
+    t_fit = time.perf_counter() - t0
+    bare, warm, diffs = [], [], []
+    for j in J[n_train:]:
+        r0 = launch("", "honeycomb", 5, "heisenberg", "su2", j, **kw)
+        r1 = launch("", "honeycomb", 5, "heisenberg", "su2", j, warm_start=ws, **kw)
+        bare.append(r0.parquet_iterations)
+        warm.append(r1.parquet_iterations)
+        msk = vertex_mask(r0.action)
+        diffs.append(float(np.max(np.abs(r0.action.buf[msk] - r1.action.buf[msk])) / np.max(np.abs(r0.action.buf[msk]))))
+    return {"workload": "honeycomb J1-J2-J3 L=5, (J2,J3) ~ U[0,0.5]^2 seed 3, 20/8/6, Λ=5, residual 1e-8, FP64",
+            "train": n_train, "test": n_test, "data_seconds": t_data, "fit_seconds": t_fit, "fit_loss": loss,
+            "iterations_bare_mean": float(np.mean(bare)), "iterations_learned_mean": float(np.mean(warm)),
+            "iteration_ratio": float(np.mean(bare) / max(np.mean(warm), 1e-9)),
+            "max_vertex_rel_diff": max(diffs)}
 
 
 def fp64_leg(args, ctx, pkg, C, a, rhs, flush, dev, da_mixed):
