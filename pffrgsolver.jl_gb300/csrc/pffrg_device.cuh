@@ -548,6 +548,21 @@ __device__ __forceinline__ void make_plan_ff(Plan<float>& P, int chan, FF w, FF 
     }
 }
 
+// True when a float-float plan argument lies within a few FP32 ulps of a point where the vertex
+// buffers switch: zero (the sign folding of buffer.jl) or the last point of a bosonic or fermionic
+// mesh (beyond it the kernel changes; beyond the bosonic one the vertex is zero).  The FP64
+// rounding of the argument decides the side there, so such a plan is built in FP64.
+__device__ __forceinline__ bool ff_near_switch(FF a, float scale, const MeshFF& M, int NO, int Nn) {
+    const float x = fabsf(a.h);
+    if (isinf(x)) return false;
+    if (x <= 1e-9f * scale) return true;
+    const float b[4] = {M.h[M.Os() + NO - 1], M.h[M.Ot() + NO - 1], M.h[M.ns() + Nn - 1], M.h[M.nt() + Nn - 1]};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (fabsf(x - b[q]) <= 4.8e-7f * b[q]) return true;
+    return false;
+}
+
 // get_Σ with the interval weight from the float-float frequency
 __device__ __forceinline__ float get_sigma_ff(const MeshFF& M, int Nsig, const float* __restrict__ Sig, FF w) {
     const FF aw = ff_abs(w);

@@ -360,8 +360,24 @@ struct Team {
                 if (A.mask[X][slot] & (1 << ch)) {
                     SetupT a0, a1, a2;
                     slot_arg<SetupT>(X, slot, ch, v, W, V, VP, a0, a1, a2);
-                    if constexpr (sizeof(R) == 4) make_plan_ff(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
-                    else make_plan<R>(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
+                    if constexpr (sizeof(R) == 4) {
+                        const float scale = fabsf(v.h) + fabsf(W.h) + (isinf(V.h) ? 0.f : fabsf(V.h)) +
+                                            (isinf(VP.h) ? 0.f : fabsf(VP.h));
+                        if (ff_near_switch(a0, scale, M, A.L.NO, A.L.Nn) ||
+                            ff_near_switch(a1, scale, M, A.L.NO, A.L.Nn) ||
+                            ff_near_switch(a2, scale, M, A.L.NO, A.L.Nn)) {
+                            // the FP64 path's rounding decides the side of a buffer switch
+                            const MeshG<double> M64 = mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+                            double W64, V64, VP64, b0, b1, b2;
+                            task_freqs(A, M64, ti, W64, V64, VP64);
+                            slot_arg<double>(X, slot, ch, x[j], W64, V64, VP64, b0, b1, b2);
+                            make_plan<R>(P, ch, b0, b1, b2, M64, Ns, A.L.NO, A.L.Nn);
+                        } else {
+                            make_plan_ff(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
+                        }
+                    } else {
+                        make_plan<R>(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
+                    }
                 } else {
                     P.kernel = 0;
                 }
