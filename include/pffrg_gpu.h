@@ -187,9 +187,15 @@ int pffrg_autotune_team_shape(pffrg_ctx* ctx, int loops, double Lam, int a_slot,
  * bounds than eps (the relative rounding allowed for the FP32 node values)
  * could be decided the other way in FP64; such subdomains are evaluated again
  * in FP64 on the FP64 actions, so every adaptive decision of the mixed path is
- * the FP64 path's and the two differ by FP32 arithmetic only.  Default 1e-5;
+ * the FP64 path's and the two differ by FP32 arithmetic only.  Default 1e-6;
  * 0 turns the hand-off off (FP32 decisions).  No counterpart in the reference. */
 int pffrg_set_fp64_handoff(pffrg_ctx* ctx, double eps);
+
+/* χ cubature: the passes whose region capacity is at least min_regions
+ * (default 32768: the few integrals that approach the evaluation cap) run
+ * each integral on a cluster of 8 blocks instead of one block; 0 = always.
+ * Results are identical.  No counterpart in the reference. */
+int pffrg_set_chi_cluster(pffrg_ctx* ctx, int64_t min_regions);
 
 /* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86,
  * correlation_u1_dm.jl:152-190): static spin correlations χ[i, w] of the

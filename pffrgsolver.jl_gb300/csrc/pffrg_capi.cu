@@ -45,7 +45,7 @@ struct pffrg_ctx {
     // the FP64 action each FP32 copy was last made from (the FP64 pass of the mixed path reads it)
     const float* f_copy[4] = {nullptr, nullptr, nullptr, nullptr};
     const double* f_src[4] = {nullptr, nullptr, nullptr, nullptr};
-    double esc_eps = 1e-5;  // FP64 hand-off margin of the mixed path (0: off)
+    double esc_eps = 1e-6;  // FP64 hand-off margin of the mixed path (0: off)
     long long chi_cluster_min = 32768;  // χ region capacity from which a cluster runs each integral
     std::vector<double> h_mesh;    // host copy of [σ|Ωs|νs|Ωt|νt]
     double* log_bounds = nullptr;  // [2][NO][eval+1]

@@ -456,11 +456,14 @@ __device__ __forceinline__ Param<float> get_param_ff(FF val, const MeshFF& M, in
     }
     int lo = 0, hi = n - 1;
     if (!(val.h == val.h)) hi = 0;
+    // first k with h[k] >= val.h, then past an equal high part whose pair is still below val
+    // (mesh points lie more than an FP32 ulp apart)
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (!(M.at(o, mid) < val)) hi = mid;
+        if (M.h[o + mid] >= val.h) hi = mid;
         else lo = mid + 1;
     }
+    if (lo < n - 1 && M.h[o + lo] == val.h && M.l[o + lo] < val.l) ++lo;
     p.hi = lo;
     p.lo = (val < M.at(o, lo)) ? lo - 1 : lo;
     if (p.lo < 0) p.lo = 0;
@@ -563,22 +566,27 @@ __device__ __forceinline__ bool ff_near_switch(FF a, float scale, const MeshFF& 
     return false;
 }
 
-// get_Σ with the interval weight from the float-float frequency
-__device__ __forceinline__ float get_sigma_ff(const MeshFF& M, int Nsig, const float* __restrict__ Sig, FF w) {
+// get_Σ of the arrays Sig (and dSig, when given) at the float-float frequency w: one interval
+// search serves both
+__device__ __forceinline__ float get_sigma_ff(const MeshFF& M, int Nsig, const float* __restrict__ Sig, FF w,
+                                              const float* __restrict__ dSig = nullptr, float* ds = nullptr) {
     const FF aw = ff_abs(w);
     const FF smax = M.at(M.sig(), Nsig - 1);
     if (!(smax < aw)) {
         const Param<float> p = get_param_ff(aw, M, M.sig(), Nsig);
-        return jl_sign(w.h) * (p.wl * ldg(Sig + p.lo) + p.wu * ldg(Sig + p.hi));
+        const float sg = jl_sign(w.h);
+        if (dSig) *ds = sg * (p.wl * ldg(dSig + p.lo) + p.wu * ldg(dSig + p.hi));
+        return sg * (p.wl * ldg(Sig + p.lo) + p.wu * ldg(Sig + p.hi));
     }
+    if (dSig) *ds = smax.h * ldg(dSig + Nsig - 1) / w.h;
     return smax.h * ldg(Sig + Nsig - 1) / w.h;
 }
 
-__device__ __forceinline__ float G_full_ff(const MeshFF& M, int Nsig, const float* Sig, float L, FF w) {
-    if (fabsf(w.h) > 1e-8f) {
-        const float s = get_sigma_ff(M, Nsig, Sig, w);
-        const float g0 = G_bare(L, w.h);
-        const float den = (w.h * s >= 0.f) ? 1.f / g0 + s : 1.f / g0;
+// G_full from Σ(w) already read
+__device__ __forceinline__ float G_full_s(float s, float L, float w) {
+    if (fabsf(w) > 1e-8f) {
+        const float g0 = G_bare(L, w);
+        const float den = (w * s >= 0.f) ? 1.f / g0 + s : 1.f / g0;
         return 1.f / den;
     }
     return 0.f;
@@ -599,17 +607,20 @@ __device__ __forceinline__ float prop_half_ff(int kind, int half, int ch, const 
         w1 = v - hW;
         w2 = v + hW;
     }
-    if (kind == 0) {
+    if (kind == 0) {  // get_propagator_kat: (S(a) + G(a)^2 dΣ(a)) G(b)
         const FF a = half == 0 ? w1 : w2, b = half == 0 ? w2 : w1;
-        const float ds = get_sigma_ff(M, Nsig, dSig, a);
-        const float g1 = G_full_ff(M, Nsig, Sig, L, a);
+        float ds = 0.f;
+        const float sa = get_sigma_ff(M, Nsig, Sig, a, dSig, &ds);
+        const float g1 = G_full_s(sa, L, a.h);
         const float g0 = G_bare(L, a.h);
         const float r = g1 / g0;
         const float s1 = fabsf(a.h) > 1e-8f ? r * r * expf(-(a.h * a.h) / (L * L)) * 2.f * a.h / (L * L * L) : 0.f;
-        const float g2 = G_full_ff(M, Nsig, Sig, L, b);
+        const float g2 = G_full_s(get_sigma_ff(M, Nsig, Sig, b), L, b.h);
         return (s1 + g1 * g1 * ds) * g2 / two_pi<float>();
     }
-    return -(G_full_ff(M, Nsig, Sig, L, w1) * G_full_ff(M, Nsig, Sig, L, w2)) / two_pi<float>();
+    const float g1 = G_full_s(get_sigma_ff(M, Nsig, Sig, w1), L, w1.h);
+    const float g2 = G_full_s(get_sigma_ff(M, Nsig, Sig, w2), L, w2.h);
+    return -(g1 * g2) / two_pi<float>();
 }
 
 }  // namespace pffrg

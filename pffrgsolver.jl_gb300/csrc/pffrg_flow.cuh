@@ -680,11 +680,12 @@ __device__ __forceinline__ void enqueue(WaveSpace& Wsp, int par, int sub, long l
     Wsp.active[par][a] = sub;
 }
 
-// the meshes of the node setup: FP64 for the FP64 path, float-float pairs for the mixed path
+// the meshes of the node setup (shared memory): FP64 for the FP64 path, float-float pairs for the
+// mixed path
 template <typename R>
-__device__ __forceinline__ auto setup_mesh(const PassArgs<R>& A) {
-    if constexpr (sizeof(R) == 4) return mesh_view_ff(A.mesh_ff, A.L.Nsig, A.L.NO, A.L.Nn);
-    else return mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+__device__ __forceinline__ auto setup_mesh(const PassArgs<R>& A, const unsigned char* smem) {
+    if constexpr (sizeof(R) == 4) return mesh_view_ff(reinterpret_cast<const float*>(smem), A.L.Nsig, A.L.NO, A.L.Nn);
+    else return mesh_view(reinterpret_cast<const double*>(smem), A.L.Nsig, A.L.NO, A.L.Nn);
 }
 
 template <typename R>
@@ -718,10 +719,15 @@ struct SmemLayout {
         return C == 2 ? (size_t)4 * Ns * t_site_stride<R, BatchOf<T, C, SPL>::NB>() + (size_t)2 * Ns * BatchOf<T, C, SPL>::NB
                       : (size_t)2 * C * Ns;
     }
+    // the meshes of the node setup: float-float pairs and inverse spacings (mixed path) or FP64
+    // values and inverse spacings, nm = Nsig + 2 NO + 2 Nn entries each
+    __host__ __device__ static size_t mesh_bytes(int nm) {
+        return sizeof(R) == 4 ? 3 * sizeof(float) * (size_t)nm : 2 * sizeof(double) * (size_t)nm;
+    }
     size_t mesh, teams, tmp, rows, total;
-    __host__ __device__ SmemLayout(int Ns, long long R_rows, bool rows_in_smem) {
-        mesh = 0;  // the meshes are read from global memory
-        teams = 0;
+    __host__ __device__ SmemLayout(int Ns, int nm, long long R_rows, bool rows_in_smem) {
+        mesh = 0;
+        teams = (mesh_bytes(nm) + 15) & ~(size_t)15;
         tmp = (teams + sizeof(TeamScratch<R, T, C, SPL>) * kWarps * NPW + 15) & ~(size_t)15;  // 16-byte loads
         rows = tmp + ((sizeof(R) * (size_t)kWarps * NPW * tmp_per_team(Ns) + 15) & ~(size_t)15);
         total = rows + (rows_in_smem ? sizeof(unsigned) * (size_t)(R_rows + Ns + 1) : 0);
@@ -734,7 +740,7 @@ __device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, un
                                                         int team, int tl) {
     constexpr int NPW = 32 / T;
     const int Ns = A.L.Ns;
-    SmemLayout<R, T, C, SPL> lay(Ns, A.rows_total, A.rows_in_smem);
+    SmemLayout<R, T, C, SPL> lay(Ns, A.L.Nsig + 2 * A.L.NO + 2 * A.L.Nn, A.rows_total, A.rows_in_smem);
     TeamScratch<R, T, C, SPL>* teams = reinterpret_cast<TeamScratch<R, T, C, SPL>*>(smem + lay.teams);
     R* tmp = reinterpret_cast<R*>(smem + lay.tmp) + (size_t)(warp * NPW + team) * lay.tmp_per_team(Ns);
     const unsigned* rows;
@@ -757,8 +763,16 @@ __device__ __forceinline__ Team<R, T, SPL, C> make_team(const PassArgs<R>& A, un
 
 template <typename R, int T, int C, int SPL>
 __device__ __forceinline__ void load_common(const PassArgs<R>& A, unsigned char* smem) {
+    const int nm = A.L.Nsig + 2 * A.L.NO + 2 * A.L.Nn;
+    if constexpr (sizeof(R) == 4) {
+        float* m = reinterpret_cast<float*>(smem);
+        for (int k = threadIdx.x; k < 3 * nm; k += blockDim.x) m[k] = ldg(A.mesh_ff + k);
+    } else {
+        double* m = reinterpret_cast<double*>(smem);
+        for (int k = threadIdx.x; k < 2 * nm; k += blockDim.x) m[k] = ldg(A.mesh + k);
+    }
     if (A.rows_in_smem) {
-        SmemLayout<R, T, C, SPL> lay(A.L.Ns, A.rows_total, true);
+        SmemLayout<R, T, C, SPL> lay(A.L.Ns, nm, A.rows_total, true);
         unsigned* rows = reinterpret_cast<unsigned*>(smem + lay.rows);
         for (long long k = threadIdx.x; k < A.rows_total; k += blockDim.x) rows[k] = ldg(A.ov_rows + k);
         int* roff = reinterpret_cast<int*>(rows + A.rows_total);
@@ -881,7 +895,7 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
     load_common<R, T, C, SPL>(A, smem);
-    const auto M = setup_mesh(A);
+    const auto M = setup_mesh(A, smem);  // staged in shared memory by load_common
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
     Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
@@ -1040,7 +1054,7 @@ __global__ void __launch_bounds__(kWarps * 32, sizeof(R) == 4 ? 4 : 1) eval_kern
     // blocks without a chunk leave before staging the meshes and rows
     if ((long long)blockIdx.x * kWarps * NPW >= Wsp.counters[par]) return;
     load_common<R, T, C, SPL>(A, smem);
-    const auto M = setup_mesh(A);
+    const auto M = setup_mesh(A, smem);  // staged in shared memory by load_common
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int team = lane / T, tl = lane % T;
     Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
@@ -1234,8 +1248,9 @@ struct PassLauncher {
         // overlap rows in shared memory only while three blocks still fit on an SM (a row word is
         // read once per batch of nodes, so from L1 it costs little)
         PassArgs<R> a = a0;
-        a.rows_in_smem = SmemLayout<R, T, C, SPL>(a.L.Ns, a.rows_total, true).total <= (size_t)75 * 1024;
-        SmemLayout<R, T, C, SPL> lay(a.L.Ns, a.rows_total, a.rows_in_smem);
+        const int nm = a.L.Nsig + 2 * a.L.NO + 2 * a.L.Nn;
+        a.rows_in_smem = SmemLayout<R, T, C, SPL>(a.L.Ns, nm, a.rows_total, true).total <= (size_t)75 * 1024;
+        SmemLayout<R, T, C, SPL> lay(a.L.Ns, nm, a.rows_total, a.rows_in_smem);
         const size_t smem = lay.total;
         if (smem > (size_t)227 * 1024) return cudaErrorInvalidConfiguration;
         cudaError_t e;

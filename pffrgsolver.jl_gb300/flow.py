@@ -152,7 +152,7 @@ class FlowContext:
         """Device-driven quadrature levels (default) or the host-driven loop; same results."""
         self._check(self.lib.pffrg_set_async_waves(self.h, int(bool(on))), "set_async_waves")
 
-    def set_fp64_handoff(self, eps: float = 1e-5) -> None:
+    def set_fp64_handoff(self, eps: float = 1e-6) -> None:
         """Mixed path: Simpson subdomains whose test FP32 rounding (relative eps) could flip are
         evaluated again in FP64, so the adaptive decisions are the FP64 path's (0: off)."""
         self._check(self.lib.pffrg_set_fp64_handoff(self.h, float(eps)), "set_fp64_handoff")
