@@ -363,9 +363,9 @@ struct Team {
                     if constexpr (sizeof(R) == 4) {
                         const float scale = fabsf(v.h) + fabsf(W.h) + (isinf(V.h) ? 0.f : fabsf(V.h)) +
                                             (isinf(VP.h) ? 0.f : fabsf(VP.h));
-                        if (ff_near_switch(a0, scale, M, A.L.NO, A.L.Nn) ||
-                            ff_near_switch(a1, scale, M, A.L.NO, A.L.Nn) ||
-                            ff_near_switch(a2, scale, M, A.L.NO, A.L.Nn)) {
+                        if (ff_near_switch(a0, scale, M, A.L.NO, A.L.Nn, v, W, V, VP) ||
+                            ff_near_switch(a1, scale, M, A.L.NO, A.L.Nn, v, W, V, VP) ||
+                            ff_near_switch(a2, scale, M, A.L.NO, A.L.Nn, v, W, V, VP)) {
                             // the FP64 path's rounding decides the side of a buffer switch
                             const MeshG<double> M64 = mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
                             double W64, V64, VP64, b0, b1, b2;
