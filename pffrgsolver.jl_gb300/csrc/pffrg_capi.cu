@@ -575,6 +575,7 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     }
     c.mesh = ctx->mesh;
     c.chi_mesh = ctx->chi_mesh;
+    c.mesh_ff = ctx->mesh_ff;
     c.num_chi = num_chi;
     c.ncomp = ncomp;
     c.exch = ctx->lat.exch;

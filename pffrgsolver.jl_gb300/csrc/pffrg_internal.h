@@ -216,6 +216,7 @@ struct ChiArgs {
     const float* af;         // its FP32 copy: integrand in FP32 (mixed path), or null
     const double* mesh;
     const double* chi_mesh;  // [num_chi]
+    const float* mesh_ff;    // float-float meshes of the mixed integrand
     int num_chi;
     int ncomp;               // 1 (SU(2)) or 3 (U(1)-DM: xx, zz, xy)
     const int* exch;

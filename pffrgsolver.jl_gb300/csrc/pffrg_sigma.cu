@@ -11,6 +11,8 @@
 // below max(atol, rtol |I|), infinite end points mapped by x = t / (1 - t^2)
 // (both ends) or x = s0 +- t / (1 - t) (one end).  One warp owns one
 // integral; the 30 nodes of a bisection are evaluated by 30 lanes.
+#include <type_traits>
+
 #include "pffrg_internal.h"
 
 namespace pffrg {
@@ -657,6 +659,81 @@ struct ChiKernel {
     }
 };
 
+// The mixed path's χ integrand: FP32 vertex and propagator arithmetic on the FP32 copy of the
+// state, with the node setup (plan arguments, interval searches, weights, propagator frequencies)
+// in float-float arithmetic as in the quadrature passes, and plans near a buffer switch built in
+// FP64 from the same FP64 arguments as the FP64 integrand.
+struct ChiKernelFF {
+    const ChiArgs& A;
+    const MeshFF& M;
+    const float* a;  // the FP32 copy of the state
+    int site;
+    int k;
+    double w;
+    __device__ void plan(Plan<float>& P, int ch, FF a0, FF a1, FF a2, double d0, double d1, double d2, FF v, FF vp,
+                         FF wr) const {
+        const Layout& L = A.L;
+        const float scale = fabsf(v.h) + fabsf(vp.h) + fabsf(wr.h);
+        if (ff_near_switch(a0, scale, M, L.NO, L.Nn, v, wr, vp, vp) ||
+            ff_near_switch(a1, scale, M, L.NO, L.Nn, v, wr, vp, vp) ||
+            ff_near_switch(a2, scale, M, L.NO, L.Nn, v, wr, vp, vp)) {
+            const MeshG<double> M64 = mesh_view(A.mesh, L.Nsig, L.NO, L.Nn);
+            make_plan<float>(P, ch, d0, d1, d2, M64, L.Ns, L.NO, L.Nn);
+        } else {
+            make_plan_ff(P, ch, a0, a1, a2, M, L.Ns, L.NO, L.Nn);
+        }
+    }
+    __device__ float G(FF x, float Lam) const { return G_full_s(get_sigma_ff(M, A.L.Nsig, a, x), Lam, x.h); }
+    __device__ double operator()(double x, double y) const {
+        const Layout& L = A.L;
+        const double vd = (2.0 * x - 1.0) / ((1.0 - x) * x);
+        const double vpd = (2.0 * y - 1.0) / ((1.0 - y) * y);
+        const float dv = (float)((2.0 * x * x - 2.0 * x + 1) / ((1.0 - x) * (1.0 - x) * x * x));
+        const float dvp = (float)((2.0 * y * y - 2.0 * y + 1) / ((1.0 - y) * (1.0 - y) * y * y));
+        const FF v(vd), vp(vpd), wr(w), h{0.5f, 0.f};
+        const double hd = 0.5;
+        Plan<float> p1[3];
+        plan(p1[0], 0, v + vp, h * (v - wr - vp), h * (-v - wr + vp), vd + vpd, hd * (vd - w - vpd),
+             hd * (-vd - w + vpd), v, vp, wr);
+        plan(p1[1], 1, wr, v, vp, w, vd, vpd, v, vp, wr);
+        plan(p1[2], 2, v - vp, h * (v - wr + vp), h * (v + wr + vp), vd - vpd, hd * (vd - w + vpd),
+             hd * (vd + w + vpd), v, vp, wr);
+        const float twoS = (float)A.twoS;
+        const float tp2 = two_pi<float>() * two_pi<float>();
+        const int ei = ldg(A.exch + site);
+        float val;
+        if (L.C == 2) val = -(twoS * twoS) * site_value<float>(L, a, p1, CH_ALL, 0, site, ei) / tp2;
+        else val = -site_value<float>(L, a, p1, CH_ALL, k, site, ei) / tp2;
+        if (site == 0) {
+            Plan<float> p2[3];
+            plan(p2[0], 0, v + vp, h * (v - wr - vp), h * (v + wr - vp), vd + vpd, hd * (vd - w - vpd),
+                 hd * (vd + w - vpd), v, vp, wr);
+            plan(p2[1], 1, -v + vp, h * (v - wr + vp), h * (v + wr + vp), -vd + vpd, hd * (vd - w + vpd),
+                 hd * (vd + w + vpd), v, vp, wr);
+            plan(p2[2], 2, -wr, v, vp, -w, vd, vpd, v, vp, wr);
+            auto g = [&](int c) { return site_value<float>(L, a, p2, CH_ALL, c, 0, ei); };
+            if (L.C == 2) {
+                const float vs = g(0);
+                const float vdd = g(1);
+                val -= twoS * (vs - vdd) / (2.f * tp2);
+            } else if (k == 0) {
+                const float vzz = g(1), vdd = g(3);
+                val -= (vzz - vdd) / (2.f * tp2);
+            } else if (k == 1) {
+                const float vxx = g(0), vzz = g(1), vdd = g(3);
+                val -= (2.f * vxx - vzz - vdd) / (2.f * tp2);
+            } else {
+                const float vzd = g(4), vdz = g(5);
+                val -= (vzd - vdz) / (2.f * tp2);
+            }
+        }
+        const float Lam = (float)A.Lam;
+        val *= G(v - h * wr, Lam) * G(v + h * wr, Lam) * dv;
+        val *= G(vp - h * wr, Lam) * G(vp + h * wr, Lam) * dvp;
+        return (double)val;
+    }
+};
+
 // evaluate regions reg(e) of one integral, e in [0, count), the block taking every CL-th
 // chunk of kChiChunk regions from chunk `first`: the 17 points of a chunk over all threads,
 // then each region's rule; emit(e, r, err) sees every result.  Region records are read
@@ -703,9 +780,15 @@ template <typename RT, int CL>
 __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, const int* __restrict__ jobs,
                                                                    int njobs, int* overflow) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SMesh<RT>& M = *reinterpret_cast<SMesh<RT>*>(smem_raw);
-    ChiScratch& S = *reinterpret_cast<ChiScratch*>(smem_raw + sizeof(SMesh<RT>));
-    load_mesh(M, A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+    // the meshes: FP64 SMesh (FP64 integrand) or the float-float block (mixed integrand)
+    ChiScratch& S = *reinterpret_cast<ChiScratch*>(smem_raw + sizeof(SMesh<double>));
+    const int nm = A.L.Nsig + 2 * A.L.NO + 2 * A.L.Nn;
+    if constexpr (sizeof(RT) == 8) {
+        load_mesh(*reinterpret_cast<SMesh<double>*>(smem_raw), A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
+    } else {
+        float* mf = reinterpret_cast<float*>(smem_raw);
+        for (int q = threadIdx.x; q < 3 * nm; q += blockDim.x) mf[q] = ldg(A.mesh_ff + q);
+    }
     const int tid = threadIdx.x;
     const long long slot = blockIdx.x / CL;
     const int rank = (int)(blockIdx.x % CL);  // the cluster's blocks are consecutive in x
@@ -742,10 +825,14 @@ __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, cons
         }
     }
     int* ctl = A.ctl + slot * 4;  // the round's orders to the cluster: stop, K, first new region, list
-    const RT* state;
-    if constexpr (sizeof(RT) == 8) state = A.a;
-    else state = A.af;
-    ChiKernel<RT> f{A, M, state, site, k, wv};
+    const MeshFF MF = mesh_view_ff(reinterpret_cast<const float*>(smem_raw), A.L.Nsig, A.L.NO, A.L.Nn);
+    using Kern = typename std::conditional<sizeof(RT) == 8, ChiKernel<double>, ChiKernelFF>::type;
+    const Kern f = [&]() {
+        if constexpr (sizeof(RT) == 8)
+            return ChiKernel<double>{A, *reinterpret_cast<const SMesh<double>*>(smem_raw), A.a, site, k, wv};
+        else
+            return ChiKernelFF{A, MF, A.af, site, k, wv};
+    }();
     if (lead && tid == 0) {
         R.c0[0] = 0.5 * (lo[col] + hi[col]);
         R.c1[0] = 0.5 * (lo[row] + hi[row]);
@@ -977,7 +1064,8 @@ __global__ void __launch_bounds__(kSigWarps * 32) chi_local_kernel(ChiArgs A) {
 
 template <typename R, int CL>
 static cudaError_t launch_chi_boxes_r(const ChiArgs& a, const int* jobs, int njobs, int* overflow, cudaStream_t st) {
-    const size_t smem = sizeof(SMesh<R>) + sizeof(ChiScratch);
+    static_assert(sizeof(SMesh<double>) >= 3 * sizeof(float) * 5 * kMaxMesh, "float-float meshes fit");
+    const size_t smem = sizeof(SMesh<double>) + sizeof(ChiScratch);
     auto kern = chi_box_kernel<R, CL>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -118,3 +118,25 @@ def test_chi_cluster_matches_single_block(pkg):
                 st = ctx.read_stats()
         assert np.array_equal(out[prec, 0], out[prec, 1 << 40]), prec
         assert st["chi_evals"] > 0
+
+
+def test_chi_mixed_vs_fp64(pkg):
+    """χ of the mixed path (FP32 integrand with the float-float node setup) against χ of the FP64
+    path on the same state, within the stated 1e-6 of max|χ|."""
+    import dataclasses
+
+    import pffrg_gb300._capi as C
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = dataclasses.replace(wl.WORKLOADS["square-L3-1l"], noise=0.05)
+    lat, r, m, a = wl.build_state(w, num_sigma=20, num_omega=8, num_nu=6)
+    chi_mesh = np.array([0.0, 0.4, 2.0])
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with FlowContext(r, m, precision=prec) as ctx:
+            ctx.upload(C.SLOT_A, a)
+            out[prec] = ctx.chi_slot(1.0, C.SLOT_A, chi_mesh)
+    e = rel_err(out["mixed"], out["fp64"])
+    print(f"χ mixed vs FP64: {e:.2e}")
+    assert e < 1e-6
