@@ -555,12 +555,9 @@ __device__ __forceinline__ void make_plan_ff(Plan<float>& P, int chan, FF w, FF 
 // point where the vertex buffers switch: zero (the sign folding of buffer.jl) or the last point
 // of a bosonic or fermionic mesh (beyond it the kernel changes; beyond the bosonic one the vertex
 // is zero).  The FP64 rounding of the argument decides the side there, so such a plan is built in
-// FP64.  An argument that is one of the inputs (node or task frequency, or its negative) is exact
-// in both arithmetics and decides alike.
-__device__ __forceinline__ bool ff_same(FF a, FF b) { return (a.h == b.h && a.l == b.l) || (a.h == -b.h && a.l == -b.l); }
-__device__ __forceinline__ bool ff_near_switch(FF a, float scale, const MeshFF& M, int NO, int Nn, FF v, FF W, FF V,
-                                               FF VP) {
-    if (ff_same(a, v) || ff_same(a, W) || ff_same(a, V) || ff_same(a, VP)) return false;
+// FP64.  (Plans whose arguments are the node and task frequencies themselves are exact in both
+// arithmetics; callers skip the test for them.)
+__device__ __forceinline__ bool ff_near_switch(FF a, float scale, const MeshFF& M, int NO, int Nn) {
     const float x = fabsf(a.h);
     if (isinf(x)) return false;
     if (x <= 1e-9f * scale) return true;
