@@ -551,12 +551,12 @@ __device__ __forceinline__ void make_plan_ff(Plan<float>& P, int chan, FF w, FF 
     }
 }
 
-// True when a float-float plan argument formed by additions lies within a few FP32 ulps of a
-// point where the vertex buffers switch: zero (the sign folding of buffer.jl) or the last point
-// of a bosonic or fermionic mesh (beyond it the kernel changes; beyond the bosonic one the vertex
-// is zero).  The FP64 rounding of the argument decides the side there, so such a plan is built in
-// FP64.  (Plans whose arguments are the node and task frequencies themselves are exact in both
-// arithmetics; callers skip the test for them.)
+// True when a float-float plan argument lies within a few FP32 ulps of a point where the vertex
+// buffers switch: zero (the sign folding of buffer.jl) or the last point of a bosonic or fermionic
+// mesh (beyond it the kernel changes; beyond the bosonic one the vertex is zero).  The FP64
+// rounding of the argument decides the side there, so such a plan is built in FP64.  (Measured:
+// skipping the test for plans read at the task frequencies themselves left 2e-6 of max|dΓ| on a
+// square L=3 flow state at Λ = 0.49, so every plan is tested.)
 __device__ __forceinline__ bool ff_near_switch(FF a, float scale, const MeshFF& M, int NO, int Nn) {
     const float x = fabsf(a.h);
     if (isinf(x)) return false;

@@ -361,15 +361,10 @@ struct Team {
                     SetupT a0, a1, a2;
                     slot_arg<SetupT>(X, slot, ch, v, W, V, VP, a0, a1, a2);
                     if constexpr (sizeof(R) == 4) {
-                        // the buffer of the bubble's own channel is read at the node and task
-                        // frequencies themselves (slot_arg): no addition, no switch test
-                        const bool direct = (X == 0 && ch == 0) || (X == 2 && ch == 2) ||
-                                            (X == 1 && ch == (slot < 2 ? 1 : 2));
                         const float scale = fabsf(v.h) + fabsf(W.h) + (isinf(V.h) ? 0.f : fabsf(V.h)) +
                                             (isinf(VP.h) ? 0.f : fabsf(VP.h));
-                        if (!direct && (ff_near_switch(a0, scale, M, A.L.NO, A.L.Nn) ||
-                                        ff_near_switch(a1, scale, M, A.L.NO, A.L.Nn) ||
-                                        ff_near_switch(a2, scale, M, A.L.NO, A.L.Nn))) {
+                        if (ff_near_switch(a0, scale, M, A.L.NO, A.L.Nn) || ff_near_switch(a1, scale, M, A.L.NO, A.L.Nn) ||
+                            ff_near_switch(a2, scale, M, A.L.NO, A.L.Nn)) {
                             // the FP64 path's rounding decides the side of a buffer switch
                             const MeshG<double> M64 = mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
                             double W64, V64, VP64, b0, b1, b2;

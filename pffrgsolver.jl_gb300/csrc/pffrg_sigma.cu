@@ -670,13 +670,12 @@ struct ChiKernelFF {
     int site;
     int k;
     double w;
-    // direct: the arguments are (±ω, v, v') themselves, exact in both arithmetics
     __device__ void plan(Plan<float>& P, int ch, FF a0, FF a1, FF a2, double d0, double d1, double d2, FF v, FF vp,
-                         FF wr, bool direct = false) const {
+                         FF wr) const {
         const Layout& L = A.L;
         const float scale = fabsf(v.h) + fabsf(vp.h) + fabsf(wr.h);
-        if (!direct && (ff_near_switch(a0, scale, M, L.NO, L.Nn) || ff_near_switch(a1, scale, M, L.NO, L.Nn) ||
-                        ff_near_switch(a2, scale, M, L.NO, L.Nn))) {
+        if (ff_near_switch(a0, scale, M, L.NO, L.Nn) || ff_near_switch(a1, scale, M, L.NO, L.Nn) ||
+            ff_near_switch(a2, scale, M, L.NO, L.Nn)) {
             const MeshG<double> M64 = mesh_view(A.mesh, L.Nsig, L.NO, L.Nn);
             make_plan<float>(P, ch, d0, d1, d2, M64, L.Ns, L.NO, L.Nn);
         } else {
@@ -695,7 +694,7 @@ struct ChiKernelFF {
         Plan<float> p1[3];
         plan(p1[0], 0, v + vp, h * (v - wr - vp), h * (-v - wr + vp), vd + vpd, hd * (vd - w - vpd),
              hd * (-vd - w + vpd), v, vp, wr);
-        plan(p1[1], 1, wr, v, vp, w, vd, vpd, v, vp, wr, true);
+        plan(p1[1], 1, wr, v, vp, w, vd, vpd, v, vp, wr);
         plan(p1[2], 2, v - vp, h * (v - wr + vp), h * (v + wr + vp), vd - vpd, hd * (vd - w + vpd),
              hd * (vd + w + vpd), v, vp, wr);
         const float twoS = (float)A.twoS;
@@ -710,7 +709,7 @@ struct ChiKernelFF {
                  hd * (vd + w - vpd), v, vp, wr);
             plan(p2[1], 1, -v + vp, h * (v - wr + vp), h * (v + wr + vp), -vd + vpd, hd * (vd - w + vpd),
                  hd * (vd + w + vpd), v, vp, wr);
-            plan(p2[2], 2, -wr, v, vp, -w, vd, vpd, v, vp, wr, true);
+            plan(p2[2], 2, -wr, v, vp, -w, vd, vpd, v, vp, wr);
             auto g = [&](int c) { return site_value<float>(L, a, p2, CH_ALL, c, 0, ei); };
             if (L.C == 2) {
                 const float vs = g(0);
