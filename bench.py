@@ -10,6 +10,14 @@ frequencies, Λ = 1, vertex entries N(0, 0.05) plus the bare coupling on the
 evaluations per second of the mixed-precision GPU path; the FP64 GPU path,
 the mixed path's error against it and the CPU oracle are reported beside it.
 
+The full-flow leg (``full_flow``) runs the square L = 3 flow of config 1
+(Λ 50 → 0.01, χ measured after every accepted step) in mixed precision and
+in FP64 and reports both wall times and χ(ω = 0) of the two at the shared
+checkpoints.  Optional legs: ``--sweep N`` (config 3: N square J1-J2 flows
+sharing the GPU) and ``--warm-start TRAIN,TEST`` (config 4: parquet
+iterations from the learned start against the bare start).  Before the
+warm-up the team shape of the passes is picked by the autotuner.
+
 ``--impl reference`` times the CPU restatement of the reference's algorithm
 (the reference is Julia, which is not installed on these machines) on all
 host cores, on a bounded sample of the same workload.

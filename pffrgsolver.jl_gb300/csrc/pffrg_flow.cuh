@@ -1239,6 +1239,16 @@ static __global__ void wave_status_kernel(const int* counters, int* status) {
     if (threadIdx.x == 0 && counters[4]) atomicOr(status, 8);
 }
 
+// Raise a kernel's dynamic shared-memory limit to the most a block may use, once per process: the
+// attribute is process-wide, and contexts of different sizes launch the same kernel from several
+// host threads (coupling sweeps), so a per-launch value could be lowered under another thread's
+// launch.  Each launch still asks for its own size.
+template <auto K>
+inline cudaError_t allow_max_dynamic_smem() {
+    static const cudaError_t e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    return e;
+}
+
 // team width T = lanes per node batch, SPL = sites per lane
 template <typename R, int C>
 struct PassLauncher {
@@ -1253,10 +1263,8 @@ struct PassLauncher {
         const size_t smem = lay.total;
         if (smem > (size_t)227 * 1024) return cudaErrorInvalidConfiguration;
         cudaError_t e;
-        if ((e = cudaFuncSetAttribute(wave0_kernel<R, T, SPL, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-            return e;
-        if ((e = cudaFuncSetAttribute(eval_kernel<R, T, SPL, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-            return e;
+        if ((e = allow_max_dynamic_smem<wave0_kernel<R, T, SPL, C>>())) return e;
+        if ((e = allow_max_dynamic_smem<eval_kernel<R, T, SPL, C>>())) return e;
         constexpr int NPW = 32 / T;
         const int teams_per_block = kWarps * NPW;
         // the FP64 pass of the mixed path keeps the count of handed subdomains (counters[5])
