@@ -164,10 +164,11 @@ def test_sweep_matches_single_runs(pkg):
     from pffrg_gb300.launcher import launch
     from pffrg_gb300.sweep import launch_sweep, square_j1j2_sweep
 
-    inst = square_j1j2_sweep(3, sizes=(3, 4))
+    # different sizes launch the same pass kernels with different shared memory from several threads
+    inst = square_j1j2_sweep(8, sizes=(3, 4, 5, 6, 8))
     kw = dict(num_sigma=10, num_omega=4, num_nu=3, num_chi=4, initial=5.0, final=4.0, parquet=False,
               precision="mixed")
-    res = launch_sweep(inst, workers=3, **kw)
+    res = launch_sweep(inst, workers=8, **kw)
     for i, r in zip(inst, res):
         single = launch("", i.name, i.size, i.model, i.symmetry, i.J, **kw)
         assert r.Lam == single.Lam
