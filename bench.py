@@ -141,14 +141,21 @@ def measured_peaks():
 
 
 def ncu_traffic_per_launch():
-    """DRAM bytes per channel-task-kernel launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "pass_kernel_traffic.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text())
-        except (OSError, ValueError):
-            return None
-    return None
+    """DRAM bytes and duration of one captured wave-kernel launch from the committed ncu summary
+    (profiles/eval_kernel_traffic.txt), or None."""
+    p = ROOT / "profiles" / "eval_kernel_traffic.txt"
+    if not p.exists():
+        return None
+    out = {}
+    for line in p.read_text().splitlines():
+        if line.strip() and not line.startswith("#"):
+            k, _, v = line.partition(" ")
+            out[k] = v.strip()
+    try:
+        return {"workload": out["workload"], "precision": out["precision"], "dram_bytes": float(out["dram_bytes"]),
+                "launch_ms": float(out["launch_ms"])}
+    except (KeyError, ValueError):
+        return None
 
 
 # ---------------------------------------------------------------------------
@@ -309,10 +316,12 @@ def ours(args):
     clk = clocks.summary()
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes_step / (pass_ms_step * 1e-3) / 1e9 if pass_ms_step > 0 else None
+    # DRAM bytes per pass launch: the captured wave launch's DRAM rate times the pass time (the
+    # traffic of a pass is taken proportional to its kernel time; the capture is one level)
     traffic = None
     tr = ncu_traffic_per_launch()
-    if tr and tr.get("workload") == w.name and tr.get("precision") == "mixed":
-        traffic = tr.get("dram_bytes_per_launch")
+    if tr and tr.get("workload") == w.name and tr.get("precision") == "mixed" and pass_launches_step:
+        traffic = tr["dram_bytes"] / tr["launch_ms"] * (pass_ms_step / pass_launches_step)
 
     if rank != 0:
         if dist:
@@ -343,7 +352,11 @@ def ours(args):
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "quadrature wave kernels of the dΓ passes", "peak_kind": peak_kind,
                      "algorithmic_bytes_per_step": alg_bytes_step, "kernel_ms_per_step": pass_ms_step,
-                     "launches_per_step": pass_launches_step},
+                     "launches_per_step": pass_launches_step,
+                     "algorithmic_bytes_per_launch": (alg_bytes_step / pass_launches_step)
+                     if pass_launches_step else None,
+                     "traffic_note": "DRAM bytes per pass launch, scaled from one captured level launch by kernel "
+                                     "time (profiles/eval_kernel_traffic.txt)"},
         "cpu_baseline": cpu,
         "fp64": {"value": 1e3 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
                  "mixed_speedup": fp64_ms / ms_step} if fp64_ms else None,
