@@ -32,8 +32,8 @@ struct PassArgs {
     int prop_kind;
     const R* prop_a;   // Σ of the propagators
     const R* prop_da;  // dΣ of the Katanin propagator
-    const double* prop_a64;   // the same in FP64: the node setup (propagators, plans) is FP64
-    const double* prop_da64;
+    const double* prop_a64;   // the same in FP64 (propagators of the FP64 path and of the mixed
+    const double* prop_da64;  // path's FP64 hand-off pass)
     double* out;       // FP64 output action
     const int* exch;
     const int* ov_off;       // [Ns+1]
