@@ -221,8 +221,8 @@ typedef struct pffrg_stats {
                                    bare and output values, t-channel overlap operands) */
     double pass_ms;             /* summed duration of the channel-task kernels since the last reset */
     double rhs_ms;              /* summed duration of pffrg_rhs calls since the last reset */
-    int64_t pass_launches;      /* channel-task kernel launches since the last reset */
-    int64_t launches;           /* all kernel launches since the last reset */
+    int64_t pass_launches;      /* channel-task passes (each a sequence of level kernels) since the last reset */
+    int64_t launches;           /* kernels this library launched since the last reset */
     int64_t chi_evals;          /* χ integrand evaluations (cubature points) of the last pffrg_chi call */
     int64_t chi_regions_max;    /* largest region count of one χ integral in that call */
     int64_t chi_rounds;         /* refinement rounds of all χ integrals in that call */

@@ -282,7 +282,9 @@ cudaError_t launch_waves(pffrg_ctx* ctx, const PassArgs<R>& p) {
     wave_space_carve(W, ctx->wave_mem, nsub, ctx->L.Ns, ctx->wave_qcap, ctx->L.C);
     // this pass uses its own subdomain count; the queues keep the allocated capacity
     W.nsub = (int)nsub;
+    ctx->h_wave_counters[7] = 0;
     e = launch_pass<R>(p, W, ctx->h_wave_counters, ctx->st);
+    ctx->launches += ctx->h_wave_counters[7];  // the kernels of the pass
     if (e == cudaErrorLaunchOutOfResources && ctx->h_wave_counters[4]) ctx->queue_overflow = 1;
     return e;
 }
@@ -335,8 +337,7 @@ cudaError_t launch_pass_all(pffrg_ctx* ctx, const PassArgs<R>& p0) {
 // pass launch, bracketed by CUDA events on the context's stream when timing is on
 template <typename R>
 cudaError_t run_pass(pffrg_ctx* ctx, const PassArgs<R>& p) {
-    ++ctx->launches;
-    ++ctx->pass_launches;
+    ++ctx->pass_launches;  // the kernels of the pass are added to ctx->launches by launch_waves
     if (!ctx->timing) return launch_pass_all<R>(ctx, p);
     while ((int)ctx->ev.size() < 2 * (ctx->ev_used + 1)) {
         cudaEvent_t e;

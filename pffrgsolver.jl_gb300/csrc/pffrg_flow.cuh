@@ -1270,7 +1270,9 @@ struct PassLauncher {
         // the FP64 pass of the mixed path keeps the count of handed subdomains (counters[5])
         if ((e = cudaMemsetAsync(Wsp.counters, 0, sizeof(int) * (a.esc_mode == 2 ? 5 : 6), st))) return e;
         int g0 = (Wsp.nsub + teams_per_block - 1) / teams_per_block;
+        // h_counters[7] counts the kernels this pass launches
         wave0_kernel<R, T, SPL, C><<<g0 < grid_cap ? g0 : grid_cap, kWarps * 32, smem, st>>>(a, Wsp);
+        ++h_counters[7];
         if ((e = cudaGetLastError())) return e;
         if (a.async_waves) {
             // device-driven levels: every wave reads its chunk and subdomain counts from the device,
@@ -1280,6 +1282,7 @@ struct PassLauncher {
             int par = 1;
             for (int wave = 1; wave <= 21; ++wave) {
                 eval_kernel<R, T, SPL, C><<<grid_cap, kWarps * 32, smem, st>>>(a, Wsp, par);
+                h_counters[7] += 2;
                 if ((e = cudaGetLastError())) return e;
                 decide_kernel<T, SPL, C><<<gd, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol, par, a.esc_mode,
                                                                      a.esc_eps);
@@ -1287,9 +1290,11 @@ struct PassLauncher {
                 par ^= 1;
             }
             wave_status_kernel<<<1, 32, 0, st>>>(Wsp.counters, a.status);
+            ++h_counters[7];
             if ((e = cudaGetLastError())) return e;
             if (a.esc_mode == 1) return cudaSuccess;  // the FP64 pass finishes and reduces
             reduce_kernel<R, C><<<a.ntasks * a.nchan, 128, 0, st>>>(a, Wsp);
+            ++h_counters[7];
             return cudaGetLastError();
         }
         int par = 1;
@@ -1304,6 +1309,7 @@ struct PassLauncher {
             if ((e = cudaMemsetAsync(Wsp.counters + 2 + (par ^ 1), 0, sizeof(int), st))) return e;
             int ge = (nchunks + teams_per_block - 1) / teams_per_block;
             eval_kernel<R, T, SPL, C><<<ge < grid_cap ? ge : grid_cap, kWarps * 32, smem, st>>>(a, Wsp, par);
+            h_counters[7] += 2;
             if ((e = cudaGetLastError())) return e;
             int gd = (nact + teams_per_block - 1) / teams_per_block;
             decide_kernel<T, SPL, C><<<gd < grid_cap ? gd : grid_cap, kWarps * 32, 0, st>>>(Wsp, a.L.Ns, a.atol, a.rtol,
@@ -1313,6 +1319,7 @@ struct PassLauncher {
         }
         if (a.esc_mode == 1) return cudaSuccess;  // the FP64 pass finishes and reduces
         reduce_kernel<R, C><<<a.ntasks * a.nchan, 128, 0, st>>>(a, Wsp);
+        ++h_counters[7];
         return cudaGetLastError();
     }
 };
