@@ -464,8 +464,8 @@ def warm_start_leg(args, dev_index):
         it_train.append(res.parquet_iterations)
     t_data = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ws = ParquetWarmStart(k=16, hidden=(64, 64))
-    loss = ws.fit(feats, verts, epochs=4000, lr=3e-3)
+    ws = ParquetWarmStart(k=32, hidden=(64, 64))
+    loss = ws.fit(feats, verts, epochs=8000, lr=3e-3)
     t_fit = time.perf_counter() - t0
     bare, warm, diffs = [], [], []
     for j in J[n_train:]:

@@ -136,7 +136,9 @@ def vertex_mask(a) -> np.ndarray:
 
 
 class ParquetWarmStart:
-    """Principal components of converged parquet vertices, and a network to their coordinates."""
+    """Principal components of converged parquet vertices and a model from the couplings to their
+    coordinates: a linear least-squares part plus the network for the rest (a residual head), so
+    the network learns only what the linear part misses."""
 
     def __init__(self, k: int = 16, hidden=(64, 64), seed: int = 0):
         self.k, self.hidden, self.seed = k, tuple(hidden), seed
@@ -146,19 +148,25 @@ class ParquetWarmStart:
         X = np.asarray(features, dtype=np.float64)
         V = np.asarray(vertices, dtype=np.float64)
         self.x_mean, self.x_std = X.mean(axis=0), X.std(axis=0) + 1e-12
+        Xn = (X - self.x_mean) / self.x_std
         self.mean = V.mean(axis=0)
         U, S, Vt = np.linalg.svd(V - self.mean, full_matrices=False)
         k = min(self.k, Vt.shape[0])
         self.basis = Vt[:k]                             # [k, D], orthonormal rows
         Z = (V - self.mean) @ self.basis.T              # principal coordinates
-        self.z_scale = Z.std(axis=0) + 1e-12
+        # linear part of the coordinates (least squares), the network fits the remainder
+        Xa = np.hstack([Xn, np.ones((len(Xn), 1))])
+        self.lin, *_ = np.linalg.lstsq(Xa, Z, rcond=None)
+        Zr = Z - Xa @ self.lin
+        self.z_scale = Zr.std(axis=0) + 1e-12
         sizes = [X.shape[1], *self.hidden, k]
         self.net = MLP(sizes, self.seed)
-        loss = self.net.train((X - self.x_mean) / self.x_std, Z / self.z_scale, epochs, lr)
+        loss = self.net.train(Xn, Zr / self.z_scale, epochs, lr)
         # the decoder undoes the coordinate scaling: vertex = mean + (z / scale) (scale basis)
         self.net.set_decoder(self.basis * self.z_scale[:, None], self.mean)
         return loss
 
     def predict(self, feature) -> np.ndarray:
         x = (np.asarray(feature, dtype=np.float64) - self.x_mean) / self.x_std
-        return self.net.predict(x).astype(np.float64)
+        z_lin = np.append(x, 1.0) @ self.lin
+        return self.net.predict(x).astype(np.float64) + z_lin @ self.basis
