@@ -135,10 +135,18 @@ def vertex_mask(a) -> np.ndarray:
     return m
 
 
+def _poly2(x) -> np.ndarray:
+    """1, x_i and x_i x_j (i <= j) of each row of x: the terms of the least-squares part."""
+    x = np.atleast_2d(x)
+    n = x.shape[1]
+    cols = [np.ones(len(x))] + [x[:, i] for i in range(n)] + [x[:, i] * x[:, j] for i in range(n) for j in range(i, n)]
+    return np.stack(cols, axis=1)
+
+
 class ParquetWarmStart:
     """Principal components of converged parquet vertices and a model from the couplings to their
-    coordinates: a linear least-squares part plus the network for the rest (a residual head), so
-    the network learns only what the linear part misses."""
+    coordinates: a least-squares part quadratic in the couplings plus the network for the rest (a
+    residual head), so the network learns only what the quadratic part misses."""
 
     def __init__(self, k: int = 16, hidden=(64, 64), seed: int = 0):
         self.k, self.hidden, self.seed = k, tuple(hidden), seed
@@ -154,8 +162,8 @@ class ParquetWarmStart:
         k = min(self.k, Vt.shape[0])
         self.basis = Vt[:k]                             # [k, D], orthonormal rows
         Z = (V - self.mean) @ self.basis.T              # principal coordinates
-        # linear part of the coordinates (least squares), the network fits the remainder
-        Xa = np.hstack([Xn, np.ones((len(Xn), 1))])
+        # quadratic part of the coordinates (least squares), the network fits the remainder
+        Xa = _poly2(Xn)
         self.lin, *_ = np.linalg.lstsq(Xa, Z, rcond=None)
         Zr = Z - Xa @ self.lin
         self.z_scale = Zr.std(axis=0) + 1e-12
@@ -168,5 +176,5 @@ class ParquetWarmStart:
 
     def predict(self, feature) -> np.ndarray:
         x = (np.asarray(feature, dtype=np.float64) - self.x_mean) / self.x_std
-        z_lin = np.append(x, 1.0) @ self.lin
+        z_lin = (_poly2(x) @ self.lin)[0]
         return self.net.predict(x).astype(np.float64) + z_lin @ self.basis
