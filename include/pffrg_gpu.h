@@ -193,9 +193,11 @@ int pffrg_set_fp64_handoff(pffrg_ctx* ctx, double eps);
 
 /* χ cubature: the passes whose region capacity is at least min_regions
  * (default 32768: the few integrals that approach the evaluation cap) run
- * each integral on a cluster of 8 blocks instead of one block; 0 = always.
- * Results are identical.  No counterpart in the reference. */
-int pffrg_set_chi_cluster(pffrg_ctx* ctx, int64_t min_regions);
+ * each integral on a cluster of `blocks` blocks (8 or 16, default 16; a
+ * 16-block cluster that does not launch falls back to 8) instead of one
+ * block; min_regions 0 = always.  Results are identical.  No counterpart in
+ * the reference. */
+int pffrg_set_chi_cluster(pffrg_ctx* ctx, int64_t min_regions, int blocks);
 
 /* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86,
  * correlation_u1_dm.jl:152-190): static spin correlations χ[i, w] of the

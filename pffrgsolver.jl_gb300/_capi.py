@@ -99,7 +99,7 @@ def load():
     L.pffrg_set_async_waves.argtypes = [vp, ctypes.c_int]
     L.pffrg_set_team_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.pffrg_set_fp64_handoff.argtypes = [vp, ctypes.c_double]
-    L.pffrg_set_chi_cluster.argtypes = [vp, ctypes.c_int64]
+    L.pffrg_set_chi_cluster.argtypes = [vp, ctypes.c_int64, ctypes.c_int]
     ip = ctypes.POINTER(ctypes.c_int)
     L.pffrg_autotune_team_shape.argtypes = [vp, ctypes.c_int, d, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d, d, d,
                                             ip, ip]

@@ -47,6 +47,7 @@ struct pffrg_ctx {
     const double* f_src[4] = {nullptr, nullptr, nullptr, nullptr};
     double esc_eps = 1e-6;  // FP64 hand-off margin of the mixed path (0: off)
     long long chi_cluster_min = 32768;  // χ region capacity from which a cluster runs each integral
+    int chi_cluster_blocks = 16;        // blocks of such a cluster (16, or 8 where 16 cannot launch)
     std::vector<double> h_mesh;    // host copy of [σ|Ωs|νs|Ωt|νt]
     double* log_bounds = nullptr;  // [2][NO][eval+1]
     int bounds_cap = 0;            // eval the buffer holds
@@ -619,7 +620,15 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
             ++ctx->launches;
             // the integrals that outgrew the first capacities are few and long: a cluster of
             // blocks evaluates each round's regions of one integral
-            CK(launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, cap >= ctx->chi_cluster_min ? 8 : 1, ctx->st));
+            const int cl = cap >= ctx->chi_cluster_min ? ctx->chi_cluster_blocks : 1;
+            cudaError_t le = launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, cl, ctx->st);
+            if (le != cudaSuccess && cl > 8) {
+                // a 16-block cluster did not launch (non-portable size): clusters of 8 from now on
+                cudaGetLastError();
+                ctx->chi_cluster_blocks = 8;
+                le = launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, 8, ctx->st);
+            }
+            CK(le);
             over.resize(nb);
             CK(cudaMemcpyAsync(over.data(), ctx->chi_over, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->st));
             CK(cudaStreamSynchronize(ctx->st));
@@ -1367,10 +1376,12 @@ int pffrg_set_fp64_handoff(pffrg_ctx* ctx, double eps) {
     return 0;
 }
 
-int pffrg_set_chi_cluster(pffrg_ctx* ctx, int64_t min_regions) {
+int pffrg_set_chi_cluster(pffrg_ctx* ctx, int64_t min_regions, int blocks) {
     if (!ctx) return PFFRG_E_ARGS;
     if (min_regions < 0) return ctx->fail(PFFRG_E_ARGS, "negative region count");
+    if (blocks != 8 && blocks != 16) return ctx->fail(PFFRG_E_ARGS, "cluster of %d blocks is not built", blocks);
     ctx->chi_cluster_min = min_regions;
+    ctx->chi_cluster_blocks = blocks;
     return 0;
 }
 

@@ -233,7 +233,7 @@ struct ChiArgs {
     int* status;             // bit 1: GK segments exhausted
 };
 // the box integrals of the listed jobs (overflow[slot] = 1: region capacity exhausted), one block
-// per integral, or a cluster of blocks per integral (cluster > 1)
+// per integral, or a cluster of 8 (cluster 2..15) or 16 (cluster >= 16) blocks per integral
 cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, int cluster,
                              cudaStream_t st);
 // the local term and the sums of the boxes into χ

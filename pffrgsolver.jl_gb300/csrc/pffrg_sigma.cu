@@ -405,7 +405,6 @@ constexpr int kChiChunk = 128;     // regions whose 17 points are evaluated per 
 constexpr int kChiScan = 1024;     // list entries staged per step of the sequential sums
 constexpr int kChiSumBlocks = 256; // blocks of the final sum (the oracle sums the same blocks)
 constexpr int kSortItems = 8;      // list entries per thread and tile of the radix sort
-constexpr int kChiCluster = 8;     // blocks per integral of the large-capacity passes
 
 // shared scratch of one integral; the phases of a round use it in turn
 struct ChiScratch {
@@ -1068,6 +1067,10 @@ static cudaError_t launch_chi_boxes_r(const ChiArgs& a, const int* jobs, int njo
     auto kern = chi_box_kernel<R, CL>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if (CL > 8) {  // clusters beyond the portable size of 8 blocks
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)njobs * CL);
     cfg.blockDim = dim3(kChiThreads);
@@ -1085,9 +1088,12 @@ static cudaError_t launch_chi_boxes_r(const ChiArgs& a, const int* jobs, int njo
 
 cudaError_t launch_chi_boxes(const ChiArgs& a, const int* jobs, int njobs, int* overflow, int cluster,
                              cudaStream_t st) {
+    if (cluster >= 16)
+        return a.af ? launch_chi_boxes_r<float, 16>(a, jobs, njobs, overflow, st)
+                    : launch_chi_boxes_r<double, 16>(a, jobs, njobs, overflow, st);
     if (cluster > 1)
-        return a.af ? launch_chi_boxes_r<float, kChiCluster>(a, jobs, njobs, overflow, st)
-                    : launch_chi_boxes_r<double, kChiCluster>(a, jobs, njobs, overflow, st);
+        return a.af ? launch_chi_boxes_r<float, 8>(a, jobs, njobs, overflow, st)
+                    : launch_chi_boxes_r<double, 8>(a, jobs, njobs, overflow, st);
     return a.af ? launch_chi_boxes_r<float, 1>(a, jobs, njobs, overflow, st)
                 : launch_chi_boxes_r<double, 1>(a, jobs, njobs, overflow, st);
 }

@@ -167,10 +167,10 @@ class FlowContext:
                                                        ctypes.byref(s)), "autotune_team_shape")
         return t.value, s.value
 
-    def set_chi_cluster(self, min_regions: int = 32768) -> None:
+    def set_chi_cluster(self, min_regions: int = 32768, blocks: int = 16) -> None:
         """χ cubature passes with at least min_regions of region capacity run each integral on a
-        cluster of 8 blocks (0: always); results are identical."""
-        self._check(self.lib.pffrg_set_chi_cluster(self.h, int(min_regions)), "set_chi_cluster")
+        cluster of `blocks` (8 or 16) blocks (min_regions 0: always); results are identical."""
+        self._check(self.lib.pffrg_set_chi_cluster(self.h, int(min_regions), int(blocks)), "set_chi_cluster")
 
     def set_team_shape(self, lanes: int = 0, sites_per_lane: int = 0) -> None:
         """Team shape of the quadrature passes (lanes x sites per lane; 0, 0: chosen from the

@@ -97,7 +97,7 @@ def test_team_shapes_agree_and_autotune(pkg):
 
 
 def test_chi_cluster_matches_single_block(pkg):
-    """χ with every integral on a cluster of 8 blocks equals χ with one block per integral
+    """χ with every integral on a cluster of 8 or 16 blocks equals χ with one block per integral
     (same pop order, same cut order, same blocked total)."""
     import dataclasses
 
@@ -110,13 +110,14 @@ def test_chi_cluster_matches_single_block(pkg):
     chi_mesh = np.array([0.0, 0.5, 3.0])
     out = {}
     for prec in ("fp64", "mixed"):
-        for cl in (0, 1 << 40):
+        for cl, blocks in ((1 << 40, 8), (0, 8), (0, 16)):
             with FlowContext(r, m, precision=prec) as ctx:
-                ctx.set_chi_cluster(cl)
+                ctx.set_chi_cluster(cl, blocks)
                 ctx.upload(C.SLOT_A, a)
-                out[prec, cl] = ctx.chi_slot(0.3, C.SLOT_A, chi_mesh)
+                out[prec, cl, blocks] = ctx.chi_slot(0.3, C.SLOT_A, chi_mesh)
                 st = ctx.read_stats()
-        assert np.array_equal(out[prec, 0], out[prec, 1 << 40]), prec
+        assert np.array_equal(out[prec, 0, 8], out[prec, 1 << 40, 8]), prec
+        assert np.array_equal(out[prec, 0, 16], out[prec, 1 << 40, 8]), prec
         assert st["chi_evals"] > 0
 
 
