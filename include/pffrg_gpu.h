@@ -193,11 +193,20 @@ int pffrg_set_fp64_handoff(pffrg_ctx* ctx, double eps);
 
 /* χ cubature: the passes whose region capacity is at least min_regions
  * (default 32768: the few integrals that approach the evaluation cap) run
- * each integral on a cluster of `blocks` blocks (8 or 16, default 16; a
+ * each integral on a cluster of `blocks` blocks (8 or 16, default 8; a
  * 16-block cluster that does not launch falls back to 8) instead of one
  * block; min_regions 0 = always.  Results are identical.  No counterpart in
  * the reference. */
 int pffrg_set_chi_cluster(pffrg_ctx* ctx, int64_t min_regions, int blocks);
+
+/* Precision of the χ integrand of a PFFRG_MIXED context: PFFRG_FP64 (default)
+ * or PFFRG_MIXED (FP32 on the FP32 copy of the state with the float-float node
+ * setup; about 1.6x faster, but near the 10^7-evaluation cap, where the
+ * cubature does not converge, its refinement differs from the FP64 one:
+ * 3.7e-6 of max|χ| measured at Λ = 0.15 on square L=3).  The cubature's
+ * coordinates, rules and sums are FP64 either way.  No counterpart in the
+ * reference. */
+int pffrg_set_chi_integrand(pffrg_ctx* ctx, int precision);
 
 /* compute_χ! (src/Observable/correlation_lib/correlation_su2.jl:58-86,
  * correlation_u1_dm.jl:152-190): static spin correlations χ[i, w] of the

@@ -28,7 +28,7 @@ EXPORTED = [
     "pffrg_download", "pffrg_rhs", "pffrg_bs_step", "pffrg_accept", "pffrg_last_integrand_evals",
     "pffrg_host_alloc", "pffrg_host_free", "pffrg_set_timing", "pffrg_read_stats", "pffrg_chi", "pffrg_chi_slot",
     "pffrg_set_async_waves", "pffrg_set_team_shape", "pffrg_autotune_team_shape", "pffrg_set_fp64_handoff",
-    "pffrg_set_chi_cluster",
+    "pffrg_set_chi_cluster", "pffrg_set_chi_integrand",
     "pffrg_scan_cuts",
     "pffrg_resample",
 ]
@@ -100,6 +100,7 @@ def load():
     L.pffrg_set_team_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.pffrg_set_fp64_handoff.argtypes = [vp, ctypes.c_double]
     L.pffrg_set_chi_cluster.argtypes = [vp, ctypes.c_int64, ctypes.c_int]
+    L.pffrg_set_chi_integrand.argtypes = [vp, ctypes.c_int]
     ip = ctypes.POINTER(ctypes.c_int)
     L.pffrg_autotune_team_shape.argtypes = [vp, ctypes.c_int, d, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d, d, d,
                                             ip, ip]

@@ -47,7 +47,10 @@ struct pffrg_ctx {
     const double* f_src[4] = {nullptr, nullptr, nullptr, nullptr};
     double esc_eps = 1e-6;  // FP64 hand-off margin of the mixed path (0: off)
     long long chi_cluster_min = 32768;  // χ region capacity from which a cluster runs each integral
-    int chi_cluster_blocks = 16;        // blocks of such a cluster (16, or 8 where 16 cannot launch)
+    int chi_cluster_blocks = 8;         // blocks of such a cluster (8 or 16)
+    // χ integrand in FP64 on both paths (default): near the 10^7-evaluation cap the cubature does not
+    // converge and FP32 rounding of the integrand changes which regions it refines
+    int chi_fp64 = 1;
     std::vector<double> h_mesh;    // host copy of [σ|Ωs|νs|Ωt|νt]
     double* log_bounds = nullptr;  // [2][NO][eval+1]
     int bounds_cap = 0;            // eval the buffer holds
@@ -570,8 +573,8 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     c.L = ctx->L;
     c.a = a;
     c.af = nullptr;
-    if (ctx->precision == PFFRG_MIXED) {
-        // mixed path: FP32 integrand on the FP32 copy, cubature sums and errors in FP64
+    if (ctx->precision == PFFRG_MIXED && !ctx->chi_fp64) {
+        // FP32 integrand on the FP32 copy (float-float node setup), cubature sums and errors in FP64
         if (int rc = to_f(ctx, a, ctx->f_a)) return rc;
         c.af = ctx->f_a;
     }
@@ -624,6 +627,7 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
             cudaError_t le = launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, cl, ctx->st);
             if (le != cudaSuccess && cl > 8) {
                 // a 16-block cluster did not launch (non-portable size): clusters of 8 from now on
+                // (measured on the GB300: 16-block clusters were 20-30 % slower than 8, so 8 is the default)
                 cudaGetLastError();
                 ctx->chi_cluster_blocks = 8;
                 le = launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, 8, ctx->st);
@@ -1382,6 +1386,13 @@ int pffrg_set_chi_cluster(pffrg_ctx* ctx, int64_t min_regions, int blocks) {
     if (blocks != 8 && blocks != 16) return ctx->fail(PFFRG_E_ARGS, "cluster of %d blocks is not built", blocks);
     ctx->chi_cluster_min = min_regions;
     ctx->chi_cluster_blocks = blocks;
+    return 0;
+}
+
+int pffrg_set_chi_integrand(pffrg_ctx* ctx, int precision) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (precision != PFFRG_FP64 && precision != PFFRG_MIXED) return ctx->fail(PFFRG_E_ARGS, "bad precision");
+    ctx->chi_fp64 = precision == PFFRG_FP64 ? 1 : 0;
     return 0;
 }
 

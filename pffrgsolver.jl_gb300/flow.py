@@ -167,7 +167,12 @@ class FlowContext:
                                                        ctypes.byref(s)), "autotune_team_shape")
         return t.value, s.value
 
-    def set_chi_cluster(self, min_regions: int = 32768, blocks: int = 16) -> None:
+    def set_chi_integrand(self, precision: str = "fp64") -> None:
+        """χ integrand of a mixed context in FP64 (default) or mixed (FP32, float-float setup)."""
+        code = {"fp64": _capi.PFFRG_FP64, "mixed": _capi.PFFRG_MIXED}[precision]
+        self._check(self.lib.pffrg_set_chi_integrand(self.h, code), "set_chi_integrand")
+
+    def set_chi_cluster(self, min_regions: int = 32768, blocks: int = 8) -> None:
         """χ cubature passes with at least min_regions of region capacity run each integral on a
         cluster of `blocks` (8 or 16) blocks (min_regions 0: always); results are identical."""
         self._check(self.lib.pffrg_set_chi_cluster(self.h, int(min_regions), int(blocks)), "set_chi_cluster")

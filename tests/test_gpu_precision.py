@@ -112,6 +112,7 @@ def test_chi_cluster_matches_single_block(pkg):
     for prec in ("fp64", "mixed"):
         for cl, blocks in ((1 << 40, 8), (0, 8), (0, 16)):
             with FlowContext(r, m, precision=prec) as ctx:
+                ctx.set_chi_integrand(prec)
                 ctx.set_chi_cluster(cl, blocks)
                 ctx.upload(C.SLOT_A, a)
                 out[prec, cl, blocks] = ctx.chi_slot(0.3, C.SLOT_A, chi_mesh)
@@ -136,6 +137,7 @@ def test_chi_mixed_vs_fp64(pkg):
     out = {}
     for prec in ("fp64", "mixed"):
         with FlowContext(r, m, precision=prec) as ctx:
+            ctx.set_chi_integrand(prec)  # the FP32 integrand (the default of a mixed context is FP64)
             ctx.upload(C.SLOT_A, a)
             out[prec] = ctx.chi_slot(1.0, C.SLOT_A, chi_mesh)
     e = rel_err(out["mixed"], out["fp64"])
