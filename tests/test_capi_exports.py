@@ -62,3 +62,17 @@ def test_no_device_means_no_context(lib):
     h = lib.pffrg_create(ctypes.byref(lv), ctypes.byref(mv), 0, 0.5, 0, 0)
     assert not h
     assert lib.pffrg_last_error(None)
+
+
+def test_committed_ncu_traffic_summary_parses():
+    """bench.py's roofline traffic comes from the committed ncu summary of the benchmark state."""
+    import importlib.util
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    spec = importlib.util.spec_from_file_location("bench_mod", root / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    tr = bench.ncu_traffic_per_launch()
+    assert tr is not None and tr["workload"] == bench.WORKLOAD and tr["precision"] == "mixed"
+    assert tr["dram_bytes"] > 0 and tr["launch_ms"] > 0

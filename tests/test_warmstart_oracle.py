@@ -20,3 +20,20 @@ def test_mlp_oracle_gradient_matches_finite_differences(O):
                    for e in np.eye(n)])
     assert np.allclose(g, fd, rtol=1e-6, atol=1e-9)
     assert loss == np.mean((M.forward(p, sizes, X)[-1] - T) ** 2)
+
+
+def test_quadratic_part_reproduces_a_quadratic_map(pkg):
+    """The least-squares part of the warm start: coordinates that are a quadratic function of the
+    couplings are reproduced exactly, so the network only sees what is beyond second order."""
+    from pffrg_gb300.warmstart import _poly2
+
+    rng = np.random.default_rng(4)
+    X = rng.normal(size=(40, 3))
+    P = _poly2(X)
+    assert P.shape == (40, 10)
+    assert np.allclose(P[:, 0], 1.0) and np.allclose(P[:, 1:4], X) and np.allclose(P[:, 4], X[:, 0] ** 2)
+    coef = rng.normal(size=(10, 5))
+    Z = P @ coef
+    fit, *_ = np.linalg.lstsq(P, Z, rcond=None)
+    assert np.allclose(P @ fit, Z, atol=1e-10)
+    assert np.allclose(_poly2(X[0]), P[:1])
