@@ -10,11 +10,11 @@ frequencies, Λ = 1, vertex entries N(0, 0.05) plus the bare coupling on the
 evaluations per second of the mixed-precision GPU path; the FP64 GPU path,
 the mixed path's error against it and the CPU oracle are reported beside it.
 
-The full-flow leg (``full_flow``) runs the square L = 3 flow of config 1
+The full-flow leg (``full_flow``) runs the square L = 3 one-loop flow
 (Λ 50 → 0.01, χ measured after every accepted step) in mixed precision and
 in FP64 and reports both wall times and χ(ω = 0) of the two at the shared
-checkpoints.  Optional legs: ``--sweep N`` (config 3: N square J1-J2 flows
-sharing the GPU) and ``--warm-start TRAIN,TEST`` (config 4: parquet
+checkpoints.  Optional legs: ``--sweep N`` (N square J1-J2 flows
+sharing the GPU) and ``--warm-start TRAIN,TEST`` (honeycomb J1-J2-J3: parquet
 iterations from the learned start against the bare start).  Before the
 warm-up the team shape of the passes is picked by the autotuner.
 
@@ -419,7 +419,7 @@ SWEEP = dict(num_sigma=30, num_omega=10, num_nu=8, num_chi=6, initial=50.0, fina
 
 
 def sweep_leg(args, dev_index):
-    """Config 3: n square-lattice J1-J2 Heisenberg flows (J2 ~ U[0, 1], seed 2; L = 3, 4, 5, 6, 8 round
+    """Coupling sweep: n square-lattice J1-J2 Heisenberg flows (J2 ~ U[0, 1], seed 2; L = 3, 4, 5, 6, 8 round
     robin), mixed precision, all on one GPU from concurrent streams; against the same instances run one
     after the other, with the on-site χ(ω=0) of each concurrent run against its single run."""
     from pffrg_gb300.launcher import launch
@@ -444,7 +444,7 @@ def sweep_leg(args, dev_index):
 
 
 def warm_start_leg(args, dev_index):
-    """Config 4: the learned parquet warm start on honeycomb J1-J2-J3 (L=5, (J2, J3) ~ U[0, 0.5]^2, seed 3):
+    """The learned parquet warm start on honeycomb J1-J2-J3 (L=5, (J2, J3) ~ U[0, 0.5]^2, seed 3):
     fit on `train` converged parquet vertices, then parquet iterations to the residual from the bare
     couplings and from the prediction on `test` held-out couplings (FP64)."""
     from pffrg_gb300.launcher import launch

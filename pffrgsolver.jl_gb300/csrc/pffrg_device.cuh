@@ -55,10 +55,10 @@ struct SMesh {
     R nt[kMaxMesh], int_[kMaxMesh];
 };
 
-// Meshes read from the FP64 device block in global memory (L1-resident): the node setup of the
-// quadrature passes (arguments, interval searches, weights, propagators) runs in FP64 on both
-// paths with these.  The block holds [σ | Ωs | νs | Ωt | νt] and then the inverse spacings
-// 1 / (x[k+1] - x[k]) of the same arrays (0 at the last entry).
+// View of the FP64 device mesh block [σ | Ωs | νs | Ωt | νt] followed by the inverse spacings
+// 1 / (x[k+1] - x[k]) of the same arrays (0 at the last entry): the node setup of the FP64 path
+// (staged in shared memory) and the FP64 plans of the mixed path near buffer switches (read from
+// global memory) use it.
 template <typename R>
 struct MeshG {
     const R *sig, *isig, *Os, *iOs, *ns, *ins, *Ot, *iOt, *nt, *int_;

@@ -39,9 +39,9 @@ class Workload:
 
 
 WORKLOADS = {
-    # BASELINE configs[0]: square L=3 Heisenberg, 1 loop, 50/15/10 frequencies, one dΓ at Λ=1, N(0, 0.1), seed 0
+    # square L=3 Heisenberg, 1 loop, 50/15/10 frequencies, one dΓ at Λ=1, N(0, 0.1), seed 0
     "square-L3-1l": Workload("square-L3-1l", "square", 3, "heisenberg", [[1.0]], 1, 1.0, 50, 15, 10, 0.1, 0),
-    # BASELINE configs[1]: pyrochlore L=6 Heisenberg, 2 loop, same meshes, N(0, 0.05) seed 1 + bare J on Ω=0 of ch_t spin
+    # pyrochlore L=6 Heisenberg, 2 loop, same meshes, N(0, 0.05) seed 1 + bare J on Ω=0 of ch_t spin (benchmark)
     "pyrochlore-L6-2l": Workload("pyrochlore-L6-2l", "pyrochlore", 6, "heisenberg", [[1.0]], 2, 1.0, 50, 15, 10,
                                  0.05, 1, bare_on_t=True),
     # the same lattice and state on small meshes (11/4/3 positive frequencies, eval 2, 1 loop): profiling case

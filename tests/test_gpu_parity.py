@@ -51,7 +51,7 @@ def test_dgamma_fp64_small(pkg, O, lattice, size, loops):
 
 
 def test_dgamma_fp64_config1_full(pkg, O):
-    """BASELINE configs[0] shapes: square L=3, 50/15/10 frequencies, Λ=1, N(0, 0.1) seed 0, 1 loop."""
+    """Square L=3, 50/15/10 frequencies, Λ=1, N(0, 0.1) seed 0, 1 loop (the CPU-runnable benchmark case)."""
     from pffrg_gb300.flow import FlowContext
 
     lat, r, m, a = state(pkg)

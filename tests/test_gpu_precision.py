@@ -61,8 +61,8 @@ def test_mixed_small_lambda_flow_state(pkg):
     assert e < 1e-6
 
 
-def test_mixed_config2_state(pkg):
-    """The config-2 state (pyrochlore L=6, 2 loops, 50/15/10, N(0, 0.05) seed 1 + bare J on the Ω=0
+def test_mixed_pyrochlore_benchmark_state(pkg):
+    """The benchmark state (pyrochlore L=6, 2 loops, 50/15/10, N(0, 0.05) seed 1 + bare J on the Ω=0
     t slice) at Λ=1: mixed against FP64 within 1e-6."""
     import pffrg_gb300.workloads as wl
 
@@ -71,7 +71,7 @@ def test_mixed_config2_state(pkg):
     ref = rhs(pkg, r, m, a, w.Lam, w.eval, w.loops, "fp64")
     got = rhs(pkg, r, m, a, w.Lam, w.eval, w.loops, "mixed")
     e = rel_err(got, ref)
-    print(f"config 2: mixed vs FP64 {e:.2e}")
+    print(f"pyrochlore L=6 benchmark state: mixed vs FP64 {e:.2e}")
     assert e < 1e-6
 
 
