@@ -228,6 +228,25 @@ def reference_arm(args):
 
 
 # ---------------------------------------------------------------------------
+# replicas: every rank runs the whole workload on its own GPU (no data-path collective)
+# ---------------------------------------------------------------------------
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest of the ranks' values (the slowest replica sets the step time)."""
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, seconds_per_step: float) -> float:
+    """Right-hand sides per second of all replicas together (one per rank and step)."""
+    return world / seconds_per_step
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def ours(args):
@@ -291,12 +310,8 @@ def ours(args):
     pass_launches_step = st["pass_launches"] / args.steps
     evals_step = st["integrand_evals"]
     alg_bytes_step = st["algorithmic_values"] * 4  # FP32 vertex values on the mixed path
-    t_max = ms_step
-    if dist:
-        tt = torch.tensor([ms_step], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * 1e3 / t_max
+    t_max = max_over_ranks(ms_step, dist, dev)
+    value = replica_throughput(world, t_max * 1e-3)
 
     # mixed result for the error report
     da_mixed = pkg.action.Action.empty_like(a)
@@ -534,12 +549,8 @@ def end_to_end(args, ctx, pkg, C, a, w, flush, dev, dist, world):
         ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
         ctx.compute_dgamma(w.Lam, A_host, D_host, w.eval, GAMMA_TOL, loops=w.loops)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = float(np.mean(e2e_times))
-    if dist:
-        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_value = world / e2e_s
+    e2e_s = max_over_ranks(float(np.mean(e2e_times)), dist, dev)
+    e2e_value = replica_throughput(world, e2e_s)
     h2d = 4 * action_bytes  # a and da uploaded by each of the two calls
     d2h = 2 * action_bytes  # da returned by each call
     lib.pffrg_host_free(pa)
