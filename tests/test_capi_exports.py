@@ -76,3 +76,16 @@ def test_committed_ncu_traffic_summary_parses():
     tr = bench.ncu_traffic_per_launch()
     assert tr is not None and tr["workload"] == bench.WORKLOAD and tr["precision"] == "mixed"
     assert tr["dram_bytes"] > 0 and tr["launch_ms"] > 0
+
+
+def test_setters_refuse_a_null_context():
+    """The tuning and precision setters check their context before anything else (no device needed)."""
+    import pffrg_gb300._capi as C
+
+    L = C.load()
+    assert L.pffrg_set_async_waves(None, 1) == 1
+    assert L.pffrg_set_team_shape(None, 16, 3) == 1
+    assert L.pffrg_set_fp64_handoff(None, 1e-6) == 1
+    assert L.pffrg_set_chi_cluster(None, 32768, 8) == 1
+    assert L.pffrg_set_chi_integrand(None, 0) == 1
+    assert L.pffrg_autotune_team_shape(None, 1, 1.0, 0, 1, 10, 1e-8, 1e-4, 1e-8, 1e-4, None, None) == 1
