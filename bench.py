@@ -56,7 +56,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default=WORKLOAD)
     p.add_argument("--fp64-steps", type=int, default=2)
-    p.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
+    p.add_argument("--ref-seconds", type=float, default=150.0,
+                   help="CPU time budget of the reference arm's timed steps (full right-hand sides)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     p.add_argument("--no-flow", action="store_true", help="skip the full-flow leg")
@@ -159,30 +160,15 @@ def ncu_traffic_per_launch():
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle (CPU restatement) on a strided sample of the channel tasks
+# CPU baseline: the oracle (CPU restatement) over every channel task, timed in full
 # ---------------------------------------------------------------------------
-def cpu_rhs_rate(O, r, m, a, w, target_s: float):
-    threads = os.cpu_count() or 1
-    # probe with a coarse stride, then pick the stride that fits the target time
-    stride = 64
-    P = O.Problem(r, m, num_threads=threads, task_stride=stride)
+def cpu_rhs_seconds(O, P, a, w):
+    """Wall seconds of one full right-hand side of the oracle (dΣ, then dΓ over all channel tasks)."""
     da = np.zeros_like(a.buf)
     t0 = time.perf_counter()
     O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
-    t_sigma = time.perf_counter() - t0
-    t0 = time.perf_counter()
     O.dgamma(P, w.loops, w.Lam, a.buf, da, w.eval, gtol=GAMMA_TOL)
-    t_probe = time.perf_counter() - t0
-    full_est = t_probe * stride
-    stride = int(max(1, min(64, np.ceil(full_est / max(target_s, 1e-3)))))
-    P = O.Problem(r, m, num_threads=threads, task_stride=stride)
-    da = np.zeros_like(a.buf)
-    O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
-    t0 = time.perf_counter()
-    st = O.dgamma(P, w.loops, w.Lam, a.buf, da, w.eval, gtol=GAMMA_TOL)
-    t_gamma = time.perf_counter() - t0
-    per_rhs = t_sigma + stride * t_gamma
-    return 1.0 / per_rhs, threads, stride, t_sigma + t_gamma, st
+    return time.perf_counter() - t0
 
 
 def reference_arm(args):
@@ -196,28 +182,26 @@ def reference_arm(args):
     w = wl.WORKLOADS[args.workload]
     lat, r, m, a = wl.build_state(w)
     threads = os.cpu_count() or 1
-    # one step = the oracle's right-hand side on a strided sample of the channel tasks,
-    # sized so that warm-up + timed steps end within a few minutes
-    per_step_target = max(2.0, 150.0 / max(1, args.steps + args.warmup))
-    rate, threads, stride, _, _ = cpu_rhs_rate(O, r, m, a, w, per_step_target)
-    P = O.Problem(r, m, num_threads=threads, task_stride=stride)
-    times = []
-    for k in range(args.warmup + args.steps):
-        da = np.zeros_like(a.buf)
-        t0 = time.perf_counter()
-        O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
-        ts = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        O.dgamma(P, w.loops, w.Lam, a.buf, da, w.eval, gtol=GAMMA_TOL)
-        tg = time.perf_counter() - t0
-        if k >= args.warmup:
-            times.append(ts + stride * tg)
+    P = O.Problem(r, m, num_threads=threads)
+    # Every step is one full right-hand side (no task sample).  A step takes seconds on the CPU, so
+    # the run does at most one untimed warm-up step and as many of the requested timed steps as fit
+    # in the time budget (--ref-seconds); "steps" and "warmup" report what was run.
+    warm = min(args.warmup, 1)
+    t_first = None
+    for _ in range(warm):
+        t_first = cpu_rhs_seconds(O, P, a, w)
+    n = args.steps
+    if t_first is not None:
+        n = max(1, min(args.steps, int(args.ref_seconds // t_first)))
+    times = [cpu_rhs_seconds(O, P, a, w) for _ in range(n)]
     per = float(np.mean(times))
     value = 1.0 / per
-    sample = (f"every {stride}-th channel task of each dΓ pass (dΣ in full), pass time scaled by {stride}; "
+    sample = (f"{n} full right-hand sides (dΣ + dΓ over every channel task) after {warm} untimed; "
+              f"{args.steps} steps were requested, the CPU budget is {args.ref_seconds:.0f} s; "
               "CPU restatement of the reference algorithm (Julia is not installed)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+            "steps": n, "warmup": warm, "requested_steps": args.steps, "requested_warmup": args.warmup,
+            "ms_per_step": per * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config(args, w), "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
                                                         "kind": "port", "sample": sample},
@@ -351,10 +335,11 @@ def ours(args):
     cpu = None
     if world == 1 and not args.no_cpu:
         O = entry.load_oracle()
-        rate, threads, stride, secs, _ = cpu_rhs_rate(O, r, m, a, w, args.cpu_seconds)
-        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"every {stride}-th channel task of each dΓ pass (dΣ in full), pass time x{stride}; "
-                         f"{secs:.1f} s of CPU work; CPU restatement of the reference algorithm"}
+        threads = os.cpu_count() or 1
+        secs = cpu_rhs_seconds(O, O.Problem(r, m, num_threads=threads), a, w)
+        cpu = {"value": 1.0 / secs, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"one full right-hand side (dΣ + dΓ over every channel task), {secs:.1f} s; "
+                         "CPU restatement of the reference algorithm"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
@@ -374,7 +359,9 @@ def ours(args):
                                      "time (profiles/eval_kernel_traffic.txt)"},
         "cpu_baseline": cpu,
         "fp64": {"value": 1e3 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
-                 "mixed_speedup": fp64_ms / ms_step} if fp64_ms else None,
+                 "mixed_speedup": fp64_ms / ms_step,
+                 "vs_cpu_baseline": (1e3 / fp64_ms) / cpu["value"] if cpu else None} if fp64_ms else None,
+        "mixed_vs_cpu_baseline": value / cpu["value"] if cpu else None,
         "mixed_vs_fp64_rel_err": err_mixed,
         "full_flow": flow,
         "sweep": sweep,

@@ -183,6 +183,21 @@ int pffrg_autotune_team_shape(pffrg_ctx* ctx, int loops, double Lam, int a_slot,
                               double gamma_atol, double gamma_rtol, double sigma_atol, double sigma_rtol,
                               int* lanes, int* sites_per_lane);
 
+/* Capacities of the context's scratch: chunks of one quadrature level's
+ * queue (0: 8 nsub + 65536 for nsub Simpson subdomains) and the first segment
+ * capacity of each adaptive Gauss-Kronrod integral (0: 2048; otherwise at
+ * least 16).  A level that needs more chunks returns PFFRG_E_LIMIT; integrals
+ * that run out of segments are repeated with 8x the segments, up to the
+ * reference's 10^7 evaluations, as always.  For tests of those paths and for
+ * callers that bound the context's memory.  No counterpart in the reference. */
+int pffrg_set_capacities(pffrg_ctx* ctx, int64_t queue_chunks, int64_t gk_segments);
+
+/* Overlap rows of the t-channel sums (flow_su2_t.jl:66-75): 0 = staged in
+ * shared memory when the block's staging stays within 75 KB (default), 1 =
+ * read through L1/L2, 2 = staged whenever they fit the 227 KB of a block.
+ * Results agree to rounding.  No counterpart in the reference. */
+int pffrg_set_overlap_staging(pffrg_ctx* ctx, int mode);
+
 /* Mixed path: a Simpson subdomain whose convergence test is closer to its
  * bounds than eps (the relative rounding allowed for the FP32 node values)
  * could be decided the other way in FP64; such subdomains are evaluated again
@@ -244,9 +259,9 @@ int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset);
 
 /* One-loop dΓ without any device allocation.  This entry point has no
  * counterpart in the reference.  It is meant for callers that cannot call
- * cudaMalloc: code running while a CUDA graph is captured (allocation is not
- * capturable), hosts whose device memory is owned by another framework's pool,
- * and embedders with a device-memory budget fixed at start-up.
+ * cudaMalloc: hosts whose device memory is owned by another framework's pool
+ * allocator (a second allocator fragments that pool and can fail under its
+ * reservations), and embedders with a device-memory budget fixed at start-up.
  *
  * Computes what pffrg_dgamma(loops = 1) computes in FP64 -- compute_dΓ_1l!'s
  * boundary corrections, the Katanin bubbles of all channel tasks and the
@@ -254,18 +269,24 @@ int pffrg_read_stats(pffrg_ctx* ctx, pffrg_stats* out, int reset);
  * state a, da_dev holds dΣ in its Σ part on entry (from compute_dΣ!) and
  * receives the vertex derivative (bare entries untouched).  lattice and mesh
  * are host views as for pffrg_create.  stream: a cudaStream_t (NULL: legacy
- * default stream); the call returns after the stream has drained.
+ * default stream).  The call copies its tables from pageable host memory,
+ * reads the status of its boundary integrals between kernels and returns
+ * after the stream has drained.
  *
  * All scratch (tables, integration bounds, boundary corrections, adaptive
  * quadrature workspace) lives in one static device array of
  * pffrg_noalloc_scratch_bytes() = 128 MiB that every GPU loading this library
  * holds until the process exits.  Problems needing more return PFFRG_E_LIMIT
  * with the required size in pffrg_noalloc_last_error() (square L = 3 with the
- * 50/15/10 default-size meshes at eval <= 10 fits).  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before capturing a stream.  Every call reuses the same
- * array, so calls whose GPU work overlaps (other streams, other host threads)
- * race and must be serialised by the caller. */
+ * 50/15/10 default-size meshes at eval <= 10 fits); so do a level of the
+ * adaptive quadrature with more chunks than the array's queue (2 nsub + 4096
+ * for nsub Simpson subdomains, a quarter of the regular path's) and boundary
+ * integrals that need more than 2048 Gauss-Kronrod segments (the regular entry
+ * points grow their buffers and repeat instead).  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before capturing a stream.  Every call reuses the same array, so calls
+ * whose GPU work overlaps (other streams, other host threads) race and must be
+ * serialised by the caller. */
 int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lattice, const pffrg_mesh_view* mesh, double S, double Lam,
                             const double* a_dev, double* da_dev, int eval, double atol, double rtol, void* stream);
 int64_t pffrg_noalloc_scratch_bytes(void);

@@ -20,6 +20,7 @@ PFFRG_FP64 = 0
 PFFRG_MIXED = 1
 PFFRG_SU2 = 0
 PFFRG_U1_DM = 1
+PFFRG_E_ARGS, PFFRG_E_CUDA, PFFRG_E_LIMIT, PFFRG_E_NONFINITE = 1, 2, 3, 4
 SLOT_A, SLOT_DA, SLOT_INTER, SLOT_ERR, SLOT_NEXT = range(5)
 
 EXPORTED = [
@@ -30,7 +31,7 @@ EXPORTED = [
     "pffrg_set_async_waves", "pffrg_set_team_shape", "pffrg_autotune_team_shape", "pffrg_set_fp64_handoff",
     "pffrg_set_chi_cluster", "pffrg_set_chi_integrand",
     "pffrg_scan_cuts",
-    "pffrg_resample",
+    "pffrg_resample", "pffrg_set_capacities", "pffrg_set_overlap_staging",
 ]
 
 
@@ -57,7 +58,11 @@ class ActionView(ctypes.Structure):
 
 
 class PffrgError(RuntimeError):
-    pass
+    """A nonzero status of the library; ``code`` is the PFFRG_E_* value (0 when unknown)."""
+
+    def __init__(self, msg: str, code: int = 0):
+        super().__init__(msg)
+        self.code = code
 
 
 _lib = None
@@ -101,6 +106,8 @@ def load():
     L.pffrg_set_fp64_handoff.argtypes = [vp, ctypes.c_double]
     L.pffrg_set_chi_cluster.argtypes = [vp, ctypes.c_int64, ctypes.c_int]
     L.pffrg_set_chi_integrand.argtypes = [vp, ctypes.c_int]
+    L.pffrg_set_capacities.argtypes = [vp, ctypes.c_int64, ctypes.c_int64]
+    L.pffrg_set_overlap_staging.argtypes = [vp, ctypes.c_int]
     ip = ctypes.POINTER(ctypes.c_int)
     L.pffrg_autotune_team_shape.argtypes = [vp, ctypes.c_int, d, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d, d, d,
                                             ip, ip]

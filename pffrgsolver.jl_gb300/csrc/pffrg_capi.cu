@@ -67,6 +67,8 @@ struct pffrg_ctx {
     long long gk_cap = 0, gk_slots = 0;
     int gk_overflow = 0;
     int async_waves = 1;  // device-driven quadrature levels (no host round trip per level)
+    long long queue_cap_req = 0;  // chunk-queue capacity of the passes (0: 8 nsub + 65536)
+    int rows_mode = 0;            // overlap rows: 0 staged by size, 1 read through L1/L2, 2 staged when they fit
     int team_T = 0, team_SPL = 0;  // requested team shape of the passes (0: chosen by Ns)
     int64_t chi_evals = 0, chi_regions_max = 0, chi_rounds = 0, chi_rounds_max = 0;
     // wave workspace of the passes (device scratch) and its host-visible counters
@@ -261,8 +263,9 @@ int copy_view(pffrg_ctx* ctx, double* dev, const pffrg_action_view* v, bool to_d
 
 // make sure the wave workspace holds a pass of ntasks x nchan tasks at this eval
 cudaError_t ensure_wave_space(pffrg_ctx* ctx, long long nsub) {
-    const long long qcap = 8 * nsub + 65536;
-    if (nsub <= ctx->wave_nsub && ctx->wave_mem) return cudaSuccess;
+    const long long qcap = ctx->queue_cap_req > 0 ? ctx->queue_cap_req : 8 * nsub + 65536;
+    if (nsub <= ctx->wave_nsub && ctx->wave_mem && (ctx->queue_cap_req <= 0 || qcap == ctx->wave_qcap))
+        return cudaSuccess;
     if (ctx->wave_mem) {
         cudaError_t e = stream_free(ctx->st, ctx->wave_mem);
         if (e != cudaSuccess) return e;
@@ -379,6 +382,7 @@ PassArgs<R> base_pass(pffrg_ctx* ctx, double Lam, int eval, double atol, double 
     p.ov_rows = ctx->lat.ov_rows;
     p.rows_total = ctx->lat.rows;
     p.rows_in_smem = 0;
+    p.rows_mode = ctx->rows_mode;
     p.mesh = ctx->mesh;
     p.mesh_ff = ctx->mesh_ff;
     p.log_bounds = ctx->log_bounds;
@@ -533,9 +537,19 @@ int check_status(pffrg_ctx* ctx) {
     if (h) {
         CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
         if (h & 8) return ctx->fail(PFFRG_E_LIMIT, "quadrature chunk queue capacity exceeded");
-        ctx->gk_overflow = 1;
-        return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity (%lld) exceeded", ctx->gk_cap);
+        if (h & ~16) {
+            ctx->gk_overflow = 1;
+            return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity (%lld) exceeded", ctx->gk_cap);
+        }
+        return ctx->fail(PFFRG_E_NONFINITE, "the result holds NaN or infinite values (non-finite input state?)");
     }
+    return 0;
+}
+
+// status bit 16 when the action holds a NaN or an infinity (read by check_status)
+int check_finite(pffrg_ctx* ctx, const double* a) {
+    ++ctx->launches;
+    CK(launch_check_finite(a, ctx->L.total, ctx->status, ctx->st));
     return 0;
 }
 
@@ -784,9 +798,11 @@ int rhs_dev(pffrg_ctx* ctx, int loops, double Lam, const double* a, double* da, 
             double grtol, double satol, double srtol, int sigma_corr) {
     int rc = dsigma_dev(ctx, Lam, a, da, satol, srtol);
     if (rc) return rc;
-    if (ctx->precision == PFFRG_FP64)
-        return dgamma_dev<double>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
-    return dgamma_dev<float>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
+    rc = ctx->precision == PFFRG_FP64
+             ? dgamma_dev<double>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol)
+             : dgamma_dev<float>(ctx, loops, Lam, a, da, eval, gatol, grtol, sigma_corr, satol, srtol);
+    if (rc) return rc;
+    return check_finite(ctx, da);
 }
 
 int read_evals(pffrg_ctx* ctx) {
@@ -1032,6 +1048,7 @@ static int dsigma_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, p
     if (int rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, true)) return rc;
     int rc = dsigma_dev(ctx, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], atol, rtol);
     if (rc) return rc;
+    if ((rc = check_finite(ctx, ctx->slot[PFFRG_SLOT_DA]))) return rc;
     if ((rc = check_status(ctx))) return rc;
     if ((rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, false))) return rc;
     CK(cudaStreamSynchronize(ctx->st));
@@ -1056,6 +1073,7 @@ static int dgamma_once(pffrg_ctx* ctx, int loops, double Lam, const pffrg_action
                  : dgamma_dev<float>(ctx, loops, Lam, ctx->slot[PFFRG_SLOT_A], ctx->slot[PFFRG_SLOT_DA], eval, gatol,
                                      grtol, sigma_corr, satol, srtol);
     if (rc) return rc;
+    if ((rc = check_finite(ctx, ctx->slot[PFFRG_SLOT_DA]))) return rc;
     if ((rc = check_status(ctx))) return rc;
     if ((rc = read_evals(ctx))) return rc;
     if ((rc = copy_view(ctx, ctx->slot[PFFRG_SLOT_DA], da, false))) return rc;
@@ -1182,6 +1200,7 @@ static int sde_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pff
     };
     int rc = ctx->precision == PFFRG_FP64 ? run(double{}) : run(float{});
     if (rc) return rc;
+    if ((rc = check_finite(ctx, d2))) return rc;
     if ((rc = check_status(ctx))) return rc;
     if ((rc = copy_view(ctx, d2, a2, false))) return rc;
     CK(cudaStreamSynchronize(ctx->st));
@@ -1226,6 +1245,8 @@ static int bse_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pff
     };
     int rc = ctx->precision == PFFRG_FP64 ? run(double{}) : run(float{});
     if (rc) return rc;
+    if ((rc = check_finite(ctx, d2))) return rc;
+    if ((rc = check_status(ctx))) return rc;
     if ((rc = copy_view(ctx, d2, a2, false))) return rc;
     CK(cudaStreamSynchronize(ctx->st));
     return 0;
@@ -1406,6 +1427,29 @@ int pffrg_set_team_shape(pffrg_ctx* ctx, int lanes, int sites_per_lane) {
             return 0;
         }
     return ctx->fail(PFFRG_E_ARGS, "team shape %dx%d is not built", lanes, sites_per_lane);
+}
+
+int pffrg_set_capacities(pffrg_ctx* ctx, int64_t queue_chunks, int64_t gk_segments) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (queue_chunks < 0 || queue_chunks > (1ll << 30)) return ctx->fail(PFFRG_E_ARGS, "queue capacity out of range");
+    if (gk_segments != 0 && (gk_segments < 16 || gk_segments > kGkCapMax))
+        return ctx->fail(PFFRG_E_ARGS, "Gauss-Kronrod capacity must be 0 or in [16, %lld]", kGkCapMax);
+    CK(cudaSetDevice(ctx->device));
+    ctx->queue_cap_req = queue_chunks;
+    ctx->wave_nsub = 0;  // the next pass allocates the requested (or the default) queue
+    ctx->gk_overflow = 0;
+    ctx->gk_cap = gk_segments > 0 ? gk_segments : kGkCap0;
+    CK(stream_free(ctx->st, ctx->gk_seg));
+    ctx->gk_seg = nullptr;
+    ctx->gk_slots = 0;
+    return 0;
+}
+
+int pffrg_set_overlap_staging(pffrg_ctx* ctx, int mode) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (mode < 0 || mode > 2) return ctx->fail(PFFRG_E_ARGS, "overlap staging mode %d (0, 1 or 2)", mode);
+    ctx->rows_mode = mode;
+    return 0;
 }
 
 void* pffrg_host_alloc(int64_t bytes) {

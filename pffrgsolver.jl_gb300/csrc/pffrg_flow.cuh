@@ -834,7 +834,9 @@ __device__ __forceinline__ int simps_test(const double s_old[C][SPL], const doub
     ss_d = in_team_sum<T>(ss_d);
     const double adiff = sqrt(ss_d);
     const double rdiff = adiff / fmax(sqrt(ss_r), sqrt(ss_n));
-    return (adiff < atol || rdiff < rtol || 2 * n > (1ll << 20)) ? 1 : 0;
+    // a non-finite integrand stops refining at once (the reference would refine it to n > 2^20);
+    // the result's finite check then reports it
+    return (adiff < atol || rdiff < rtol || 2 * n > (1ll << 20) || !isfinite(adiff)) ? 1 : 0;
 }
 
 // The same test on the FP32 pass of the mixed path: 1 done, 0 next level, 2 hand the subdomain to
@@ -862,7 +864,7 @@ __device__ __forceinline__ int simps_decide(const double s_old[C][SPL], const do
     ss_d = in_team_sum<T>(ss_d);
     const double adiff = sqrt(ss_d);
     const double den = fmax(sqrt(ss_r), sqrt(ss_n));
-    if (2 * n > (1ll << 20)) return 1;
+    if (2 * n > (1ll << 20) || !isfinite(adiff)) return 1;
     const int done = (adiff < atol || adiff / den < rtol) ? 1 : 0;
     const double E = eps * (sa_new + sa_old) / 15.0;          // |Δ64 - Δ32|
     const double Es = eps * (16.0 * sa_new + sa_old) / 15.0;  // change of the norms in the bound
@@ -1059,7 +1061,8 @@ __global__ void __launch_bounds__(kWarps * 32, sizeof(R) == 4 ? 4 : 1) eval_kern
     Team<R, T, SPL, C> tm = make_team<R, T, SPL, C>(A, smem, M, warp, team, tl);
     const int Ns = A.L.Ns;
     const int jobs = 4 * A.eval + 1;
-    const int nchunks = Wsp.counters[par];
+    // a level whose chunks overflowed the queue counted them all; only the first qcap were filed
+    const int nchunks = min(Wsp.counters[par], Wsp.qcap);
     const long long nwarps = (long long)gridDim.x * kWarps;
     constexpr int NB = BatchOf<T, C, SPL>::NB;
     R g[NB][C][SPL];
@@ -1258,7 +1261,8 @@ struct PassLauncher {
         // read once per batch of nodes, so from L1 it costs little)
         PassArgs<R> a = a0;
         const int nm = a.L.Nsig + 2 * a.L.NO + 2 * a.L.Nn;
-        a.rows_in_smem = SmemLayout<R, T, C, SPL>(a.L.Ns, nm, a.rows_total, true).total <= (size_t)75 * 1024;
+        const size_t staged = SmemLayout<R, T, C, SPL>(a.L.Ns, nm, a.rows_total, true).total;
+        a.rows_in_smem = a.rows_mode == 1 ? 0 : (staged <= (size_t)(a.rows_mode == 2 ? 227 : 75) * 1024);
         SmemLayout<R, T, C, SPL> lay(a.L.Ns, nm, a.rows_total, a.rows_in_smem);
         const size_t smem = lay.total;
         if (smem > (size_t)227 * 1024) return cudaErrorInvalidConfiguration;

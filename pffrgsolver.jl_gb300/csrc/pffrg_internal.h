@@ -40,6 +40,7 @@ struct PassArgs {
     const unsigned* ov_rows; // [R] site a | site b << 8 | multiplicity << 16
     long long rows_total;
     int rows_in_smem;        // stage the rows in shared memory
+    int rows_mode;           // 0: staging chosen by size, 1: rows read through L1/L2, 2: staged when they fit
     const double* mesh;   // [σ | Ωs | νs | Ωt | νt] then their inverse spacings (FP64)
     const float* mesh_ff; // the same as float pairs h, l and FP32 inverse spacings (mixed path)
     const double* corrs;  // [2,3,NO]
@@ -247,6 +248,8 @@ cudaError_t launch_symmetrize_add_to(const Layout& L, const int* exch, const dou
 cudaError_t launch_axpby(const Layout& L, double alpha, const double* x, double beta, double* y, bool sigma_too,
                          bool gamma_too, cudaStream_t st);
 cudaError_t launch_to_float(const double* x, float* y, int64_t n, cudaStream_t st);
+// *status |= 16 when any of a[0..n) is NaN or infinite
+cudaError_t launch_check_finite(const double* a, int64_t n, int* status, cudaStream_t st);
 // max |q3| over all components/channels -> out[0] (double, via block partials)
 cudaError_t launch_absmax_q3(const Layout& L, const double* a, double* partial, int npartial, double* out,
                              cudaStream_t st);

@@ -1,15 +1,16 @@
 // One-loop dΓ without device allocation.
 //
-// Some callers cannot allocate device memory themselves: code that runs while
-// a CUDA graph is being captured (cudaMalloc is not capturable), hosts whose
-// device memory belongs to another framework's pool allocator, or embedders
-// whose allocation budget is fixed at start-up.  For them
+// Some callers cannot allocate device memory themselves: hosts whose device
+// memory belongs to another framework's pool allocator (a second allocator
+// fragments the pool and can fail under the first one's reservations), and
+// embedders whose device-memory budget is fixed when they start.  For them
 // pffrg_dgamma_1l_noalloc computes compute_dΓ_1l!'s result (boundary
 // corrections, Katanin bubbles of all channel tasks, symmetrisation) with
 // every piece of scratch -- lattice and mesh tables, the integration bounds,
 // the boundary corrections and the adaptive-quadrature workspace -- inside
 // one statically sized device array of this file.  It calls no cudaMalloc,
-// cudaFree or other allocating CUDA routine.
+// cudaFree or other allocating CUDA routine.  It copies its tables from
+// pageable host memory and waits for the stream before it returns.
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -81,10 +82,11 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
                             const double* a_dev, double* da_dev, int eval, double atol, double rtol,
                             void* stream) {
     g_noalloc_error.clear();
-    if (!lat || !mesh || !a_dev || !da_dev || !lat->exchange || !lat->mult || !lat->overlap_offsets ||
-        (!lat->overlap_rows && lat->overlap_offsets[lat->num_sites] > 0))
+    if (!lat || !mesh || !a_dev || !da_dev || !lat->exchange || !lat->mult || !lat->overlap_offsets)
         return fail(PFFRG_E_ARGS, "null argument");
+    // the site count bounds every table read below, the overlap offsets included
     if (lat->num_sites < 1 || lat->num_sites > 256) return fail(PFFRG_E_LIMIT, "between 1 and 256 irreducible sites");
+    if (!lat->overlap_rows && lat->overlap_offsets[lat->num_sites] > 0) return fail(PFFRG_E_ARGS, "null overlap rows");
     if (!mesh->sigma || !mesh->omega_s || !mesh->nu_s || !mesh->omega_t || !mesh->nu_t)
         return fail(PFFRG_E_ARGS, "mesh view has null arrays");
     if (mesh->num_sigma < 2 || mesh->num_omega < 2 || mesh->num_nu < 2 || mesh->num_sigma > kMaxMesh ||
@@ -151,6 +153,8 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     // carve the static scratch
     const long long ntasks = (long long)tasks.size();
     const long long nsub = ntasks * 3 * (4 * eval + 1);
+    // chunk queue of one level: a quarter of the regular path's 8 nsub + 65536, so that square L = 3
+    // with 50/15/10 meshes at eval 10 fits the array; a level that needs more returns PFFRG_E_LIMIT
     const long long qcap = 2 * nsub + 4096;
     size_t o = 0;
     const size_t o_exch = o;
@@ -169,6 +173,8 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     o = align_up(o + sizeof(double) * 6 * NO);
     const size_t o_gk = o;  // Gauss-Kronrod segments of the 6 NO boundary integrals
     o = align_up(o + sizeof(double) * 4 * (size_t)kGkCap0 * 6 * NO);
+    const size_t o_gk_status = o;  // segment-capacity flag of those integrals (the passes clear their counters)
+    o = align_up(o + sizeof(int));
     const size_t o_wave = o;
     o += wave_space_bytes(nsub, Ns, qcap, 2);
     if (o > kNoAllocScratchBytes)
@@ -185,8 +191,10 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     NK(cudaMemcpyAsync(base + o_tasks, tasks.data(), sizeof(int4) * tasks.size(), cudaMemcpyHostToDevice, st));
     WaveSpace W;
     wave_space_carve(W, base + o_wave, nsub, Ns, qcap, 2);
-    // the wave counters are the only scratch read before this call writes it
+    // the wave counters and the Gauss-Kronrod flag are the only scratch read before this call writes it
     NK(cudaMemsetAsync(W.counters, 0, sizeof(int) * 8, st));
+    int* gk_status = reinterpret_cast<int*>(base + o_gk_status);
+    NK(cudaMemsetAsync(gk_status, 0, sizeof(int), st));
 
     // boundary corrections of the Katanin bubbles (bubbles.jl:99-159)
     CorrsArgs<double> c;
@@ -203,8 +211,16 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
     c.corrs = reinterpret_cast<double*>(base + o_corrs);
     c.seg = reinterpret_cast<double*>(base + o_gk);
     c.seg_cap = kGkCap0;
-    c.status = W.counters + 5;
+    c.status = gk_status;
     NK(launch_corrs<double>(c, st));
+    // the passes weight their boundary nodes with these corrections: stop here if any integral ran
+    // out of segments (the regular entry points grow the segment buffer and repeat instead)
+    int status = 0;
+    NK(cudaMemcpyAsync(&status, gk_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NK(cudaStreamSynchronize(st));
+    if (status)
+        return fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity (%lld per boundary integral) exceeded",
+                    (long long)kGkCap0);
 
     // Katanin bubbles of all channel tasks (flow_su2_{s,t,u}.jl:2-55)
     PassArgs<double> p;
@@ -244,10 +260,7 @@ int pffrg_dgamma_1l_noalloc(const pffrg_lattice_view* lat, const pffrg_mesh_view
         return fail(PFFRG_E_LIMIT, "quadrature chunk queue of the static scratch exceeded");
     NK(e);
     NK(launch_symmetrize(L, p.exch, da_dev, st));
-    int status = 0;
-    NK(cudaMemcpyAsync(&status, W.counters + 5, sizeof(int), cudaMemcpyDeviceToHost, st));
     NK(cudaStreamSynchronize(st));
-    if (status) return fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity exceeded");
     return 0;
 }
 

@@ -120,6 +120,15 @@ __global__ void axpby_kernel(Layout L, double alpha, const double* __restrict__ 
     }
 }
 
+// status bit 4 (16) when any of the n values is NaN or infinite: a right-hand side whose result is
+// not finite is reported as PFFRG_E_NONFINITE instead of flowing into the next ODE stage
+__global__ void finite_kernel(const double* __restrict__ a, int64_t n, int* status) {
+    int bad = 0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        bad |= !isfinite(a[e]);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, 16);
+}
+
 __global__ void to_float_kernel(const double* __restrict__ x, float* y, int64_t n) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
         y[e] = (float)x[e];
@@ -342,6 +351,11 @@ cudaError_t launch_axpby(const Layout& L, double alpha, const double* x, double 
                          bool gamma_too, cudaStream_t st) {
     const int64_t n = (sigma_too ? L.Nsig : 0) + (gamma_too ? L.C * 3 * L.chan : 0);
     axpby_kernel<<<grid_for(n, 256), 256, 0, st>>>(L, alpha, x, beta, y, sigma_too, gamma_too);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_check_finite(const double* a, int64_t n, int* status, cudaStream_t st) {
+    finite_kernel<<<grid_for(n, 256), 256, 0, st>>>(a, n, status);
     return cudaGetLastError();
 }
 

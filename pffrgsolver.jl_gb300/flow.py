@@ -61,7 +61,7 @@ class FlowContext:
     def _check(self, rc: int, what: str):
         if rc != 0:
             msg = self.lib.pffrg_last_error(self.h).decode()
-            raise _capi.PffrgError(f"{what}: code {rc}: {msg}")
+            raise _capi.PffrgError(f"{what}: code {rc}: {msg}", rc)
 
     @property
     def action_size(self) -> int:
@@ -176,6 +176,16 @@ class FlowContext:
         """χ cubature passes with at least min_regions of region capacity run each integral on a
         cluster of `blocks` (8 or 16) blocks (min_regions 0: always); results are identical."""
         self._check(self.lib.pffrg_set_chi_cluster(self.h, int(min_regions), int(blocks)), "set_chi_cluster")
+
+    def set_capacities(self, queue_chunks: int = 0, gk_segments: int = 0) -> None:
+        """Chunk-queue capacity of the quadrature levels and first Gauss-Kronrod segment capacity
+        (0: the defaults); a level beyond the queue raises PffrgError with PFFRG_E_LIMIT."""
+        self._check(self.lib.pffrg_set_capacities(self.h, int(queue_chunks), int(gk_segments)), "set_capacities")
+
+    def set_overlap_staging(self, mode: int = 0) -> None:
+        """Overlap rows of the t-channel sums: 0 staged by size, 1 through L1/L2, 2 staged when
+        they fit a block's shared memory.  Results agree to rounding."""
+        self._check(self.lib.pffrg_set_overlap_staging(self.h, int(mode)), "set_overlap_staging")
 
     def set_team_shape(self, lanes: int = 0, sites_per_lane: int = 0) -> None:
         """Team shape of the quadrature passes (lanes x sites per lane; 0, 0: chosen from the

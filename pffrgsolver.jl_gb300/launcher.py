@@ -5,8 +5,8 @@ loop of src/Launcher/launcher_{1l,2l,ml}.jl (the four stages and the error
 ratio run on the device through ``pffrg_bs_step``), the parquet warm start of
 src/Launcher/parquet.jl:1-100, and the mesh scan/resampling between steps
 (src/Action/Action.jl:361-527, src/Action/channel.jl:416-471).  Observables
-are handed to ``measure`` callbacks; the HDF5 files of the reference are not
-written by this module.
+go to ``measure`` callbacks and, when ``launch`` is given a file name, to the
+reference's ``*_obs`` / ``*_cp`` HDF5 files (through ``disk`` and ``hdf5``).
 """
 from __future__ import annotations
 
@@ -406,8 +406,16 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
     while Lam > Lf:
         eval_ = get_eval(Lam, min_eval, max_eval)
         t0 = time.perf_counter()
-        err, amax = ctx.bs_step(Lam, dLam, eval_, loops=loops, gamma_tol=gamma_tol, sigma_tol=sigma_tol,
-                                sigma_corr=sigma_corr, ode_tol=ode_tol)
+        try:
+            err, amax = ctx.bs_step(Lam, dLam, eval_, loops=loops, gamma_tol=gamma_tol, sigma_tol=sigma_tol,
+                                    sigma_corr=sigma_corr, ode_tol=ode_tol)
+        except _capi.PffrgError as e:
+            if e.code != _capi.PFFRG_E_NONFINITE:
+                raise
+            # a stage derivative with NaN or infinite entries: stop as the reference's sanity checks
+            # stop an unstable integration (launcher_1l.jl:125-128), with the state of the last step
+            res.reason = "right-hand side is not finite"
+            break
         t_step = time.perf_counter() - t0
         res.timers["steps"] += t_step
         res.rhs_evals += 4

@@ -64,7 +64,7 @@ def test_dgamma_fp64_config1_full(pkg, O):
 
 
 def test_dgamma_mixed_config1(pkg, O):
-    """Mixed precision against the FP64 oracle (error bound 1e-4 relative in the max norm)."""
+    """Mixed precision against the FP64 oracle (the stated bound: 1e-6 relative in the max norm)."""
     from pffrg_gb300.flow import FlowContext
 
     lat, r, m, a = state(pkg)
@@ -75,7 +75,7 @@ def test_dgamma_mixed_config1(pkg, O):
         ctx.compute_dgamma(1.0, a, da, 10)
     e = rel_err(da.buf, ref)
     print(f"mixed vs FP64 oracle: {e:.3e}")
-    assert e < 1e-4
+    assert e < 1e-6
 
 
 def test_parquet_fp64_small(pkg, O):
@@ -144,7 +144,7 @@ def test_dgamma_u1dm_fp64(pkg, O, lattice, size, model, J, loops):
 
 
 def test_dgamma_u1dm_mixed(pkg, O):
-    """U(1)-DM mixed precision against the FP64 oracle (bound 1e-4 relative in the max norm)."""
+    """U(1)-DM mixed precision against the FP64 oracle (the stated bound: 1e-6 relative in the max norm)."""
     import pffrg_gb300.workloads as wl
     from pffrg_gb300.flow import FlowContext
 
@@ -161,7 +161,7 @@ def test_dgamma_u1dm_mixed(pkg, O):
         ctx.compute_dgamma(1.0, a, da, 2, loops=2)
     e = rel_err(da.buf, ref)
     print(f"u1-dm mixed vs FP64 oracle: {e:.3e}")
-    assert e < 1e-4
+    assert e < 1e-6
 
 
 def test_parquet_u1dm_fp64(pkg, O):
