@@ -113,6 +113,20 @@ int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
 int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval,
               double atol, double rtol);
 
+/* The parquet fixed point of launch_parquet! (src/Launcher/parquet.jl:43-80)
+ * on the device: the action in slot A is the starting vertex and is replaced
+ * by the iterate; every iteration converges the SDE (compute_Σ!, damped
+ * Σ update, Σ errors), evaluates the BSEs (compute_Γ!), takes the residual
+ * abs = max|ap.q3 - a.q3|, rel = abs / max(max|a.q3|, max|ap.q3|) and damps
+ * a = (1 - beta) a + beta ap on the vertex, until abs < tol_abs or
+ * rel < tol_rel or max_iter iterations (the reference's beta is min(Λ, 1)).
+ * Slots DA and ERR are overwritten.  The actions stay on the device; only the
+ * three error norms of an iteration are read back to steer the loop.  Returns
+ * the iterations run and the last residuals. */
+int pffrg_parquet(pffrg_ctx* ctx, double Lam, int eval, double gamma_atol, double gamma_rtol, double sigma_atol,
+                  double sigma_rtol, double tol_abs, double tol_rel, double beta, int max_iter, int* iterations,
+                  double* abs_err, double* rel_err);
+
 /* ---- device-resident interface (no host copies inside the step) ---- */
 
 /* Number of doubles of one packed action (Σ, then per component bare and

@@ -192,6 +192,52 @@ def bse(P: Problem, Lam: float, a1: np.ndarray, a2: np.ndarray, corrs_buf: np.nd
     _check(lib().oracle_bse(P.ref, Lam, _f(a1), _f(a2), _f(corrs_buf), eval_, gtol[0], gtol[1]), "bse")
 
 
+def _masks(P: Problem):
+    """(vertex mask without bare, q3 mask) of a packed action of P's layout."""
+    ns, nsig, no, nn = (int(P.s.num_sites), int(P.s.num_sigma), int(P.s.num_omega), int(P.s.num_nu))
+    ncomp = 2 if int(P.s.symmetry) == 0 else 6
+    k1, k2, k3 = ns * no, ns * no * nn, ns * no * nn * nn
+    chan = k1 + 2 * k2 + k3
+    size = nsig + ncomp * (ns + 3 * chan)
+    gm = np.zeros(size, dtype=bool)
+    q3 = np.zeros(size, dtype=bool)
+    for c in range(ncomp):
+        base = nsig + c * (ns + 3 * chan) + ns
+        gm[base:base + 3 * chan] = True
+        for ch in range(3):
+            o = base + ch * chan + k1 + 2 * k2
+            q3[o:o + k3] = True
+    return gm, q3
+
+
+def parquet(P: Problem, Lam: float, a: np.ndarray, eval_: int, gtol=(1e-8, 1e-4), stol=(1e-8, 1e-4),
+            ptol=(1e-8, 1e-4), beta=None, max_iter: int = 50):
+    """launch_parquet!'s fixed point (src/Launcher/parquet.jl:43-80) with the oracle's compute_Σ! and
+    compute_Γ!: a (packed) is replaced by the iterate; returns (iterations, abs residual, rel residual)."""
+    beta = min(Lam, 1.0) if beta is None else beta
+    gm, q3 = _masks(P)
+    nsig = int(P.s.num_sigma)
+    ap = np.zeros_like(a)
+    abs_err = rel_err = np.inf
+    count = 1
+    while abs_err >= ptol[0] and rel_err >= ptol[1] and count <= max_iter:
+        s_abs = s_rel = np.inf
+        s_count = 1
+        corrs_buf = None
+        while s_abs >= ptol[0] and s_rel >= ptol[1] and s_count <= max_iter:
+            corrs_buf = sde(P, Lam, a, ap, eval_, gtol, stol)
+            s_abs = float(np.max(np.abs(ap[:nsig] - a[:nsig])))
+            s_rel = s_abs / max(float(np.max(np.abs(a[:nsig]))), float(np.max(np.abs(ap[:nsig]))))
+            a[:nsig] = (1.0 - beta) * a[:nsig] + beta * ap[:nsig]
+            s_count += 1
+        bse(P, Lam, a, ap, corrs_buf, eval_, gtol)
+        abs_err = float(np.max(np.abs(ap[q3] - a[q3])))
+        rel_err = abs_err / max(float(np.max(np.abs(a[q3]))), float(np.max(np.abs(ap[q3]))))
+        a[gm] = (1.0 - beta) * a[gm] + beta * ap[gm]
+        count += 1
+    return count - 1, abs_err, rel_err
+
+
 def chi(P: Problem, Lam: float, a: np.ndarray, chi_mesh: np.ndarray, tol=(1e-8, 1e-4)):
     """compute_χ!: χ[site, w] on the χ mesh (Fortran-ordered [Ns, num_chi]); for u1-dm the list
     [χxx, χzz, χxy] of such arrays (correlation_u1_dm.jl:152-190)."""

@@ -1163,14 +1163,14 @@ int pffrg_autotune_team_shape(pffrg_ctx* ctx, int loops, double Lam, int a_slot,
     return 0;
 }
 
-static int sde_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
-              double grtol, double satol, double srtol) {
-    if (!ctx) return PFFRG_E_ARGS;
-    CK(cudaSetDevice(ctx->device));
-    double* d1 = ctx->slot[PFFRG_SLOT_A];
-    double* d2 = ctx->slot[PFFRG_SLOT_DA];
-    if (int rc = copy_view(ctx, d1, a1, true)) return rc;
-    if (int rc = copy_view(ctx, d2, a2, true)) return rc;
+}  // extern "C"
+
+namespace {
+
+// compute_Σ! (SDE.jl:58-96) on device actions d1 -> d2: the boundary corrections (kept for the
+// next BSE), the reduced s bubble (slot 1 is the bare vertex) and the SDE self energy
+int sde_dev(pffrg_ctx* ctx, double Lam, double* d1, double* d2, int eval, double gatol, double grtol, double satol,
+            double srtol) {
     auto run = [&](auto tag) -> int {
         using R = decltype(tag);
         const R* r1;
@@ -1200,26 +1200,12 @@ static int sde_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pff
     };
     int rc = ctx->precision == PFFRG_FP64 ? run(double{}) : run(float{});
     if (rc) return rc;
-    if ((rc = check_finite(ctx, d2))) return rc;
-    if ((rc = check_status(ctx))) return rc;
-    if ((rc = copy_view(ctx, d2, a2, false))) return rc;
-    CK(cudaStreamSynchronize(ctx->st));
-    return 0;
+    return check_finite(ctx, d2);
 }
 
-int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
-              double grtol, double satol, double srtol) {
-    return gk_retry(ctx, [&] { return sde_once(ctx, Lam, a1, a2, eval, gatol, grtol, satol, srtol); });
-}
-
-static int bse_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double atol,
-              double rtol) {
-    if (!ctx) return PFFRG_E_ARGS;
-    CK(cudaSetDevice(ctx->device));
-    double* d1 = ctx->slot[PFFRG_SLOT_A];
-    double* d2 = ctx->slot[PFFRG_SLOT_DA];
-    if (int rc = copy_view(ctx, d1, a1, true)) return rc;
-    if (int rc = copy_view(ctx, d2, a2, true)) return rc;
+// compute_Γ! (compute.jl:2-54) on device actions d1 -> d2 with the boundary corrections of the
+// last SDE call
+int bse_dev(pffrg_ctx* ctx, double Lam, double* d1, double* d2, int eval, double atol, double rtol) {
     auto run = [&](auto tag) -> int {
         using R = decltype(tag);
         const R* r1;
@@ -1245,7 +1231,55 @@ static int bse_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pff
     };
     int rc = ctx->precision == PFFRG_FP64 ? run(double{}) : run(float{});
     if (rc) return rc;
-    if ((rc = check_finite(ctx, d2))) return rc;
+    return check_finite(ctx, d2);
+}
+
+// One SDE or BSE evaluation of the device parquet loop, repeated with more Gauss-Kronrod segments
+// when an integral ran out of them (the inputs are unchanged by a failed evaluation)
+template <class Fn>
+int parquet_eval(pffrg_ctx* ctx, Fn fn) {
+    for (;;) {
+        int rc = fn();
+        if (!rc) rc = check_status(ctx);
+        if (rc != PFFRG_E_LIMIT || !grow_gk(ctx)) return rc;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+static int sde_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
+              double grtol, double satol, double srtol) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    double* d1 = ctx->slot[PFFRG_SLOT_A];
+    double* d2 = ctx->slot[PFFRG_SLOT_DA];
+    if (int rc = copy_view(ctx, d1, a1, true)) return rc;
+    if (int rc = copy_view(ctx, d2, a2, true)) return rc;
+    int rc = sde_dev(ctx, Lam, d1, d2, eval, gatol, grtol, satol, srtol);
+    if (rc) return rc;
+    if ((rc = check_status(ctx))) return rc;
+    if ((rc = copy_view(ctx, d2, a2, false))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pffrg_sde(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double gatol,
+              double grtol, double satol, double srtol) {
+    return gk_retry(ctx, [&] { return sde_once(ctx, Lam, a1, a2, eval, gatol, grtol, satol, srtol); });
+}
+
+static int bse_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double atol,
+              double rtol) {
+    if (!ctx) return PFFRG_E_ARGS;
+    CK(cudaSetDevice(ctx->device));
+    double* d1 = ctx->slot[PFFRG_SLOT_A];
+    double* d2 = ctx->slot[PFFRG_SLOT_DA];
+    if (int rc = copy_view(ctx, d1, a1, true)) return rc;
+    if (int rc = copy_view(ctx, d2, a2, true)) return rc;
+    int rc = bse_dev(ctx, Lam, d1, d2, eval, atol, rtol);
+    if (rc) return rc;
     if ((rc = check_status(ctx))) return rc;
     if ((rc = copy_view(ctx, d2, a2, false))) return rc;
     CK(cudaStreamSynchronize(ctx->st));
@@ -1255,6 +1289,58 @@ static int bse_once(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pff
 int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_action_view* a2, int eval, double atol,
               double rtol) {
     return gk_retry(ctx, [&] { return bse_once(ctx, Lam, a1, a2, eval, atol, rtol); });
+}
+
+int pffrg_parquet(pffrg_ctx* ctx, double Lam, int eval, double gatol, double grtol, double satol, double srtol,
+                  double tol_abs, double tol_rel, double beta, int max_iter, int* iterations, double* abs_err,
+                  double* rel_err) {
+    if (!ctx) return PFFRG_E_ARGS;
+    if (eval < 1 || max_iter < 0 || !(beta > 0.0) || beta > 1.0)
+        return ctx->fail(PFFRG_E_ARGS, "eval >= 1, max_iter >= 0 and 0 < beta <= 1 required");
+    CK(cudaSetDevice(ctx->device));
+    const Layout& L = ctx->L;
+    double* A = ctx->slot[PFFRG_SLOT_A];    // a: the iterate, updated in place
+    double* P = ctx->slot[PFFRG_SLOT_DA];   // ap: SDE / BSE result
+    double* E = ctx->slot[PFFRG_SLOT_ERR];  // a_err = ap - a on the vertex
+    double* h = ctx->h_scalars;
+    double ea = INFINITY, er = INFINITY;
+    int count = 1;
+    // parquet.jl:43-80
+    while (ea >= tol_abs && er >= tol_rel && count <= max_iter) {
+        double sa = INFINITY, sr = INFINITY;
+        int scount = 1;
+        while (sa >= tol_abs && sr >= tol_rel && scount <= max_iter) {
+            if (int rc = parquet_eval(ctx, [&] { return sde_dev(ctx, Lam, A, P, eval, gatol, grtol, satol, srtol); }))
+                return rc;
+            // max|ap.Σ - a.Σ|, max|a.Σ|, max|ap.Σ|, then a.Σ = (1 - β) a.Σ + β ap.Σ
+            ++ctx->launches;
+            CK(launch_sigma_err(L.Nsig, A, P, ctx->scalars, ctx->st));
+            CK((++ctx->launches, launch_axpby)(L, 1.0 - beta, P, beta, A, true, false, ctx->st));
+            CK(cudaMemcpyAsync(h, ctx->scalars, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->st));
+            CK(cudaStreamSynchronize(ctx->st));
+            sa = h[0];
+            sr = sa / std::max(h[1], h[2]);
+            ++scount;
+        }
+        if (int rc = parquet_eval(ctx, [&] { return bse_dev(ctx, Lam, A, P, eval, gatol, grtol); })) return rc;
+        // a_err = ap - a on the vertex; abs = max|a_err.q3|, rel = abs / max(max|a.q3|, max|ap.q3|)
+        CK(cudaMemcpyAsync(E, P, sizeof(double) * L.total, cudaMemcpyDeviceToDevice, ctx->st));
+        CK((++ctx->launches, launch_axpby)(L, 1.0, A, -1.0, E, false, true, ctx->st));
+        if (int rc = absmax(ctx, E, ctx->scalars + 0)) return rc;
+        if (int rc = absmax(ctx, A, ctx->scalars + 1)) return rc;
+        if (int rc = absmax(ctx, P, ctx->scalars + 2)) return rc;
+        // a = (1 - β) a + β ap on the vertex (bare excluded)
+        CK((++ctx->launches, launch_axpby)(L, 1.0 - beta, P, beta, A, false, true, ctx->st));
+        CK(cudaMemcpyAsync(h, ctx->scalars, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        ea = h[0];
+        er = ea / std::max(h[1], h[2]);
+        ++count;
+    }
+    if (iterations) *iterations = count - 1;
+    if (abs_err) *abs_err = ea;
+    if (rel_err) *rel_err = er;
+    return 0;
 }
 
 static int bs_step_once(pffrg_ctx* ctx, int loops, double Lam, double dLam, int eval, double gatol, double grtol,

@@ -248,6 +248,8 @@ cudaError_t launch_symmetrize_add_to(const Layout& L, const int* exch, const dou
 cudaError_t launch_axpby(const Layout& L, double alpha, const double* x, double beta, double* y, bool sigma_too,
                          bool gamma_too, cudaStream_t st);
 cudaError_t launch_to_float(const double* x, float* y, int64_t n, cudaStream_t st);
+// out = [max|ap.Σ - a.Σ|, max|a.Σ|, max|ap.Σ|] over the Nsig self-energy values
+cudaError_t launch_sigma_err(int Nsig, const double* a, const double* ap, double* out, cudaStream_t st);
 // *status |= 16 when any of a[0..n) is NaN or infinite
 cudaError_t launch_check_finite(const double* a, int64_t n, int* status, cudaStream_t st);
 // max |q3| over all components/channels -> out[0] (double, via block partials)

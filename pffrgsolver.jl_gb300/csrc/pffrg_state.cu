@@ -129,6 +129,26 @@ __global__ void finite_kernel(const double* __restrict__ a, int64_t n, int* stat
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, 16);
 }
 
+// the SDE iteration's errors (parquet.jl:59-61): out = [max|ap.Σ - a.Σ|, max|a.Σ|, max|ap.Σ|]
+__global__ void sigma_err_kernel(int Nsig, const double* __restrict__ a, const double* __restrict__ ap, double* out) {
+    double d = 0.0, ma = 0.0, mp = 0.0;
+    for (int k = threadIdx.x; k < Nsig; k += blockDim.x) {
+        d = fmax(d, fabs(ap[k] - a[k]));
+        ma = fmax(ma, fabs(a[k]));
+        mp = fmax(mp, fabs(ap[k]));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+        ma = fmax(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+        mp = fmax(mp, __shfl_xor_sync(0xffffffffu, mp, o));
+    }
+    if (threadIdx.x == 0) {
+        out[0] = d;
+        out[1] = ma;
+        out[2] = mp;
+    }
+}
+
 __global__ void to_float_kernel(const double* __restrict__ x, float* y, int64_t n) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
         y[e] = (float)x[e];
@@ -351,6 +371,11 @@ cudaError_t launch_axpby(const Layout& L, double alpha, const double* x, double 
                          bool gamma_too, cudaStream_t st) {
     const int64_t n = (sigma_too ? L.Nsig : 0) + (gamma_too ? L.C * 3 * L.chan : 0);
     axpby_kernel<<<grid_for(n, 256), 256, 0, st>>>(L, alpha, x, beta, y, sigma_too, gamma_too);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sigma_err(int Nsig, const double* a, const double* ap, double* out, cudaStream_t st) {
+    sigma_err_kernel<<<1, 32, 0, st>>>(Nsig, a, ap, out);
     return cudaGetLastError();
 }
 

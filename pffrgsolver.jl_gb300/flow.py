@@ -215,6 +215,17 @@ class FlowContext:
                                            ctypes.byref(amax)), "bs_step")
         return float(err.value), float(amax.value)
 
+    def parquet(self, Lam: float, eval_: int, gamma_tol=(1e-8, 1e-4), sigma_tol=(1e-8, 1e-4),
+                parquet_tol=(1e-8, 1e-4), beta=None, max_iter: int = 50):
+        """launch_parquet!'s fixed point (parquet.jl:43-80) on the action in slot A, in place on the
+        device; returns (iterations, absolute residual, relative residual)."""
+        beta = min(Lam, 1.0) if beta is None else beta
+        it, ea, er = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.pffrg_parquet(self.h, Lam, eval_, gamma_tol[0], gamma_tol[1], sigma_tol[0], sigma_tol[1],
+                                           parquet_tol[0], parquet_tol[1], beta, max_iter, ctypes.byref(it),
+                                           ctypes.byref(ea), ctypes.byref(er)), "parquet")
+        return it.value, ea.value, er.value
+
     def accept(self) -> None:
         self._check(self.lib.pffrg_accept(self.h), "accept")
 

@@ -488,29 +488,16 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
 
 def launch_parquet(ctx: FlowContext, r, m, a: A.Action, Lam: float, max_iter: int, min_eval: int, max_eval: int,
                    sigma_tol, gamma_tol, parquet_tol, beta=None, verbose: bool = False) -> int:
-    """Parquet fixed point of the SDE and the BSEs at cutoff Λ (parquet.jl:1-100); returns iterations."""
-    ap = A.Action.empty_like(a)
+    """Parquet fixed point of the SDE and the BSEs at cutoff Λ (parquet.jl:1-100); returns iterations.
+
+    The iteration runs on the device (``pffrg_parquet``): ``a`` is uploaded once, the SDE / BSE
+    evaluations, the residuals and the damping stay on the device, and the converged iterate is
+    downloaded into ``a`` at the end."""
     beta = min(Lam, 1.0) if beta is None else beta
     eval_ = get_eval(Lam, min_eval, max_eval)
-    gm = a.gamma_mask()
-    q3 = a.q3_mask()
-    abs_err = rel_err = math.inf
-    count = 1
-    while abs_err >= parquet_tol[0] and rel_err >= parquet_tol[1] and count <= max_iter:
-        s_abs = s_rel = math.inf
-        s_count = 1
-        while s_abs >= parquet_tol[0] and s_rel >= parquet_tol[1] and s_count <= max_iter:
-            ctx.compute_sigma_sde(Lam, a, ap, eval_, gamma_tol, sigma_tol)
-            s_abs = float(np.max(np.abs(ap.Σ - a.Σ)))
-            s_rel = s_abs / max(float(np.max(np.abs(a.Σ))), float(np.max(np.abs(ap.Σ))))
-            a.Σ[:] = (1.0 - beta) * a.Σ + beta * ap.Σ
-            s_count += 1
-        ctx.compute_gamma_bse(Lam, a, ap, eval_, gamma_tol)
-        diff = ap.buf[q3] - a.buf[q3]
-        abs_err = float(np.max(np.abs(diff))) if diff.size else 0.0
-        rel_err = abs_err / max(a.abs_max(), ap.abs_max())
-        if verbose:
-            print(f"parquet iteration {count}: rel err {rel_err:.3e}", flush=True)
-        a.buf[gm] = (1.0 - beta) * a.buf[gm] + beta * ap.buf[gm]
-        count += 1
-    return count - 1
+    ctx.upload(_capi.SLOT_A, a)
+    it, abs_err, rel_err = ctx.parquet(Lam, eval_, gamma_tol, sigma_tol, parquet_tol, beta, max_iter)
+    ctx.download(_capi.SLOT_A, a)
+    if verbose:
+        print(f"parquet: {it} iterations, residual {abs_err:.3e} (relative {rel_err:.3e})", flush=True)
+    return it
