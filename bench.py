@@ -62,11 +62,16 @@ def parse():
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     p.add_argument("--no-flow", action="store_true", help="skip the full-flow leg")
     p.add_argument("--flow-final", type=float, default=0.01, help="final cutoff of the full-flow leg")
-    p.add_argument("--flow-precisions", default="mixed,fp64", help="precisions of the full-flow leg")
+    p.add_argument("--flow-precisions", default="fp64,mixed", help="precisions of the full-flow leg")
+    p.add_argument("--flow", default="square-L3-1l", choices=sorted(FLOWS), help="workload of the full-flow leg")
+    p.add_argument("--no-replay", action="store_true", help="skip the mixed replay of the FP64 flow's steps")
     p.add_argument("--sweep", type=int, default=0,
                    help="instances of the coupling-sweep leg (square J1-J2, L in 3,4,5,6,8; 0: skip)")
     p.add_argument("--warm-start", default="",
                    help="train,test counts of the learned parquet warm-start leg (honeycomb J1-J2-J3; empty: skip)")
+    p.add_argument("--warm-lambda", type=float, default=2.0, help="cutoff of the warm-start leg's parquet solves")
+    p.add_argument("--warm-meshes", default="25/15/10", help="positive σ/Ω/ν frequencies of the warm-start leg")
+    p.add_argument("--warm-k", type=int, default=32, help="principal components of the warm start")
     return p.parse_args()
 
 
@@ -378,26 +383,55 @@ def ours(args):
 # the full flow of the square-lattice case: L = 3, nearest-neighbour Heisenberg, 1 loop, 50/15/10
 # frequencies, bare couplings at Λ = 50 (no parquet start), Bogacki-Shampine tolerance 1e-3, χ at
 # every accepted step; both precisions pass the same checkpoints, where their χ(ω = 0) is compared
-FLOW = dict(name="square", size=3, model="heisenberg", symmetry="su2", J=[[1.0]], num_sigma=50, num_omega=15,
-            num_nu=10, num_chi=10, initial=50.0, ode_tol=(1e-3, 1e-3), parquet=False, loops=1)
+FLOWS = {
+    "square-L3-1l": dict(name="square", size=3, model="heisenberg", symmetry="su2", J=[[1.0]], num_sigma=50,
+                         num_omega=15, num_nu=10, num_chi=10, initial=50.0, ode_tol=(1e-3, 1e-3), parquet=False,
+                         loops=1),
+    # the flow of the benchmark lattice: pyrochlore L = 6, nearest-neighbour Heisenberg, 2 loops, same meshes
+    "pyrochlore-L6-2l": dict(name="pyrochlore", size=6, model="heisenberg", symmetry="su2", J=[[1.0]],
+                             num_sigma=50, num_omega=15, num_nu=10, num_chi=10, initial=50.0, ode_tol=(1e-3, 1e-3),
+                             parquet=False, loops=2),
+}
 FLOW_CPS = [10.0, 5.0, 2.0, 1.0, 0.5, 0.2, 0.1, 0.05, 0.02]
 
 
+def _chi0(res):
+    """χ(ω = 0) of every site at every measured cutoff of a run (the χ meshes adapt, ω = 0 stays)."""
+    return {round(L, 12): c[:, 0] for (L, mesh, c) in res.chi}
+
+
+def _chi_err(cm, cf, keys):
+    errs = {}
+    for L in keys:
+        a, b = cm.get(round(L, 12)), cf.get(round(L, 12))
+        if a is not None and b is not None:
+            errs[str(L)] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    return errs
+
+
 def flow_leg(args, dev_index):
-    """Seconds of full flows (ODE steps, χ, resampling) per precision and χ(ω=0) of the mixed flow
-    against the FP64 flow at the shared checkpoints."""
+    """Full flows (ODE steps, χ after every accepted step, resampling) of one workload, Λ 50 -> final, in
+    FP64 and mixed precision: seconds, steps and χ(ω = 0) of the mixed flow against the FP64 flow at the
+    shared checkpoints.  The mixed right-hand side also replays the FP64 flow's accepted (Λ, dΛ)
+    sequence, so that its χ at every one of those cutoffs differs from the FP64 one by the arithmetic
+    alone (the two free-running flows choose their steps from their own error ratios)."""
     from pffrg_gb300.launcher import launch
 
+    kw = dict(FLOWS[args.flow])
+    name, size, model, sym, J = (kw.pop(k) for k in ("name", "size", "model", "symmetry", "J"))
     runs = {}
     for prec in [s for s in args.flow_precisions.split(",") if s]:
-        kw = dict(FLOW)
-        name, size, model, sym, J = (kw.pop(k) for k in ("name", "size", "model", "symmetry", "J"))
         t0 = time.perf_counter()
         res = launch("", name, size, model, sym, J, final=args.flow_final, cps=FLOW_CPS, precision=prec,
                      device=dev_index, **kw)
         runs[prec] = (time.perf_counter() - t0, res)
-    out = {"workload": "square L=3 Heisenberg, 1 loop, 50/15/10, Λ 50 -> %g, ODE tol 1e-3, bare start"
-                       % args.flow_final}
+    if "fp64" in runs and "mixed" in runs and not args.no_replay:
+        t0 = time.perf_counter()
+        res = launch("", name, size, model, sym, J, final=args.flow_final, cps=FLOW_CPS, precision="mixed",
+                     device=dev_index, schedule=runs["fp64"][1].steps, **kw)
+        runs["mixed_replay"] = (time.perf_counter() - t0, res)
+    out = {"workload": "%s L=%d Heisenberg, %d loop, %d/%d/%d, Λ 50 -> %g, ODE tol 1e-3, bare start"
+                       % (name, size, kw["loops"], kw["num_sigma"], kw["num_omega"], kw["num_nu"], args.flow_final)}
     for prec, (secs, res) in runs.items():
         out[prec] = {"seconds": secs, "accepted_steps": len(res.Lam), "rejected_steps": res.rejected,
                      "final_lambda": res.Lam[-1] if res.Lam else None, "reason": res.reason or "final cutoff",
@@ -405,14 +439,16 @@ def flow_leg(args, dev_index):
                      "rhs_evaluations": res.rhs_evals}
     if "mixed" in runs and "fp64" in runs:
         out["speedup_mixed_vs_fp64"] = runs["fp64"][0] / runs["mixed"][0]
-        cm = {round(L, 12): c[:, 0] for (L, mesh, c) in runs["mixed"][1].chi}
-        cf = {round(L, 12): c[:, 0] for (L, mesh, c) in runs["fp64"][1].chi}
-        errs = {}
-        for L in FLOW_CPS:
-            a, b = cm.get(round(L, 12)), cf.get(round(L, 12))
-            if a is not None and b is not None:
-                errs[str(L)] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
-        out["chi_static_rel_err_mixed_vs_fp64"] = errs
+        cf = _chi0(runs["fp64"][1])
+        out["chi_static_rel_err_mixed_vs_fp64"] = _chi_err(_chi0(runs["mixed"][1]), cf, FLOW_CPS)
+        if "mixed_replay" in runs:
+            cr = _chi0(runs["mixed_replay"][1])
+            every = _chi_err(cr, cf, [L for (L, mesh, c) in runs["fp64"][1].chi])
+            out["chi_static_rel_err_replay_vs_fp64"] = {
+                "checkpoints": _chi_err(cr, cf, FLOW_CPS),
+                "max_over_steps": max(every.values()) if every else None,
+                "steps_compared": len(every),
+                "steps_above_1e-6": sum(1 for v in every.values() if v > 1e-6)}
     return out
 
 
@@ -453,35 +489,62 @@ def warm_start_leg(args, dev_index):
     from pffrg_gb300.warmstart import ParquetWarmStart, coupling_features, vertex_mask
 
     n_train, n_test = (int(x) for x in args.warm_start.split(","))
-    kw = dict(num_sigma=20, num_omega=8, num_nu=6, num_chi=4, initial=5.0, final=5.0, parquet=True,
-              parquet_tol=(1e-8, 1e-8), max_iter=200, precision="fp64", correlations=False, device=dev_index)
+    Lam = args.warm_lambda
+    sizes = dict(zip(("num_sigma", "num_omega", "num_nu"), (int(x) for x in args.warm_meshes.split("/"))))
+    kw = dict(num_chi=4, initial=Lam, final=Lam, parquet=True, parquet_tol=(1e-8, 1e-8), max_iter=200,
+              precision="fp64", correlations=False, device=dev_index, **sizes)
     rng = np.random.default_rng(3)
     J = [[[1.0], [float(a)], [float(b)]] for a, b in rng.uniform(0.0, 0.5, size=(n_train + n_test, 2))]
     t0 = time.perf_counter()
-    feats, verts, it_train = [], [], []
+    feats, verts = [], []
     for j in J[:n_train]:
         res = launch("", "honeycomb", 5, "heisenberg", "su2", j, **kw)
         feats.append(coupling_features(j))
         verts.append(res.action.buf[vertex_mask(res.action)].copy())
-        it_train.append(res.parquet_iterations)
     t_data = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ws = ParquetWarmStart(k=32, hidden=(64, 64))
+    ws = ParquetWarmStart(k=args.warm_k, hidden=(64, 64))
     loss = ws.fit(feats, verts, epochs=8000, lr=3e-3)
     t_fit = time.perf_counter() - t0
-    bare, warm, diffs = [], [], []
+
+    class Part:
+        """A start predicted by one part of the fitted model (the ablation)."""
+
+        def __init__(self, part):
+            self.part = part
+
+        def predict(self, f):
+            return ws.predict(f, self.part)
+
+    starts = {"bare": None, "mean": Part("mean"), "lsq": Part("lsq"), "full": Part("full")}
+    its = {k: [] for k in starts}
+    start_err = {k: [] for k in starts if k != "bare"}
+    diffs, rates = [], []
     for j in J[n_train:]:
-        r0 = launch("", "honeycomb", 5, "heisenberg", "su2", j, **kw)
-        r1 = launch("", "honeycomb", 5, "heisenberg", "su2", j, warm_start=ws, **kw)
-        bare.append(r0.parquet_iterations)
-        warm.append(r1.parquet_iterations)
-        msk = vertex_mask(r0.action)
-        diffs.append(float(np.max(np.abs(r0.action.buf[msk] - r1.action.buf[msk])) / np.max(np.abs(r0.action.buf[msk]))))
-    return {"workload": "honeycomb J1-J2-J3 L=5, (J2,J3) ~ U[0,0.5]^2 seed 3, 20/8/6, Λ=5, residual 1e-8, FP64",
-            "train": n_train, "test": n_test, "data_seconds": t_data, "fit_seconds": t_fit, "fit_loss": loss,
-            "iterations_bare_mean": float(np.mean(bare)), "iterations_learned_mean": float(np.mean(warm)),
-            "iteration_ratio": float(np.mean(bare) / max(np.mean(warm), 1e-9)),
-            "max_vertex_rel_diff": max(diffs)}
+        ref = None
+        for name, st in starts.items():
+            r = launch("", "honeycomb", 5, "heisenberg", "su2", j, warm_start=st, **kw)
+            its[name].append(r.parquet_iterations)
+            msk = vertex_mask(r.action)
+            if ref is None:
+                ref = r.action.buf[msk].copy()
+                h = r.parquet_residuals
+                if len(h) > 2:  # geometric contraction of the bare iteration's residual
+                    rates.append(float((h[-1] / h[1]) ** (1.0 / (len(h) - 2))))
+                continue
+            scale = float(np.max(np.abs(ref)))
+            start_err[name].append(float(np.max(np.abs(st.predict(coupling_features(j)) - ref))) / scale)
+            diffs.append(float(np.max(np.abs(r.action.buf[msk] - ref))) / scale)
+    mean_it = {k: float(np.mean(v)) for k, v in its.items()}
+    return {"workload": "honeycomb J1-J2-J3 L=5, (J2,J3) ~ U[0,0.5]^2 seed 3, %s, Λ=%g, residual 1e-8, FP64"
+                        % (args.warm_meshes, Lam),
+            "train": n_train, "test": n_test, "components": args.warm_k, "data_seconds": t_data,
+            "fit_seconds": t_fit, "fit_loss": loss,
+            "iterations_mean": mean_it,
+            "iteration_ratio": {k: mean_it["bare"] / max(v, 1e-9) for k, v in mean_it.items() if k != "bare"},
+            "start_error_median": {k: float(np.median(v)) for k, v in start_err.items()},
+            "bare_contraction_per_iteration_median": float(np.median(rates)) if rates else None,
+            "max_converged_vertex_rel_diff": max(diffs) if diffs else None}
 
 
 def fp64_leg(args, ctx, pkg, C, a, rhs, flush, dev, da_mixed):

@@ -122,10 +122,11 @@ int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
  * rel < tol_rel or max_iter iterations (the reference's beta is min(Λ, 1)).
  * Slots DA and ERR are overwritten.  The actions stay on the device; only the
  * three error norms of an iteration are read back to steer the loop.  Returns
- * the iterations run and the last residuals. */
+ * the iterations run and the last residuals; residuals (NULL or max_iter
+ * entries) receives the absolute residual of every iteration. */
 int pffrg_parquet(pffrg_ctx* ctx, double Lam, int eval, double gamma_atol, double gamma_rtol, double sigma_atol,
                   double sigma_rtol, double tol_abs, double tol_rel, double beta, int max_iter, int* iterations,
-                  double* abs_err, double* rel_err);
+                  double* abs_err, double* rel_err, double* residuals);
 
 /* ---- device-resident interface (no host copies inside the step) ---- */
 

@@ -109,7 +109,7 @@ def load():
     L.pffrg_set_chi_integrand.argtypes = [vp, ctypes.c_int]
     L.pffrg_set_capacities.argtypes = [vp, ctypes.c_int64, ctypes.c_int64]
     L.pffrg_parquet.argtypes = [vp, d, ctypes.c_int, d, d, d, d, d, d, d, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
-                                ctypes.POINTER(d), ctypes.POINTER(d)]
+                                ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d)]
     L.pffrg_set_overlap_staging.argtypes = [vp, ctypes.c_int]
     ip = ctypes.POINTER(ctypes.c_int)
     L.pffrg_autotune_team_shape.argtypes = [vp, ctypes.c_int, d, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d, d, d,

@@ -518,7 +518,10 @@ int sigma_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* aux, do
     return 0;
 }
 
-int to_f(pffrg_ctx* ctx, const double* x, float* y) {
+// FP32 copy of an action for the mixed passes (SU(2): the pair layout of Layout::pq); the FP64
+// source is remembered for the FP64 hand-off pass.  `plain` keeps the FP64 layout (the FP32 χ
+// integrand reads it).
+int to_f(pffrg_ctx* ctx, const double* x, float* y, bool plain = false) {
     for (int k = 0; k < 4; ++k)
         if (ctx->f_copy[k] == y || !ctx->f_copy[k]) {
             ctx->f_copy[k] = y;
@@ -526,7 +529,8 @@ int to_f(pffrg_ctx* ctx, const double* x, float* y) {
             break;
         }
     ++ctx->launches;
-    CK(launch_to_float(x, y, ctx->L.total, ctx->st));
+    if (ctx->L.C == 2 && !plain) CK(launch_to_float_pairs(ctx->L, x, y, ctx->st));
+    else CK(launch_to_float(x, y, ctx->L.total, ctx->st));
     return 0;
 }
 
@@ -589,7 +593,7 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     c.af = nullptr;
     if (ctx->precision == PFFRG_MIXED && !ctx->chi_fp64) {
         // FP32 integrand on the FP32 copy (float-float node setup), cubature sums and errors in FP64
-        if (int rc = to_f(ctx, a, ctx->f_a)) return rc;
+        if (int rc = to_f(ctx, a, ctx->f_a, true)) return rc;
         c.af = ctx->f_a;
     }
     c.mesh = ctx->mesh;
@@ -966,9 +970,10 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
          dalloc((void**)&ctx->da_temp, sizeof(double) * L.total) &&
          dalloc((void**)&ctx->da_sig, sizeof(double) * L.total) &&
          dalloc((void**)&ctx->sig_tmp, sizeof(double) * L.Nsig) &&
-         dalloc((void**)&ctx->f_a, sizeof(float) * L.total) && dalloc((void**)&ctx->f_da, sizeof(float) * L.total) &&
-         dalloc((void**)&ctx->f_dal, sizeof(float) * L.total) &&
-         dalloc((void**)&ctx->f_dtemp, sizeof(float) * L.total) &&
+         dalloc((void**)&ctx->f_a, sizeof(float) * (L.total + 2)) &&
+         dalloc((void**)&ctx->f_da, sizeof(float) * (L.total + 2)) &&
+         dalloc((void**)&ctx->f_dal, sizeof(float) * (L.total + 2)) &&
+         dalloc((void**)&ctx->f_dtemp, sizeof(float) * (L.total + 2)) &&
          dalloc((void**)&ctx->corrs, sizeof(double) * 6 * L.NO) &&
          dalloc((void**)&ctx->corrs_sde, sizeof(double) * 6 * L.NO) &&
          dalloc((void**)&ctx->partial, sizeof(double) * kPartials) &&
@@ -1293,7 +1298,7 @@ int pffrg_bse(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a1, pffrg_act
 
 int pffrg_parquet(pffrg_ctx* ctx, double Lam, int eval, double gatol, double grtol, double satol, double srtol,
                   double tol_abs, double tol_rel, double beta, int max_iter, int* iterations, double* abs_err,
-                  double* rel_err) {
+                  double* rel_err, double* residuals) {
     if (!ctx) return PFFRG_E_ARGS;
     if (eval < 1 || max_iter < 0 || !(beta > 0.0) || beta > 1.0)
         return ctx->fail(PFFRG_E_ARGS, "eval >= 1, max_iter >= 0 and 0 < beta <= 1 required");
@@ -1334,6 +1339,7 @@ int pffrg_parquet(pffrg_ctx* ctx, double Lam, int eval, double gatol, double grt
         CK(cudaMemcpyAsync(h, ctx->scalars, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));
         ea = h[0];
+        if (residuals) residuals[count - 1] = ea;
         er = ea / std::max(h[1], h[2]);
         ++count;
     }

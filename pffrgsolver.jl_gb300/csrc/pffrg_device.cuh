@@ -26,6 +26,14 @@ struct Layout {
         int64_t b = Nsig + c * comp + Ns + ch * chan;
         return b + (k == 0 ? 0 : (k == 1 ? K1 : (k == 2 ? K1 + K2 : K1 + 2 * K2)));
     }
+    // The FP32 copies of the mixed path for SU(2) keep the two components of every vertex entry side
+    // by side (one 8-byte read fetches spin and density): Σ[Nsig] padded to an even length, then
+    // bare[Ns] and ch s, t, u: q1 q2_1 q2_2 q3 as (spin, density) pairs.  Offsets in pairs.
+    __host__ __device__ int64_t pbare() const { return (Nsig + 1) / 2; }
+    __host__ __device__ int64_t pq(int ch, int k) const {
+        return pbare() + Ns + ch * chan + (k == 0 ? 0 : (k == 1 ? K1 : (k == 2 ? K1 + K2 : K1 + 2 * K2)));
+    }
+    __host__ __device__ int64_t pair_floats() const { return 2 * (pbare() + comp); }
 };
 
 inline Layout make_layout(int Ns, int Nsig, int NO, int Nn, int C) {

@@ -50,6 +50,7 @@ constexpr int kWarps = 4;
 
 template <typename R, int C>
 struct NodeScratch {
+    double x;      // the node (integration variable v)
     R p_half[2];
     R loc[2 * C];  // t channel: local vertices v3[C], v4[C] at site 1
     Plan<R> plan[4][3];
@@ -179,6 +180,23 @@ template <typename R, int C>
 __device__ __forceinline__ R gather_one(const PassArgs<R>& A, const NodeScratch<R, C>& ns, int slot, int c, int i,
                                         int exch_i) {
     const R* __restrict__ src = A.src[slot];
+    if constexpr (sizeof(R) == 4 && C == 2) {
+        // FP32 copies of SU(2) actions hold (spin, density) pairs
+        const float* __restrict__ s2 = src + c;
+        R val = ldg(s2 + 2 * (A.L.pbare() + i));
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            const Plan<R>& P = ns.plan[slot][ch];
+            if (P.kernel) {
+                const float* q = s2 + 2 * A.L.pq(P.src_ch, P.kernel - 1);
+                const int s = P.exch ? exch_i : i;
+                R acc = P.w[0] * ldg(q + 2 * (P.off[0] + s));
+                for (int k = 1; k < corners_of(P.kernel); ++k) acc += P.w[k] * ldg(q + 2 * (P.off[k] + s));
+                val += (c == 1 ? P.sgn_d : (R)1) * acc;
+            }
+        }
+        return val;
+    }
     R val = ldg(src + A.L.bare(c) + i);
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
@@ -325,11 +343,12 @@ struct Team {
     int site_ex[SPL];       // exchange[site] of this lane's sites
     unsigned long long nodes, alg;
 
-    // Evaluate the integrand of channel X at up to NB nodes x[0..count) of one task:
-    // g[j][c][k] = Γ_c(site tl + k T; x_j).  Team-collective: all lanes of the warp call it
+    // Evaluate the integrand of channel X at the up to NB nodes ts.node[0..count).x of one task and
+    // hand each node's values to sink(j, g) in node order, g[c][k] = Γ_c(site tl + k T; x_j)
+    // (zero on the padding sites k T + tl >= Ns).  Team-collective: all lanes of the warp call it
     // together (inactive teams with count = 0).
-    __device__ void eval(const TaskInfo& ti, SetupT W, SetupT V, SetupT VP, const double* x, int count,
-                         R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
+    template <class Sink>
+    __device__ __forceinline__ void eval(const TaskInfo& ti, SetupT W, SetupT V, SetupT VP, int count, Sink& sink) {
         const int X = ti.X;
         const int Ns = A.L.Ns;
         const int nslots = (X == 1) ? 4 : 2;
@@ -345,7 +364,8 @@ struct Team {
         for (int it = tl; it < count * nitems; it += T) {
             const int j = it / nitems, item = it - j * nitems;
             NodeScratch<R, C>& ns = ts.node[j];
-            const SetupT v = SetupT(x[j]);
+            const double xj = ns.x;
+            const SetupT v = SetupT(xj);
             if (item < nprop) {
                 if constexpr (sizeof(R) == 4)
                     ns.p_half[item] = prop_half_ff(A.prop_kind, item, X, M, A.L.Nsig, A.prop_a, A.prop_da,
@@ -369,7 +389,7 @@ struct Team {
                             const MeshG<double> M64 = mesh_view(A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
                             double W64, V64, VP64, b0, b1, b2;
                             task_freqs(A, M64, ti, W64, V64, VP64);
-                            slot_arg<double>(X, slot, ch, x[j], W64, V64, VP64, b0, b1, b2);
+                            slot_arg<double>(X, slot, ch, xj, W64, V64, VP64, b0, b1, b2);
                             make_plan<R>(P, ch, b0, b1, b2, M64, Ns, A.L.NO, A.L.Nn);
                         } else {
                             make_plan_ff(P, ch, a0, a1, a2, M, Ns, A.L.NO, A.L.Nn);
@@ -404,13 +424,13 @@ struct Team {
         }
         if constexpr (C == 2) {
             // every team of the warp passes the same two warp barriers, whatever its channel
-            eval_su2_nodes(X, count, g);
+            eval_su2_nodes(X, count, sink);
             __syncwarp();
-            if (X == 1) eval_t_overlap(count, g);
+            if (X == 1) eval_t_overlap(count, sink);
             __syncwarp();
             return;
         }
-        // phase B: gathers and per-site combination, node by node
+        // phase B of U(1)-DM: gathers and per-site combination, node by node
         for (int j = 0; j < mx; ++j) {
             const bool act = j < count;
             const NodeScratch<R, C>& ns = ts.node[act ? j : 0];
@@ -421,84 +441,139 @@ struct Team {
                 gather_slot<R, T, SPL, C>(A, ns, 0, tl, site_ex, v1);
                 gather_slot<R, T, SPL, C>(A, ns, 1, tl, site_ex, v2);
             }
-            if constexpr (C != 2) {
-                eval_u1dm(X, j, act, p, ns, v1, v2, g);
-                continue;
-            }
-            if (act && X != 1) {
-                const R two = (X == 0) ? (R)-2 : (R)2;
-#pragma unroll
-                for (int k = 0; k < SPL; ++k) {
-                    g[j][0][k] = -p * (two * v1[0][k] * v2[0][k] + v1[0][k] * v2[1][k] + v1[1][k] * v2[0][k]);
-                    g[j][1][k] = -p * ((R)3 * v1[0][k] * v2[0][k] + v1[1][k] * v2[1][k]);
-                }
-            }
-            const bool tch = act && X == 1;
-            if (tch) {
-#pragma unroll
-                for (int k = 0; k < SPL; ++k) {
-                    const int i = tl + k * T;
-                    if (i < Ns) {
-                        tmp[i] = v1[0][k];
-                        tmp[Ns + i] = v1[1][k];
-                        tmp[2 * Ns + i] = v2[0][k];
-                        tmp[3 * Ns + i] = v2[1][k];
-                    }
-                }
-            }
-            __syncwarp();
-            if (tch) {
-                const R v3s = ns.loc[0], v3d = ns.loc[1], v4s = ns.loc[2], v4d = ns.loc[3];
-                const R coef = -p * (R)-2;
-                const R twoS = (R)A.twoS;
-#pragma unroll
-                for (int k = 0; k < SPL; ++k) {
-                    const int i = tl + k * T;
-                    const R v1s = v1[0][k], v1d = v1[1][k], v2s = v2[0][k], v2d = v2[1][k];
-                    R Gs = -p * ((R)-1 * v1s * v4s + v1s * v4d - (R)1 * v3s * v2s + v3d * v2s);
-                    R Gd = -p * ((R)3 * v1d * v4s + v1d * v4d + (R)3 * v3s * v2d + v3d * v2d);
-                    if (i < Ns) {
-                        const int j0 = row_off[i], j1 = row_off[i + 1];
-                        for (int r = j0; r < j1; ++r) {
-                            const unsigned row = rows[r];
-                            const int ia = row & 0xff, ib = (row >> 8) & 0xff;
-                            const R mm = coef * (R)(row >> 16) * twoS;
-                            Gs += mm * tmp[ia] * tmp[2 * Ns + ib];
-                            Gd += mm * tmp[Ns + ia] * tmp[3 * Ns + ib];
-                        }
-                    }
-                    g[j][0][k] = Gs;
-                    g[j][1][k] = Gd;
-                }
-            }
-            __syncwarp();
+            eval_u1dm(X, j, act, p, ns, v1, v2, sink);
         }
     }
 
-    // phase B of SU(2), node by node (one gather site for all channels keeps the kernel small):
-    // the s and u bubbles (flow_su2_s.jl, flow_su2_u.jl) per site, or for the t channel
-    // (flow_su2_t.jl:46-81) the local part per site and both slots staged in shared memory as
-    // [site][node] (spin, density) pairs for the overlap sums that follow
-    __device__ void eval_su2_nodes(int X, int count, R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
+    // One non-local vertex slot of an SU(2) node on this lane's sites (get_Γ_avx!,
+    // action_su2.jl:115-134): bare + Σ_ch sgn Σ_q w_q q[off_q + site], channels in the reference's
+    // order.  The loop over the lane's sites has no branch (padding sites read site 0 and are zeroed
+    // at the end), so the reads of all corners, both components and all sites of a channel can be
+    // in flight together.
+    __device__ __forceinline__ void gather_su2(const NodeScratch<R, C>& ns, int slot, R v[2][SPL]) {
+        const int Ns = A.L.Ns;
+        const R* __restrict__ src = A.src[slot];
+        int si[SPL];
+#pragma unroll
+        for (int k = 0; k < SPL; ++k) {
+            const int i = tl + k * T;
+            si[k] = i < Ns ? i : 0;
+        }
+        if constexpr (sizeof(R) == 4) {
+            // FP32 copies hold (spin, density) pairs: one 8-byte read per corner and site
+            const float2* __restrict__ src2 = reinterpret_cast<const float2*>(src);
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const float2 b = ldg(src2 + A.L.pbare() + si[k]);
+                v[0][k] = b.x;
+                v[1][k] = b.y;
+            }
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                const Plan<R>& P = ns.plan[slot][ch];
+                const int kern = P.kernel;
+                if (!kern) continue;
+                const int nc = corners_of(kern);
+                const float2* q = src2 + A.L.pq(P.src_ch, kern - 1);
+                const R sgn_d = P.sgn_d;
+                const int ex = P.exch;
+                R w[8];
+                int off[8];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    w[c] = c < nc ? P.w[c] : (R)0;
+                    off[c] = c < nc ? P.off[c] : 0;
+                }
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) {
+                    const int st = ex ? site_ex[k] : si[k];
+                    R a0 = (R)0, a1 = (R)0;
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        if (c < nc) {
+                            const float2 t = ldg(q + off[c] + st);
+                            a0 += w[c] * t.x;
+                            a1 += w[c] * t.y;
+                        }
+                    }
+                    v[0][k] += a0;
+                    v[1][k] += sgn_d * a1;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < SPL; ++k)
+                if (tl + k * T >= Ns) v[0][k] = v[1][k] = (R)0;
+            return;
+        }
+#pragma unroll
+        for (int k = 0; k < SPL; ++k) {
+            v[0][k] = ldg(src + A.L.bare(0) + si[k]);
+            v[1][k] = ldg(src + A.L.bare(1) + si[k]);
+        }
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            const Plan<R>& P = ns.plan[slot][ch];
+            const int kern = P.kernel;
+            if (!kern) continue;
+            const int nc = corners_of(kern);
+            const R* q0 = src + A.L.qbase(0, P.src_ch, kern - 1);
+            const R* q1 = src + A.L.qbase(1, P.src_ch, kern - 1);
+            const R sgn_d = P.sgn_d;
+            const int ex = P.exch;
+            R w[8];
+            int off[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                w[q] = q < nc ? P.w[q] : (R)0;
+                off[q] = q < nc ? P.off[q] : 0;
+            }
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int st = ex ? site_ex[k] : si[k];
+                R a0 = (R)0, a1 = (R)0;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    if (q < nc) {
+                        a0 += w[q] * ldg(q0 + off[q] + st);
+                        a1 += w[q] * ldg(q1 + off[q] + st);
+                    }
+                }
+                v[0][k] += a0;
+                v[1][k] += sgn_d * a1;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < SPL; ++k)
+            if (tl + k * T >= Ns) v[0][k] = v[1][k] = (R)0;
+    }
+
+    // phase B of SU(2), node by node: the s and u bubbles (flow_su2_s.jl, flow_su2_u.jl) per site,
+    // handed to the sink, or for the t channel (flow_su2_t.jl:46-81) the local part per site kept in
+    // shared memory and both slots staged as [site][node] (spin, density) pairs for the overlap sums
+    template <class Sink>
+    __device__ __forceinline__ void eval_su2_nodes(int X, int count, Sink& sink) {
         constexpr int NB = BatchOf<T, C, SPL>::NB;
         using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
         const int Ns = A.L.Ns;
         constexpr int SS = t_site_stride<R, NB>();
         R2* tb1 = reinterpret_cast<R2*>(tmp);  // [Ns][SS]
         R2* tb2 = tb1 + (size_t)Ns * SS;
+        R2* tloc = tb2 + (size_t)Ns * SS + (size_t)Ns * NB;  // [Ns][NB] local parts (after the overlap sums)
         const R two = (X == 0) ? (R)-2 : (R)2;
         for (int j = 0; j < count; ++j) {
             const NodeScratch<R, C>& ns = ts.node[j];
             const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
-            R v1[C][SPL], v2[C][SPL];
-            gather_slot<R, T, SPL, C>(A, ns, 0, tl, site_ex, v1);
-            gather_slot<R, T, SPL, C>(A, ns, 1, tl, site_ex, v2);
+            R v1[2][SPL], v2[2][SPL];
+            gather_su2(ns, 0, v1);
+            gather_su2(ns, 1, v2);
             if (X != 1) {
+                R g[2][SPL];
 #pragma unroll
                 for (int k = 0; k < SPL; ++k) {
-                    g[j][0][k] = -p * (two * v1[0][k] * v2[0][k] + v1[0][k] * v2[1][k] + v1[1][k] * v2[0][k]);
-                    g[j][1][k] = -p * ((R)3 * v1[0][k] * v2[0][k] + v1[1][k] * v2[1][k]);
+                    g[0][k] = -p * (two * v1[0][k] * v2[0][k] + v1[0][k] * v2[1][k] + v1[1][k] * v2[0][k]);
+                    g[1][k] = -p * ((R)3 * v1[0][k] * v2[0][k] + v1[1][k] * v2[1][k]);
                 }
+                sink(j, g);
                 continue;
             }
             const R v3s = ns.loc[0], v3d = ns.loc[1], v4s = ns.loc[2], v4d = ns.loc[3];
@@ -506,9 +581,10 @@ struct Team {
             for (int k = 0; k < SPL; ++k) {
                 const int i = tl + k * T;
                 const R v1s = v1[0][k], v1d = v1[1][k], v2s = v2[0][k], v2d = v2[1][k];
-                g[j][0][k] = -p * ((R)-1 * v1s * v4s + v1s * v4d - (R)1 * v3s * v2s + v3d * v2s);
-                g[j][1][k] = -p * ((R)3 * v1d * v4s + v1d * v4d + (R)3 * v3s * v2d + v3d * v2d);
                 if (i < Ns) {
+                    const R Gs = -p * ((R)-1 * v1s * v4s + v1s * v4d - (R)1 * v3s * v2s + v3d * v2s);
+                    const R Gd = -p * ((R)3 * v1d * v4s + v1d * v4d + (R)3 * v3s * v2d + v3d * v2d);
+                    tloc[(size_t)i * NB + j] = R2{Gs, Gd};
                     tb1[(size_t)i * SS + j] = R2{v1s, v1d};
                     tb2[(size_t)i * SS + j] = R2{v2s, v2d};
                 }
@@ -520,9 +596,11 @@ struct Team {
     // are (node j of the batch, row group q of G = T / NB): all lanes walk the sites in the same
     // order, a lane adds every G-th row of a site for its node (the row word is the same for the NB
     // lanes of a group, the vertex pairs of neighbouring nodes are neighbours in shared memory),
-    // the G partial sums meet by shuffles, and the owner of a site scales its nodes' sums by
-    // -p (-2) (2S) at the end.  Nodes past `count` hold stale values whose sums are never used.
-    __device__ void eval_t_overlap(int count, R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
+    // the G partial sums meet by shuffles, and the owner of a site adds -p (-2) (2S) times them to
+    // its nodes' local parts and hands the nodes to the sink.  Nodes past `count` hold stale values
+    // whose sums are never used.
+    template <class Sink>
+    __device__ __forceinline__ void eval_t_overlap(int count, Sink& sink) {
         constexpr int NB = BatchOf<T, C, SPL>::NB;
         constexpr int G = T / NB;  // row groups per node
         using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
@@ -531,6 +609,7 @@ struct Team {
         const R2* tb1 = reinterpret_cast<const R2*>(tmp);
         const R2* tb2 = tb1 + (size_t)Ns * SS;
         R2* ov = const_cast<R2*>(tb2) + (size_t)Ns * SS;  // [Ns][NB] overlap sums
+        const R2* tloc = ov + (size_t)Ns * NB;
         const int j = tl % NB, q = tl / NB;
         const unsigned team_mask = (T == 32) ? kFull : (((1u << T) - 1u) << ((threadIdx.x & 31) / T * T));
         for (int i = 0; i < Ns; ++i) {
@@ -554,27 +633,33 @@ struct Team {
         __syncwarp(team_mask);
         const R twoS = (R)A.twoS;
 #pragma unroll
-        for (int k = 0; k < SPL; ++k) {
-            const int i = tl + k * T;
-            if (i >= Ns) continue;
+        for (int jj = 0; jj < NB; ++jj) {
+            if (jj >= count) continue;
+            const NodeScratch<R, C>& ns = ts.node[jj];
+            const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
+            const R coef = -p * (R)-2 * twoS;
+            R g[2][SPL];
 #pragma unroll
-            for (int jj = 0; jj < NB; ++jj) {
-                if (jj >= count) continue;
-                const NodeScratch<R, C>& ns = ts.node[jj];
-                const R p = ns.p_half[0] + (A.prop_kind == PROP_KAT ? ns.p_half[1] : (R)0);
-                const R coef = -p * (R)-2 * twoS;
-                const R2 s = ov[(size_t)i * NB + jj];
-                g[jj][0][k] += coef * s.x;
-                g[jj][1][k] += coef * s.y;
+            for (int k = 0; k < SPL; ++k) {
+                const int i = tl + k * T;
+                g[0][k] = g[1][k] = (R)0;
+                if (i < Ns) {
+                    const R2 lo = tloc[(size_t)i * NB + jj], s = ov[(size_t)i * NB + jj];
+                    g[0][k] = lo.x + coef * s.x;
+                    g[1][k] = lo.y + coef * s.y;
+                }
             }
+            sink(jj, g);
         }
     }
 
     // phase B of one node for U(1)-DM (flow_u1_dm_{s,t,u}.jl); team-collective like eval
+    template <class Sink>
     __device__ void eval_u1dm(int X, int j, bool act, R p, const NodeScratch<R, C>& ns, const R v1[C][SPL],
-                              const R v2[C][SPL], R g[BatchOf<T, C, SPL>::NB][C][SPL]) {
+                              const R v2[C][SPL], Sink& sink) {
         const int Ns = A.L.Ns;
         if (act && X != 1) {
+            R g[C][SPL];
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 R a[C], b[C], h[C];
@@ -586,14 +671,15 @@ struct Team {
                 if (X == 0) u1dm_s(a, b, h);
                 else u1dm_u(a, b, h);
 #pragma unroll
-                for (int c = 0; c < C; ++c) g[j][c][k] = -p * h[c];
+                for (int c = 0; c < C; ++c) g[c][k] = -p * h[c];
                 if (A.reduced) {
                     // the reduced s bubble of the SDE keeps xx, zz, dd (SDE_u1_dm.jl:38-46)
-                    g[j][2][k] = (R)0;
-                    g[j][4][k] = (R)0;
-                    g[j][5][k] = (R)0;
+                    g[2][k] = (R)0;
+                    g[4][k] = (R)0;
+                    g[5][k] = (R)0;
                 }
             }
+            sink(j, g);
         }
         const bool tch = act && X == 1;
         if (tch) {
@@ -612,6 +698,7 @@ struct Team {
         __syncwarp();
         if (tch) {
             const R coef = -p * (R)-2;
+            R g[C][SPL];
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 const int i = tl + k * T;
@@ -642,8 +729,9 @@ struct Team {
                     }
                 }
 #pragma unroll
-                for (int c = 0; c < C; ++c) g[j][c][k] = G[c];
+                for (int c = 0; c < C; ++c) g[c][k] = G[c];
             }
+            sink(j, g);
         }
         __syncwarp();
     }
@@ -713,9 +801,10 @@ __device__ __forceinline__ void task_freqs(const PassArgs<R>& A, const MeshG<dou
 template <typename R, int T, int C, int SPL>
 struct SmemLayout {
     static constexpr int NPW = 32 / T;
-    // t-channel staging per team: SU(2) both slots of the whole batch, U(1)-DM one node
+    // t-channel staging per team: SU(2) both slots, the overlap sums and the local parts of the
+    // whole batch, U(1)-DM one node
     __host__ __device__ static size_t tmp_per_team(int Ns) {
-        return C == 2 ? (size_t)4 * Ns * t_site_stride<R, BatchOf<T, C, SPL>::NB>() + (size_t)2 * Ns * BatchOf<T, C, SPL>::NB
+        return C == 2 ? (size_t)4 * Ns * t_site_stride<R, BatchOf<T, C, SPL>::NB>() + (size_t)4 * Ns * BatchOf<T, C, SPL>::NB
                       : (size_t)2 * C * Ns;
     }
     // the meshes of the node setup: float-float pairs and inverse spacings (mixed path) or FP64
@@ -942,14 +1031,16 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
         // all teams of the warp evaluate together (cnt = 0 for idle teams), NB nodes at a time
         R g[5][C][SPL];
         for (int b = 0; b < 5; b += NB) {
-            R gb[NB][C][SPL];
             const int nb = max(0, min(NB, cnt - b));
-            tm.eval(ti, W, V, VP, x + b, nb, gb);
-            for (int j = 0; j < NB && b + j < 5; ++j)
+            for (int j = tl; j < nb; j += T) tm.ts.node[j].x = x[b + j];
+            __syncwarp();
+            auto keep = [&](int j, const R (&gv)[C][SPL]) {
 #pragma unroll
                 for (int c = 0; c < C; ++c)
 #pragma unroll
-                    for (int k = 0; k < SPL; ++k) g[b + j][c][k] = gb[j][c][k];
+                    for (int k = 0; k < SPL; ++k) g[b + j][c][k] = gv[c][k];
+            };
+            tm.eval(ti, W, V, VP, nb, keep);
         }
         const bool simpson = valid && !boundary && cnt == 5;
         // simps!: 3-point sum, 5-point sum via residual! with n = 2, Richardson test
@@ -1042,9 +1133,10 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
 }
 
 // ---- wave k >= 1: evaluate queued chunks, one partial node sum per chunk ----
-// (FP32 kernels held to 128 registers: four blocks of 128 threads per SM)
+// (FP32 kernels held to 168 registers, three blocks of 128 threads per SM: measured 3 % faster than
+// four blocks at 128 registers, whose gathers spill, and 9 % faster than two)
 template <typename R, int T, int SPL, int C>
-__global__ void __launch_bounds__(kWarps * 32, sizeof(R) == 4 ? 4 : 1) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
+__global__ void __launch_bounds__(kWarps * 32, sizeof(R) == 4 ? 3 : 1) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1065,7 +1157,6 @@ __global__ void __launch_bounds__(kWarps * 32, sizeof(R) == 4 ? 4 : 1) eval_kern
     const int nchunks = min(Wsp.counters[par], Wsp.qcap);
     const long long nwarps = (long long)gridDim.x * kWarps;
     constexpr int NB = BatchOf<T, C, SPL>::NB;
-    R g[NB][C][SPL];
     for (long long base = ((long long)blockIdx.x * kWarps + warp) * NPW; base < nchunks; base += nwarps * NPW) {
         const int chunk = (int)(base + team);
         const bool valid = chunk < nchunks;
@@ -1096,22 +1187,24 @@ __global__ void __launch_bounds__(kWarps * 32, sizeof(R) == 4 ? 4 : 1) eval_kern
                 acc[c][k] = Acc<R>{(R)0, (R)0};
                 aab[c][k] = (R)0;
             }
+        // each node's values go straight into the chunk's compensated sums, in node order
+        auto add = [&](int, const R (&gv)[C][SPL]) {
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) {
+                    acc_add(acc[c][k], gv[c][k]);
+                    if constexpr (sizeof(R) == 4) aab[c][k] += fabsf(gv[c][k]);
+                }
+        };
         for (int b = 0; b < mx; b += NB) {
-            double x[NB];
             const int nb = max(0, min(NB, cnt - b));
-            for (int j = 0; j < nb; ++j) {
-                const long long nd = (long long)cr.y + b + j;  // 0-based new node of the level
-                x[j] = sgn * __dadd_rn(lo, __dmul_rn(2.0 * (double)(nd + 1) - 1.0, h));
+            if (tl < nb) {
+                const long long nd = (long long)cr.y + b + tl;  // 0-based new node of the level
+                tm.ts.node[tl].x = sgn * __dadd_rn(lo, __dmul_rn(2.0 * (double)(nd + 1) - 1.0, h));
             }
-            tm.eval(ti, W, V, VP, x, nb, g);
-            for (int j = 0; j < nb; ++j)
-#pragma unroll
-                for (int c = 0; c < C; ++c)
-#pragma unroll
-                    for (int k = 0; k < SPL; ++k) {
-                        acc_add(acc[c][k], g[j][c][k]);
-                        if constexpr (sizeof(R) == 4) aab[c][k] += fabsf(g[j][c][k]);
-                    }
+            __syncwarp();
+            tm.eval(ti, W, V, VP, nb, add);
         }
         if constexpr (sizeof(R) == 4) {
             if (A.esc_mode == 1) {

@@ -248,6 +248,8 @@ cudaError_t launch_symmetrize_add_to(const Layout& L, const int* exch, const dou
 cudaError_t launch_axpby(const Layout& L, double alpha, const double* x, double beta, double* y, bool sigma_too,
                          bool gamma_too, cudaStream_t st);
 cudaError_t launch_to_float(const double* x, float* y, int64_t n, cudaStream_t st);
+// the FP32 copy of an SU(2) action (C = 2) in the pair layout of the mixed passes (Layout::pq)
+cudaError_t launch_to_float_pairs(const Layout& L, const double* x, float* y, cudaStream_t st);
 // out = [max|ap.Σ - a.Σ|, max|a.Σ|, max|ap.Σ|] over the Nsig self-energy values
 cudaError_t launch_sigma_err(int Nsig, const double* a, const double* ap, double* out, cudaStream_t st);
 // *status |= 16 when any of a[0..n) is NaN or infinite

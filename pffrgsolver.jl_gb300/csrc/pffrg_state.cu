@@ -149,6 +149,18 @@ __global__ void sigma_err_kernel(int Nsig, const double* __restrict__ a, const d
     }
 }
 
+// FP32 copy of an SU(2) action with the two components of every entry side by side (Layout::pq):
+// Σ as is, then (spin, density) pairs of bare and every channel array
+__global__ void to_float_pairs_kernel(Layout L, const double* __restrict__ x, float* y) {
+    const int64_t np = L.comp;  // entries per component after Σ
+    float2* y2 = reinterpret_cast<float2*>(y) + L.pbare();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < np + L.Nsig;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        if (e < np) y2[e] = make_float2((float)x[L.Nsig + e], (float)x[L.Nsig + L.comp + e]);
+        else y[e - np] = (float)x[e - np];
+    }
+}
+
 __global__ void to_float_kernel(const double* __restrict__ x, float* y, int64_t n) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
         y[e] = (float)x[e];
@@ -381,6 +393,11 @@ cudaError_t launch_sigma_err(int Nsig, const double* a, const double* ap, double
 
 cudaError_t launch_check_finite(const double* a, int64_t n, int* status, cudaStream_t st) {
     finite_kernel<<<grid_for(n, 256), 256, 0, st>>>(a, n, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_float_pairs(const Layout& L, const double* x, float* y, cudaStream_t st) {
+    to_float_pairs_kernel<<<grid_for(L.comp + L.Nsig, 256), 256, 0, st>>>(L, x, y);
     return cudaGetLastError();
 }
 

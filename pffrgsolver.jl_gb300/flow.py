@@ -216,14 +216,19 @@ class FlowContext:
         return float(err.value), float(amax.value)
 
     def parquet(self, Lam: float, eval_: int, gamma_tol=(1e-8, 1e-4), sigma_tol=(1e-8, 1e-4),
-                parquet_tol=(1e-8, 1e-4), beta=None, max_iter: int = 50):
+                parquet_tol=(1e-8, 1e-4), beta=None, max_iter: int = 50, history: bool = False):
         """launch_parquet!'s fixed point (parquet.jl:43-80) on the action in slot A, in place on the
-        device; returns (iterations, absolute residual, relative residual)."""
+        device; returns (iterations, absolute residual, relative residual) and, with ``history``, the
+        absolute residual of every iteration as a fourth item."""
         beta = min(Lam, 1.0) if beta is None else beta
         it, ea, er = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        hist = np.zeros(max(1, max_iter))
         self._check(self.lib.pffrg_parquet(self.h, Lam, eval_, gamma_tol[0], gamma_tol[1], sigma_tol[0], sigma_tol[1],
                                            parquet_tol[0], parquet_tol[1], beta, max_iter, ctypes.byref(it),
-                                           ctypes.byref(ea), ctypes.byref(er)), "parquet")
+                                           ctypes.byref(ea), ctypes.byref(er),
+                                           hist.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "parquet")
+        if history:
+            return it.value, ea.value, er.value, hist[:it.value].copy()
         return it.value, ea.value, er.value
 
     def accept(self) -> None:

@@ -216,12 +216,14 @@ class FlowResult:
     err: list = field(default_factory=list)
     abs_max: list = field(default_factory=list)
     rejected: int = 0
+    steps: list = field(default_factory=list)     # (Λ before, dΛ taken) of every accepted step
     # wall seconds per part of the loop (the reference's timers, src/Flow/timers.jl): ODE steps on the
     # device, correlations, host transfers and resampling
     timers: dict = field(default_factory=lambda: {"steps": 0.0, "chi": 0.0, "transfer": 0.0, "resample": 0.0})
     rhs_evals: int = 0
     integrand_evals: int = 0
     parquet_iterations: int = 0
+    parquet_residuals: list = field(default_factory=list)  # absolute residual of every parquet iteration
     seconds: float = 0.0
     finished: bool = False
     reason: str = ""
@@ -289,7 +291,7 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
            loops: int = 1, parquet: bool = True, sigma_corr: bool = True, initial: float = 5.0,
            final: float = 0.05, bmin: float = 1e-4, bmax: float = 0.1, cps=(), overwrite: bool = True,
            wt: float = 23.5, ct: float = 1.0, precision: str = "mixed", device: int = 0, measure=None,
-           correlations: bool = True, warm_start=None, verbose: bool = False) -> FlowResult:
+           correlations: bool = True, warm_start=None, verbose: bool = False, schedule=None) -> FlowResult:
     """Run the FRG flow from ``initial`` to ``final`` (launch!, Launcher.jl:565-773).
 
     After every accepted step the static correlations χ of the new state are
@@ -302,7 +304,9 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
     HDF5 files; ``overwrite = False`` resumes from the last checkpoint of
     existing files (Launcher.jl:704-760).  ``warm_start`` (a fitted
     ``warmstart.ParquetWarmStart``) starts the parquet iteration from its
-    predicted vertex instead of the bare couplings.
+    predicted vertex instead of the bare couplings.  ``schedule`` (another
+    run's ``steps``) replays that run's accepted (Λ, dΛ) sequence instead of
+    choosing step sizes: the two runs then differ by their arithmetic only.
     """
     t0 = time.perf_counter()
     if symmetry not in A.SYMMETRIES:
@@ -350,7 +354,8 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
                 mask = vertex_mask(a)
                 a.buf[mask] = warm_start.predict(coupling_features(J))
             res.parquet_iterations = launch_parquet(ctx, r, m, a, initial, max_iter, min_eval, max_eval, sigma_tol,
-                                                    gamma_tol, parquet_tol, verbose=verbose)
+                                                    gamma_tol, parquet_tol, verbose=verbose,
+                                                    residuals=res.parquet_residuals)
             if out:
                 # the parquet solution is measured and checkpointed (parquet.jl:96-98)
                 ctx.upload(_capi.SLOT_NEXT, a)
@@ -359,7 +364,7 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
         _flow(ctx, r, m, a, res, loops=loops, sigma_corr=sigma_corr and loops >= 3, Li=Li, Lf=final,
               dLi=dLi, bmin=bmin, bmax=bmax, min_eval=min_eval, max_eval=max_eval, sigma_tol=sigma_tol,
               gamma_tol=gamma_tol, ode_tol=ode_tol, p=p, cps=list(cps), measure=measure,
-              chi_tol=chi_tol if correlations or out else None, out=out, verbose=verbose)
+              chi_tol=chi_tol if correlations or out else None, out=out, verbose=verbose, schedule=schedule)
         if out:
             out.finish()
     finally:
@@ -369,15 +374,25 @@ def launch(f: str, name: str, size: int, model: str, symmetry: str, J, *, A_rep:
 
 
 def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, Lf, dLi, bmin, bmax, min_eval,
-          max_eval, sigma_tol, gamma_tol, ode_tol, p, cps, measure, chi_tol=None, out=None, verbose=False):
-    """Bogacki-Shampine loop of launch_1l!/2l!/ml! (launcher_1l.jl:56-198) with device stages."""
+          max_eval, sigma_tol, gamma_tol, ode_tol, p, cps, measure, chi_tol=None, out=None, verbose=False,
+          schedule=None):
+    """Bogacki-Shampine loop of launch_1l!/2l!/ml! (launcher_1l.jl:56-198) with device stages.
+
+    ``schedule`` (the ``steps`` of another run: (Λ, dΛ) of each accepted step) replays that run's
+    step sequence: every step takes the scheduled dΛ and is accepted, and the flow ends after the
+    last one; the measurements are those of this run's arithmetic on the other run's cutoffs."""
     p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds = p
     Lam, dLam = Li, dLi
+    step_i = 0
     cps = sorted(set(list(cps) + [Li, Lf]), reverse=True)
     for c in cps:
         if c < Lam:
             dLam = min(dLam, 0.85 * (Lam - c))
             break
+    if schedule is not None:
+        if not schedule:
+            return
+        dLam = schedule[0][1]
     ctx.upload(_capi.SLOT_A, a)
     a_next = A.Action.empty_like(a)
     a_new = A.Action.empty_like(a)
@@ -433,9 +448,17 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
             lam_cp = lower[0] if lower else 0.0
             return min(dl, Lam - lam_cp)
 
-        if err <= 1.0 or dLam <= bmin:
+        if err <= 1.0 or dLam <= bmin or schedule is not None:
+            res.steps.append((Lam, dLam))
             Lam -= dLam
             dLam = next_dlam(dLam)
+            if schedule is not None:
+                # replay: the next step of the given sequence, whatever the error ratio says
+                step_i += 1
+                if step_i >= len(schedule):
+                    Lf = Lam
+                else:
+                    dLam = schedule[step_i][1]
             res.Lam.append(Lam)
             res.dLam.append(dLam)
             res.err.append(err)
@@ -487,7 +510,7 @@ def _flow(ctx: FlowContext, r, m, a, res: FlowResult, *, loops, sigma_corr, Li, 
 
 
 def launch_parquet(ctx: FlowContext, r, m, a: A.Action, Lam: float, max_iter: int, min_eval: int, max_eval: int,
-                   sigma_tol, gamma_tol, parquet_tol, beta=None, verbose: bool = False) -> int:
+                   sigma_tol, gamma_tol, parquet_tol, beta=None, verbose: bool = False, residuals=None) -> int:
     """Parquet fixed point of the SDE and the BSEs at cutoff Λ (parquet.jl:1-100); returns iterations.
 
     The iteration runs on the device (``pffrg_parquet``): ``a`` is uploaded once, the SDE / BSE
@@ -496,8 +519,11 @@ def launch_parquet(ctx: FlowContext, r, m, a: A.Action, Lam: float, max_iter: in
     beta = min(Lam, 1.0) if beta is None else beta
     eval_ = get_eval(Lam, min_eval, max_eval)
     ctx.upload(_capi.SLOT_A, a)
-    it, abs_err, rel_err = ctx.parquet(Lam, eval_, gamma_tol, sigma_tol, parquet_tol, beta, max_iter)
+    it, abs_err, rel_err, hist = ctx.parquet(Lam, eval_, gamma_tol, sigma_tol, parquet_tol, beta, max_iter,
+                                             history=True)
     ctx.download(_capi.SLOT_A, a)
+    if residuals is not None:
+        residuals.extend(float(x) for x in hist)
     if verbose:
         print(f"parquet: {it} iterations, residual {abs_err:.3e} (relative {rel_err:.3e})", flush=True)
     return it

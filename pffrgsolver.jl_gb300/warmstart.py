@@ -174,7 +174,16 @@ class ParquetWarmStart:
         self.net.set_decoder(self.basis * self.z_scale[:, None], self.mean)
         return loss
 
-    def predict(self, feature) -> np.ndarray:
+    def predict(self, feature, part: str = "full") -> np.ndarray:
+        """The predicted vertex; ``part`` selects what predicts it, for ablations: "full" (the
+        least-squares part plus the network), "lsq" (the least-squares part alone) or "mean" (the
+        mean of the training vertices)."""
         x = (np.asarray(feature, dtype=np.float64) - self.x_mean) / self.x_std
+        if part == "mean":
+            return self.mean.copy()
         z_lin = (_poly2(x) @ self.lin)[0]
+        if part == "lsq":
+            return self.mean + z_lin @ self.basis
+        if part != "full":
+            raise ValueError(f"unknown part {part!r}")
         return self.net.predict(x).astype(np.float64) + z_lin @ self.basis

@@ -107,8 +107,13 @@ def test_noalloc_rejects_problems_beyond_the_array(pkg):
 
 
 def test_noalloc_reports_gauss_kronrod_overflow(pkg):
-    """With zero tolerances the boundary integrals bisect until the array's 2048 segments per
-    integral run out: the call returns PFFRG_E_LIMIT before any pass runs."""
+    """With negative tolerances no error estimate meets them (zero ones can: |K15 - G7| reaches 0 on
+    nearly linear segments), so the boundary integrals bisect until the array's 2048 segments per
+    integral run out: the call returns PFFRG_E_LIMIT before any pass runs.  The meshes are squeezed
+    so that Ω[end] + ν[end] = 3 Λ: on the regular meshes the Katanin propagator vanishes at the
+    integration bound and the boundary integrals are skipped (bubbles.jl:121-153)."""
+    import dataclasses
+
     import torch
 
     import pffrg_gb300.workloads as wl
@@ -116,8 +121,12 @@ def test_noalloc_reports_gauss_kronrod_overflow(pkg):
     lib = _lib()
     w = wl.Workload("noalloc", "square", 3, "heisenberg", [[1.0]], 1, 1.0, 11, 4, 3, 0.1, 3)
     lat, r, m, a = wl.build_state(w)
+    f = 3.0 / (m.omega_s[-1] + m.nu_s[-1])
+    m = dataclasses.replace(m, sigma=m.sigma * f, omega_s=m.omega_s * f, nu_s=m.nu_s * f, omega_t=m.omega_t * f,
+                            nu_t=m.nu_t * f)
     a_dev = torch.from_numpy(a.buf.copy()).cuda()
     da_dev = torch.zeros_like(a_dev)
-    rc = _call(lib, r, m, a, a_dev, da_dev, 1.0, 4, (0.0, 0.0))
+    rc = _call(lib, r, m, a, a_dev, da_dev, 1.0, 4, (-1.0, -1.0))
     msg = lib.pffrg_noalloc_last_error().decode()
     assert rc == LIMIT and "Gauss-Kronrod" in msg, (rc, msg)
+    assert float(da_dev.abs().max()) == 0.0  # no pass ran
