@@ -391,13 +391,20 @@ FLOWS = {
     "pyrochlore-L6-2l": dict(name="pyrochlore", size=6, model="heisenberg", symmetry="su2", J=[[1.0]],
                              num_sigma=50, num_omega=15, num_nu=10, num_chi=10, initial=50.0, ode_tol=(1e-3, 1e-3),
                              parquet=False, loops=2),
+    # the largest configuration: kagome L = 8 XXZ + DM (J⊥ = 1, Jz = 0.8, Dz = 0.2), U(1)-DM, 3 loops,
+    # 60/20/15 frequencies
+    "kagome-L8-3l-u1dm": dict(name="kagome", size=8, model="kagome-xxz-dm", symmetry="u1-dm",
+                              J=[[1.0, 0.8, 0.2]], num_sigma=60, num_omega=20, num_nu=15, num_chi=10, initial=50.0,
+                              ode_tol=(1e-3, 1e-3), parquet=False, loops=3),
 }
-FLOW_CPS = [10.0, 5.0, 2.0, 1.0, 0.5, 0.2, 0.1, 0.05, 0.02]
+FLOW_CPS = [20.0, 10.0, 5.0, 2.0, 1.0, 0.5, 0.2, 0.1, 0.05, 0.02]
 
 
 def _chi0(res):
-    """χ(ω = 0) of every site at every measured cutoff of a run (the χ meshes adapt, ω = 0 stays)."""
-    return {round(L, 12): c[:, 0] for (L, mesh, c) in res.chi}
+    """χ(ω = 0) of every site at every measured cutoff of a run (the χ meshes adapt, ω = 0 stays);
+    U(1)-DM runs stack χxx, χzz, χxy."""
+    return {round(L, 12): (np.concatenate([x[:, 0] for x in c]) if isinstance(c, list) else c[:, 0])
+            for (L, mesh, c) in res.chi}
 
 
 def _chi_err(cm, cf, keys):
@@ -430,8 +437,9 @@ def flow_leg(args, dev_index):
         res = launch("", name, size, model, sym, J, final=args.flow_final, cps=FLOW_CPS, precision="mixed",
                      device=dev_index, schedule=runs["fp64"][1].steps, **kw)
         runs["mixed_replay"] = (time.perf_counter() - t0, res)
-    out = {"workload": "%s L=%d Heisenberg, %d loop, %d/%d/%d, Λ 50 -> %g, ODE tol 1e-3, bare start"
-                       % (name, size, kw["loops"], kw["num_sigma"], kw["num_omega"], kw["num_nu"], args.flow_final)}
+    out = {"workload": "%s L=%d %s %s, %d loop, %d/%d/%d, Λ 50 -> %g, ODE tol 1e-3, bare start"
+                       % (name, size, model, sym, kw["loops"], kw["num_sigma"], kw["num_omega"], kw["num_nu"],
+                          args.flow_final)}
     for prec, (secs, res) in runs.items():
         out[prec] = {"seconds": secs, "accepted_steps": len(res.Lam), "rejected_steps": res.rejected,
                      "final_lambda": res.Lam[-1] if res.Lam else None, "reason": res.reason or "final cutoff",

@@ -199,9 +199,11 @@ int pffrg_autotune_team_shape(pffrg_ctx* ctx, int loops, double Lam, int a_slot,
                               int* lanes, int* sites_per_lane);
 
 /* Capacities of the context's scratch: chunks of one quadrature level's
- * queue (0: 8 nsub + 65536 for nsub Simpson subdomains) and the first segment
+ * queue (0: 8 nsub + 65536 for nsub Simpson subdomains, which a call that
+ * overflows it repeats with 4x, up to 128 nsub + 65536) and the first segment
  * capacity of each adaptive Gauss-Kronrod integral (0: 2048; otherwise at
- * least 16).  A level that needs more chunks returns PFFRG_E_LIMIT; integrals
+ * least 16).  A level that needs more chunks than a set queue returns
+ * PFFRG_E_LIMIT; integrals
  * that run out of segments are repeated with 8x the segments, up to the
  * reference's 10^7 evaluations, as always.  For tests of those paths and for
  * callers that bound the context's memory.  No counterpart in the reference. */

@@ -67,7 +67,9 @@ struct pffrg_ctx {
     long long gk_cap = 0, gk_slots = 0;
     int gk_overflow = 0;
     int async_waves = 1;  // device-driven quadrature levels (no host round trip per level)
-    long long queue_cap_req = 0;  // chunk-queue capacity of the passes (0: 8 nsub + 65536)
+    long long queue_cap_req = 0;  // chunk-queue capacity of the passes (0: queue_factor nsub + 65536)
+    long long queue_factor = 8;   // chunks per subdomain of the default queue, grown after an overflow
+    int queue_grow = 0;           // the last call's queue overflowed (the call is repeated with a bigger one)
     int rows_mode = 0;            // overlap rows: 0 staged by size, 1 read through L1/L2, 2 staged when they fit
     int team_T = 0, team_SPL = 0;  // requested team shape of the passes (0: chosen by Ns)
     int64_t chi_evals = 0, chi_regions_max = 0, chi_rounds = 0, chi_rounds_max = 0;
@@ -120,6 +122,7 @@ struct pffrg_ctx {
         if (e_ != cudaSuccess) {                                                                          \
             if (ctx->queue_overflow) {                                                                    \
                 ctx->queue_overflow = 0;                                                                  \
+                ctx->queue_grow = 1;                                                                      \
                 return ctx->fail(PFFRG_E_LIMIT, "quadrature chunk queue capacity exceeded");              \
             }                                                                                             \
             return ctx->fail(PFFRG_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
@@ -263,7 +266,7 @@ int copy_view(pffrg_ctx* ctx, double* dev, const pffrg_action_view* v, bool to_d
 
 // make sure the wave workspace holds a pass of ntasks x nchan tasks at this eval
 cudaError_t ensure_wave_space(pffrg_ctx* ctx, long long nsub) {
-    const long long qcap = ctx->queue_cap_req > 0 ? ctx->queue_cap_req : 8 * nsub + 65536;
+    const long long qcap = ctx->queue_cap_req > 0 ? ctx->queue_cap_req : ctx->queue_factor * nsub + 65536;
     if (nsub <= ctx->wave_nsub && ctx->wave_mem && (ctx->queue_cap_req <= 0 || qcap == ctx->wave_qcap))
         return cudaSuccess;
     if (ctx->wave_mem) {
@@ -469,6 +472,16 @@ bool grow_gk(pffrg_ctx* ctx) {
     return true;
 }
 
+// after a chunk-queue overflow of the default-sized queue: 4x the chunks per subdomain (up to 128;
+// a queue size the caller set with pffrg_set_capacities is kept)
+bool grow_queue(pffrg_ctx* ctx) {
+    if (!ctx->queue_grow || ctx->queue_cap_req > 0 || ctx->queue_factor >= 128) return false;
+    ctx->queue_grow = 0;
+    ctx->queue_factor *= 4;
+    ctx->wave_nsub = 0;  // the next pass allocates the bigger queue
+    return true;
+}
+
 template <typename R>
 int corrs_run(pffrg_ctx* ctx, int kind, double Lam, const R* a, const R* da, double atol, double rtol,
               double* out) {
@@ -540,7 +553,10 @@ int check_status(pffrg_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->st));
     if (h) {
         CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
-        if (h & 8) return ctx->fail(PFFRG_E_LIMIT, "quadrature chunk queue capacity exceeded");
+        if (h & 8) {
+            ctx->queue_grow = 1;
+            return ctx->fail(PFFRG_E_LIMIT, "quadrature chunk queue capacity exceeded");
+        }
         if (h & ~16) {
             ctx->gk_overflow = 1;
             return ctx->fail(PFFRG_E_LIMIT, "adaptive Gauss-Kronrod segment capacity (%lld) exceeded", ctx->gk_cap);
@@ -826,12 +842,13 @@ int absmax(pffrg_ctx* ctx, const double* a, double* dst) {
 
 }  // namespace
 
-// rerun a call whose Gauss-Kronrod integrals ran out of segments with 8x the capacity
+// rerun a call whose Gauss-Kronrod integrals ran out of segments with 8x the capacity, or whose
+// quadrature levels overflowed the default chunk queue with a 4x bigger queue
 template <class Fn>
 int gk_retry(pffrg_ctx* ctx, Fn fn) {
     for (;;) {
         const int rc = fn();
-        if (rc != PFFRG_E_LIMIT || !ctx || !grow_gk(ctx)) return rc;
+        if (rc != PFFRG_E_LIMIT || !ctx || !(grow_gk(ctx) || grow_queue(ctx))) return rc;
     }
 }
 
@@ -960,7 +977,7 @@ pffrg_ctx* pffrg_create(const pffrg_lattice_view* lat, const pffrg_mesh_view* me
               dalloc((void**)&ctx->lat.ov_off, sizeof(int) * (Ns + 1)) &&
               dalloc((void**)&ctx->lat.ov_rows, sizeof(unsigned) * rows.size()) &&
               dalloc((void**)&ctx->mesh, 2 * sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
-              dalloc((void**)&ctx->mesh_ff, 3 * sizeof(float) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
+              dalloc((void**)&ctx->mesh_ff, sizeof(float) * (3 * (L.Nsig + 2 * L.NO + 2 * L.Nn) + kMeshGuess)) &&
               dalloc((void**)&ctx->mesh_new, sizeof(double) * (L.Nsig + 2 * L.NO + 2 * L.Nn)) &&
               dalloc((void**)&ctx->scan_arg, sizeof(long long) * 3 * L.C) &&
               dalloc((void**)&ctx->scan_cuts, sizeof(double) * 3 * L.C * (L.NO + 3 * L.Nn));
@@ -1240,13 +1257,13 @@ int bse_dev(pffrg_ctx* ctx, double Lam, double* d1, double* d2, int eval, double
 }
 
 // One SDE or BSE evaluation of the device parquet loop, repeated with more Gauss-Kronrod segments
-// when an integral ran out of them (the inputs are unchanged by a failed evaluation)
+// or a bigger chunk queue when it ran out of them (the inputs are unchanged by a failed evaluation)
 template <class Fn>
 int parquet_eval(pffrg_ctx* ctx, Fn fn) {
     for (;;) {
         int rc = fn();
         if (!rc) rc = check_status(ctx);
-        if (rc != PFFRG_E_LIMIT || !grow_gk(ctx)) return rc;
+        if (rc != PFFRG_E_LIMIT || !(grow_gk(ctx) || grow_queue(ctx))) return rc;
     }
 }
 

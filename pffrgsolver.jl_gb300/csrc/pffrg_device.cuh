@@ -434,11 +434,18 @@ __device__ __forceinline__ bool operator<(FF a, FF b) { return a.h < b.h || (a.h
 __device__ __forceinline__ bool operator<(FF a, float b) { return a.h < b || (a.h == b && a.l < 0.f); }
 __device__ __forceinline__ FF ff_abs(FF a) { return a < 0.f ? -a : a; }
 
-// Mesh block of the mixed path (floats): [h | l | inverse spacing], each [σ | Ωs | νs | Ωt | νt]
+// Per mesh of the float block, four floats that place a frequency near its interval for the lin-log
+// meshes of get_mesh (mesh.jl:86-121): 1 / spacing of the linear part, its last index, its last
+// point and 1 / log(ratio) of the logarithmic part (all 0 when the mesh has no such form)
+constexpr int kMeshGuess = 20;
+
+// Mesh block of the mixed path (floats): [h | l | inverse spacing], each [σ | Ωs | νs | Ωt | νt],
+// then the kMeshGuess placement parameters
 struct MeshFF {
     const float* h;
     const float* l;
     const float* inv;
+    const float* g;
     int Nsig, NO, Nn;
     __device__ __forceinline__ int sig() const { return 0; }
     __device__ __forceinline__ int Os() const { return Nsig; }
@@ -450,7 +457,7 @@ struct MeshFF {
 
 __device__ __forceinline__ MeshFF mesh_view_ff(const float* block, int Nsig, int NO, int Nn) {
     const int n = Nsig + 2 * NO + 2 * Nn;
-    return MeshFF{block, block + n, block + 2 * n, Nsig, NO, Nn};
+    return MeshFF{block, block + n, block + 2 * n, block + 3 * n, Nsig, NO, Nn};
 }
 
 // get_indices + get_param (param.jl:26-87) on the mesh at offset o of length n, as get_param
@@ -462,15 +469,17 @@ __device__ __forceinline__ Param<float> get_param_ff(FF val, const MeshFF& M, in
         p.wu = 0.f;
         return p;
     }
-    int lo = 0, hi = n - 1;
-    if (!(val.h == val.h)) hi = 0;
-    // first k with h[k] >= val.h, then past an equal high part whose pair is still below val
-    // (mesh points lie more than an FP32 ulp apart)
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (M.h[o + mid] >= val.h) hi = mid;
-        else lo = mid + 1;
-    }
+    // first k with h[k] >= val.h (val < x[n-1] here, so one exists): a guess from the lin-log form of
+    // the mesh, then steps to the exact index, which any increasing mesh reaches
+    const int gi = o == 0 ? 0 : (o == M.Os() ? 1 : (o == M.ns() ? 2 : (o == M.Ot() ? 3 : 4)));
+    const float* g = M.g + 4 * gi;
+    const float v = val.h;
+    const float kf = v <= g[2] ? ceilf(v * g[0]) : g[1] + ceilf(__logf(v / g[2]) * g[3]);
+    int lo = (kf >= 0.f && kf <= (float)(n - 1)) ? (int)kf : (kf > 0.f ? n - 1 : 0);
+    while (lo > 0 && M.h[o + lo - 1] >= v) --lo;
+    while (lo < n - 1 && M.h[o + lo] < v) ++lo;
+    // then past an equal high part whose pair is still below val (mesh points lie more than an
+    // FP32 ulp apart)
     if (lo < n - 1 && M.h[o + lo] == val.h && M.l[o + lo] < val.l) ++lo;
     p.hi = lo;
     p.lo = (val < M.at(o, lo)) ? lo - 1 : lo;

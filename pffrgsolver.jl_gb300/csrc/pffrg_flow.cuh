@@ -741,7 +741,10 @@ struct Team {
 // wave workspace (device scratch of a pass; one block carved into arrays)
 // ---------------------------------------------------------------------------
 constexpr int kChunk = 32;      // nodes per chunk
-constexpr int kMaxChunks = 64;  // chunks per subdomain and level (bigger levels use bigger chunks)
+// chunks per subdomain and level (bigger levels use bigger chunks): the deepest subdomains set the
+// length of a pass, so their levels are spread over up to 256 teams (measured on the pyrochlore
+// L = 6 two-loop state: 7 % faster than 64 chunks; 1024 gave the same as 256)
+constexpr int kMaxChunks = 256;
 
 // Queue the next level (n new nodes) of subdomain sub into wave parity `par`.
 __device__ __forceinline__ void enqueue(WaveSpace& Wsp, int par, int sub, long long n) {
@@ -808,9 +811,10 @@ struct SmemLayout {
                       : (size_t)2 * C * Ns;
     }
     // the meshes of the node setup: float-float pairs and inverse spacings (mixed path) or FP64
-    // values and inverse spacings, nm = Nsig + 2 NO + 2 Nn entries each
+    // values and inverse spacings, nm = Nsig + 2 NO + 2 Nn entries each (the float block ends with the
+    // placement parameters of its meshes)
     __host__ __device__ static size_t mesh_bytes(int nm) {
-        return sizeof(R) == 4 ? 3 * sizeof(float) * (size_t)nm : 2 * sizeof(double) * (size_t)nm;
+        return sizeof(R) == 4 ? sizeof(float) * (3 * (size_t)nm + kMeshGuess) : 2 * sizeof(double) * (size_t)nm;
     }
     size_t mesh, teams, tmp, rows, total;
     __host__ __device__ SmemLayout(int Ns, int nm, long long R_rows, bool rows_in_smem) {
@@ -854,7 +858,7 @@ __device__ __forceinline__ void load_common(const PassArgs<R>& A, unsigned char*
     const int nm = A.L.Nsig + 2 * A.L.NO + 2 * A.L.Nn;
     if constexpr (sizeof(R) == 4) {
         float* m = reinterpret_cast<float*>(smem);
-        for (int k = threadIdx.x; k < 3 * nm; k += blockDim.x) m[k] = ldg(A.mesh_ff + k);
+        for (int k = threadIdx.x; k < 3 * nm + kMeshGuess; k += blockDim.x) m[k] = ldg(A.mesh_ff + k);
     } else {
         double* m = reinterpret_cast<double*>(smem);
         for (int k = threadIdx.x; k < 2 * nm; k += blockDim.x) m[k] = ldg(A.mesh + k);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
 #include <vector>
 
 #include "pffrg_device.cuh"
@@ -92,11 +93,13 @@ struct WaveSpace {
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // float-float form of a mesh block [σ | Ωs | νs | Ωt | νt] (without inverses): the high floats,
-// the low floats (x - h) and the FP32 inverse spacings
+// the low floats (x - h) and the FP32 inverse spacings, then per mesh the placement parameters of
+// MeshFF::g (the lin-log form of get_mesh read off the mesh itself; any increasing mesh is
+// searched correctly, a mesh of that form in a step or two)
 inline std::vector<float> mesh_block_ff(const std::vector<double>& x, int Nsig, int NO, int Nn) {
     const int len[5] = {Nsig, NO, Nn, NO, Nn};
     const size_t n = (size_t)Nsig + 2 * NO + 2 * Nn;
-    std::vector<float> f(3 * n);
+    std::vector<float> f(3 * n + kMeshGuess, 0.f);
     size_t o = 0;
     for (int a = 0; a < 5; ++a) {
         for (int k = 0; k < len[a]; ++k) {
@@ -105,6 +108,18 @@ inline std::vector<float> mesh_block_ff(const std::vector<double>& x, int Nsig, 
             f[o + k] = h;
             f[n + o + k] = (float)(v - (double)h);
             f[2 * n + o + k] = k + 1 < len[a] ? (float)(1.0 / (x[o + k + 1] - v)) : 0.f;
+        }
+        const double* m = x.data() + o;
+        const int N = len[a];
+        const double step = m[1] - m[0];
+        if (m[0] == 0.0 && step > 0.0) {
+            int nlin = 1;
+            while (nlin + 1 < N && std::fabs(m[nlin + 1] - (nlin + 1) * step) <= 1e-6 * m[nlin + 1]) ++nlin;
+            float* g = f.data() + 3 * n + 4 * a;
+            g[0] = (float)(1.0 / step);
+            g[1] = (float)nlin;
+            g[2] = (float)m[nlin];
+            if (nlin < N - 1 && m[N - 1] > m[nlin]) g[3] = (float)((N - 1 - nlin) / std::log(m[N - 1] / m[nlin]));
         }
         o += len[a];
     }

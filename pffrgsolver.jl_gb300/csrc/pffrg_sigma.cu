@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, cons
         load_mesh(*reinterpret_cast<SMesh<double>*>(smem_raw), A.mesh, A.L.Nsig, A.L.NO, A.L.Nn);
     } else {
         float* mf = reinterpret_cast<float*>(smem_raw);
-        for (int q = threadIdx.x; q < 3 * nm; q += blockDim.x) mf[q] = ldg(A.mesh_ff + q);
+        for (int q = threadIdx.x; q < 3 * nm + kMeshGuess; q += blockDim.x) mf[q] = ldg(A.mesh_ff + q);
     }
     const int tid = threadIdx.x;
     const long long slot = blockIdx.x / CL;
