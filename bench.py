@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     p.add_argument("--no-flow", action="store_true", help="skip the full-flow leg")
+    p.add_argument("--team-shape", default="", help="lanes x sites per lane of the passes (empty: autotuned)")
     p.add_argument("--flow-final", type=float, default=0.01, help="final cutoff of the full-flow leg")
     p.add_argument("--flow-precisions", default="fp64,mixed", help="precisions of the full-flow leg")
     p.add_argument("--flow", default="square-L3-1l", choices=sorted(FLOWS), help="workload of the full-flow leg")
@@ -146,9 +147,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch():
-    """DRAM bytes and duration of one captured wave-kernel launch from the committed ncu summary
-    (profiles/eval_kernel_traffic.txt), or None."""
+def ncu_profile_summary():
+    """Figures of the committed ncu summary of the dominant kernel (profiles/eval_kernel_traffic.txt): the
+    workload and precision it was captured on, DRAM bytes of all wave-kernel launches of one right-hand
+    side, and the issue, occupancy and cache figures of one captured eval_kernel launch; or None."""
     p = ROOT / "profiles" / "eval_kernel_traffic.txt"
     if not p.exists():
         return None
@@ -156,12 +158,12 @@ def ncu_traffic_per_launch():
     for line in p.read_text().splitlines():
         if line.strip() and not line.startswith("#"):
             k, _, v = line.partition(" ")
-            out[k] = v.strip()
-    try:
-        return {"workload": out["workload"], "precision": out["precision"], "dram_bytes": float(out["dram_bytes"]),
-                "launch_ms": float(out["launch_ms"])}
-    except (KeyError, ValueError):
-        return None
+            v = v.strip()
+            try:
+                out[k] = float(v)
+            except ValueError:
+                out[k] = v
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -272,7 +274,12 @@ def ours(args):
     ctx = FlowContext(r, m, precision="mixed", device=local)
     ctx.upload(C.SLOT_A, a)
     # the team shape of the quadrature passes, picked by timing one right-hand side per candidate
-    team = ctx.autotune_team_shape(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
+    # (or given, for profiling runs that must launch the same kernels every time)
+    if args.team_shape:
+        team = tuple(int(x) for x in args.team_shape.split("x"))
+        ctx.set_team_shape(*team)
+    else:
+        team = ctx.autotune_team_shape(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
 
     def rhs():
         ctx.rhs(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
@@ -322,10 +329,12 @@ def ours(args):
     achieved = alg_bytes_step / (pass_ms_step * 1e-3) / 1e9 if pass_ms_step > 0 else None
     # DRAM bytes per pass launch: the captured wave launch's DRAM rate times the pass time (the
     # traffic of a pass is taken proportional to its kernel time; the capture is one level)
-    traffic = None
-    tr = ncu_traffic_per_launch()
-    if tr and tr.get("workload") == w.name and tr.get("precision") == "mixed" and pass_launches_step:
-        traffic = tr["dram_bytes"] / tr["launch_ms"] * (pass_ms_step / pass_launches_step)
+    # DRAM bytes per pass launch: the wave kernels of one right-hand side captured with ncu, divided by
+    # the right-hand side's passes; issue and cache figures from one captured eval_kernel launch
+    prof = ncu_profile_summary()
+    if not (prof and prof.get("workload") == w.name and prof.get("precision") == "mixed"):
+        prof = {}
+    traffic = (prof["dram_bytes_per_rhs"] / prof["passes_per_rhs"]) if "dram_bytes_per_rhs" in prof else None
 
     if rank != 0:
         if dist:
@@ -360,8 +369,15 @@ def ours(args):
                      "launches_per_step": pass_launches_step,
                      "algorithmic_bytes_per_launch": (alg_bytes_step / pass_launches_step)
                      if pass_launches_step else None,
-                     "traffic_note": "DRAM bytes per pass launch, scaled from one captured level launch by kernel "
-                                     "time (profiles/eval_kernel_traffic.txt)"},
+                     "traffic_note": "DRAM bytes per pass launch: all wave-kernel launches of one right-hand side "
+                                     "under ncu / passes per right-hand side (profiles/eval_kernel_traffic.txt)",
+                     "limiter": prof.get("limiter"),
+                     "issue_active_frac": prof["issue_active_pct"] / 100 if "issue_active_pct" in prof else None,
+                     "warps_active_per_sm": prof.get("warps_active_per_sm"),
+                     "l1_hit_frac": prof["l1_hit_pct"] / 100 if "l1_hit_pct" in prof else None,
+                     "l1_throughput_frac": prof["l1_throughput_pct"] / 100 if "l1_throughput_pct" in prof else None,
+                     "l2_throughput_frac": prof["l2_throughput_pct"] / 100 if "l2_throughput_pct" in prof else None,
+                     "profile_team_shape": prof.get("team_shape")},
         "cpu_baseline": cpu,
         "fp64": {"value": 1e3 / fp64_ms, "unit": UNIT, "ms_per_step": fp64_ms,
                  "mixed_speedup": fp64_ms / ms_step,

@@ -56,11 +56,14 @@ struct NodeScratch {
     Plan<R> plan[4][3];
 };
 
-// nodes per team batch: 8 per warp in total for SU(2), 4 for U(1)-DM; fewer when each lane holds
-// many sites (the SU(2) t-channel staging grows with sites x nodes)
+// nodes per team batch: 4 per warp in total, 2 for SU(2) when each lane holds more than four sites
+// (the SU(2) t-channel staging grows with sites x nodes).  The node scratch and t-channel staging
+// of a batch set the shared memory of a block, which limits the blocks per SM: on the pyrochlore
+// L = 6 two-loop state 32x2 teams with 4 nodes ran 403 ms against 470 ms with 8 nodes (two blocks
+// per SM instead of three), and 16x3 teams were slower with 1 node than with 2.
 template <int T, int C, int SPL>
 struct BatchOf {
-    static constexpr int NB = (C == 2 ? (SPL <= 2 ? 8 : (SPL <= 4 ? 4 : 2)) : 4) * T / 32;
+    static constexpr int NB = (C == 2 ? (SPL <= 4 ? 4 : 2) : 4) * T / 32;
 };
 
 // SU(2) t-channel staging: per site the NB (spin, density) pairs of a batch, padded by 16 bytes so
@@ -1435,14 +1438,14 @@ cudaError_t run_shape(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cud
 // the team shapes built: lanes per node batch x sites per lane
 #define PFFRG_TEAM_SHAPES(X) X(8, 1) X(16, 1) X(32, 1) X(16, 3) X(16, 4) X(32, 2) X(32, 4) X(32, 8)
 
-// the default shape for Ns sites: the narrowest team (more teams per warp, smaller node
-// batches and staging) whose lanes hold at most four sites each
+// the default shape for Ns sites: the narrowest team whose lanes hold at most two sites (up to 64
+// sites; measured on the pyrochlore L = 6 two-loop state, 48 sites: 32x2 403 ms, 16x3 460 ms,
+// 16x4 511 ms), beyond that at most four or eight
 __host__ __device__ inline void default_team_shape(int Ns, int& T, int& SPL) {
     if (Ns <= 8) T = 8, SPL = 1;
     else if (Ns <= 16) T = 16, SPL = 1;
     else if (Ns <= 32) T = 32, SPL = 1;
-    else if (Ns <= 48) T = 16, SPL = 3;
-    else if (Ns <= 64) T = 16, SPL = 4;
+    else if (Ns <= 64) T = 32, SPL = 2;
     else if (Ns <= 128) T = 32, SPL = 4;
     else T = 32, SPL = 8;
 }

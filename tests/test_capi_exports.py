@@ -65,7 +65,8 @@ def test_no_device_means_no_context(lib):
 
 
 def test_committed_ncu_traffic_summary_parses():
-    """bench.py's roofline traffic comes from the committed ncu summary of the benchmark state."""
+    """bench.py's roofline traffic and limiter figures come from the committed ncu summary of the
+    benchmark state."""
     import importlib.util
     from pathlib import Path
 
@@ -73,9 +74,11 @@ def test_committed_ncu_traffic_summary_parses():
     spec = importlib.util.spec_from_file_location("bench_mod", root / "bench.py")
     bench = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(bench)
-    tr = bench.ncu_traffic_per_launch()
-    assert tr is not None and tr["workload"] == bench.WORKLOAD and tr["precision"] == "mixed"
-    assert tr["dram_bytes"] > 0 and tr["launch_ms"] > 0
+    prof = bench.ncu_profile_summary()
+    assert prof is not None and prof["workload"] == bench.WORKLOAD and prof["precision"] == "mixed"
+    assert prof["dram_bytes_per_rhs"] > 0 and prof["passes_per_rhs"] == 2
+    assert 0 < prof["issue_active_pct"] <= 100 and 0 < prof["warps_active_per_sm"] <= 64
+    assert isinstance(prof["limiter"], str) and prof["limiter"]
 
 
 def test_setters_refuse_a_null_context():
