@@ -10,17 +10,23 @@ frequencies, Λ = 1, vertex entries N(0, 0.05) plus the bare coupling on the
 evaluations per second of the mixed-precision GPU path; the FP64 GPU path,
 the mixed path's error against it and the CPU oracle are reported beside it.
 
-The full-flow leg (``full_flow``) runs the square L = 3 one-loop flow
-(Λ 50 → 0.01, χ measured after every accepted step) in mixed precision and
-in FP64 and reports both wall times and χ(ω = 0) of the two at the shared
-checkpoints.  Optional legs: ``--sweep N`` (N square J1-J2 flows
-sharing the GPU) and ``--warm-start TRAIN,TEST`` (honeycomb J1-J2-J3: parquet
-iterations from the learned start against the bare start).  Before the
-warm-up the team shape of the passes is picked by the autotuner.
+The full-flow leg (``full_flow``) runs the flow of the same lattice and
+model, pyrochlore L = 6 two-loop (Λ 50 → 0.01 or the breakdown, χ measured
+after every accepted step), in FP64 and in mixed precision, and the mixed
+right-hand side once more on the FP64 flow's accepted step sequence; it
+reports the wall times and χ(ω = 0) of the mixed flows against the FP64 one
+(``--flow`` selects the square L = 3 one-loop or the kagome L = 8 U(1)-DM
+three-loop flow instead).  The warm-start leg (``--warm-start TRAIN,TEST``,
+honeycomb J1-J2-J3) counts parquet iterations from the bare couplings, the
+mean training vertex, the least-squares part alone and the least-squares
+part with the network.  ``--sweep N`` runs N square J1-J2 flows sharing the
+GPU.  Before the warm-up the team shape of the passes is picked by the
+autotuner.
 
 ``--impl reference`` times the CPU restatement of the reference's algorithm
 (the reference is Julia, which is not installed on these machines) on all
-host cores, on a bounded sample of the same workload.
+host cores: full right-hand sides of the same workload, as many as fit its
+time budget.
 """
 from __future__ import annotations
 
@@ -64,11 +70,11 @@ def parse():
     p.add_argument("--team-shape", default="", help="lanes x sites per lane of the passes (empty: autotuned)")
     p.add_argument("--flow-final", type=float, default=0.01, help="final cutoff of the full-flow leg")
     p.add_argument("--flow-precisions", default="fp64,mixed", help="precisions of the full-flow leg")
-    p.add_argument("--flow", default="square-L3-1l", choices=sorted(FLOWS), help="workload of the full-flow leg")
+    p.add_argument("--flow", default="pyrochlore-L6-2l", choices=sorted(FLOWS), help="workload of the full-flow leg")
     p.add_argument("--no-replay", action="store_true", help="skip the mixed replay of the FP64 flow's steps")
     p.add_argument("--sweep", type=int, default=0,
                    help="instances of the coupling-sweep leg (square J1-J2, L in 3,4,5,6,8; 0: skip)")
-    p.add_argument("--warm-start", default="",
+    p.add_argument("--warm-start", default="64,16",
                    help="train,test counts of the learned parquet warm-start leg (honeycomb J1-J2-J3; empty: skip)")
     p.add_argument("--warm-lambda", type=float, default=2.0, help="cutoff of the warm-start leg's parquet solves")
     p.add_argument("--warm-meshes", default="25/15/10", help="positive σ/Ω/ν frequencies of the warm-start leg")
