@@ -215,81 +215,61 @@ __device__ __forceinline__ R gather_one(const PassArgs<R>& A, const NodeScratch<
     return val;
 }
 
-// all components of one slot on this lane's sites: v[c][k] = Γ_c(site tl + k T)
+// all components of one slot on this lane's sites, v[c][k] = Γ_c(site tl + k T) (the U(1)-DM passes;
+// SU(2) reads its pair-layout copies in Team::gather_su2): bare + Σ_ch sgn Σ_q w_q q_c'[off_q + site]
+// with the read component c' and sign of apply_flags_u1_dm, channels and corners in the reference's
+// order.  The plan is held in registers per channel and the loop over the lane's sites has no branch
+// (padding sites read site 0 and are zeroed at the end), so a channel's reads can be in flight together.
 template <typename R, int T, int SPL, int C>
 __device__ __forceinline__ void gather_slot(const PassArgs<R>& A, const NodeScratch<R, C>& ns, int slot, int tl,
                                             const int* site_ex, R v[C][SPL]) {
     const R* __restrict__ src = A.src[slot];
     const int Ns = A.L.Ns;
+    int si[SPL];
 #pragma unroll
     for (int k = 0; k < SPL; ++k) {
         const int i = tl + k * T;
-#pragma unroll
-        for (int c = 0; c < C; ++c) v[c][k] = i < Ns ? ldg(src + A.L.bare(c) + i) : (R)0;
+        si[k] = i < Ns ? i : 0;
     }
-    if constexpr (C != 2) {
-        // U(1)-DM: component by component, each with its own read component and sign
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-            const Plan<R>& P = ns.plan[slot][ch];
-            const int kern = P.kernel;
-            if (!kern) continue;
-            const int ex = P.exch;
-            const int nc = corners_of(kern);
+    for (int k = 0; k < SPL; ++k)
 #pragma unroll
-            for (int c = 0; c < C; ++c) {
-                R sgn;
-                const int cs = comp_read(P, C, c, sgn);
-                const R* q = src + A.L.qbase(cs, P.src_ch, kern - 1);
-#pragma unroll
-                for (int k = 0; k < SPL; ++k) {
-                    const int i = tl + k * T;
-                    if (i >= Ns) continue;
-                    const int s = ex ? site_ex[k] : i;
-                    R a = P.w[0] * ldg(q + P.off[0] + s);
-                    for (int qq = 1; qq < nc; ++qq) a += P.w[qq] * ldg(q + P.off[qq] + s);
-                    v[c][k] += sgn * a;
-                }
-            }
-        }
-        return;
-    }
+        for (int c = 0; c < C; ++c) v[c][k] = ldg(src + A.L.bare(c) + si[k]);
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
-        const int kern = ns.plan[slot][ch].kernel;
+        const Plan<R>& P = ns.plan[slot][ch];
+        const int kern = P.kernel;
         if (!kern) continue;
-        // the plan in registers once per node, reused for both components and all sites
-        const int src_ch = ns.plan[slot][ch].src_ch;
-        const int ex = ns.plan[slot][ch].exch;
-        const R sgn_d = ns.plan[slot][ch].sgn_d;
         const int nc = corners_of(kern);
+        const int ex = P.exch;
         R w[8];
         int off[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            w[q] = q < nc ? ns.plan[slot][ch].w[q] : (R)0;
-            off[q] = q < nc ? ns.plan[slot][ch].off[q] : 0;
+            w[q] = q < nc ? P.w[q] : (R)0;
+            off[q] = q < nc ? P.off[q] : 0;
         }
-        const R* q0 = src + A.L.qbase(0, src_ch, kern - 1);
-        const R* q1 = src + A.L.qbase(1, src_ch, kern - 1);
 #pragma unroll
-        for (int k = 0; k < SPL; ++k) {
-            const int i = tl + k * T;
-            if (i >= Ns) continue;
-            const int s = ex ? site_ex[k] : i;
-            R a0 = w[0] * ldg(q0 + off[0] + s);
-            R a1 = w[0] * ldg(q1 + off[0] + s);
+        for (int c = 0; c < C; ++c) {
+            R sgn;
+            const int cs = comp_read(P, C, c, sgn);
+            const R* q0 = src + A.L.qbase(cs, P.src_ch, kern - 1);
 #pragma unroll
-            for (int q = 1; q < 8; ++q) {
-                if (q < nc) {
-                    a0 += w[q] * ldg(q0 + off[q] + s);
-                    a1 += w[q] * ldg(q1 + off[q] + s);
-                }
+            for (int k = 0; k < SPL; ++k) {
+                const int st = ex ? site_ex[k] : si[k];
+                R a = (R)0;
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (q < nc) a += w[q] * ldg(q0 + off[q] + st);
+                v[c][k] += sgn * a;
             }
-            v[0][k] += a0;
-            v[1][k] += sgn_d * a1;
         }
     }
+#pragma unroll
+    for (int k = 0; k < SPL; ++k)
+        if (tl + k * T >= Ns)
+#pragma unroll
+            for (int c = 0; c < C; ++c) v[c][k] = (R)0;
 }
 
 template <typename R>

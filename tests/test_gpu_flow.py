@@ -217,3 +217,62 @@ def test_device_resample_matches_host(pkg, symmetry):
             dev = Action.empty_like(a)
             ctx.download(C.SLOT_A, dev)
         assert np.max(np.abs(dev.buf - host.buf)) <= 1e-13 * np.max(np.abs(host.buf))
+
+
+def test_flow_matches_oracle_flow(pkg, O):
+    """The whole flow loop against the oracle: launch! in FP64 on the GPU (device steps, device scans and
+    resampling, χ after every step) and the same loop of launcher_1l.jl:56-198 restated here on the
+    oracle's right-hand side, host scans and resampling (launcher.resample_from_to) and the oracle's χ.
+    Square L = 3, 10/4/3 frequencies, Λ 5 → 0.5: both take the same steps, and χ(ω = 0) agrees at every
+    accepted cutoff within the stated 1e-6 of max|χ|."""
+    from pffrg_gb300 import action as A
+    from pffrg_gb300 import frequency as F
+    from pffrg_gb300 import lattice as L
+    from pffrg_gb300.flow import get_eval
+    from pffrg_gb300.launcher import launch, resample_from_to
+
+    kw = dict(num_sigma=10, num_omega=4, num_nu=3, num_chi=4, initial=5.0, final=0.5, parquet=False,
+              ode_tol=(1e-3, 1e-3))
+    res = launch("", "square", 3, "heisenberg", "su2", [[1.0]], precision="fp64", **kw)
+    # the same loop on the oracle
+    lat = L.get_lattice("square", 3)
+    r = L.get_reduced_lattice("heisenberg", [[1.0]], lat)
+    p = (F.DEFAULT_P_SIGMA, F.DEFAULT_P_OMEGA, F.DEFAULT_P_NU, F.DEFAULT_P_OMEGA, F.DEFAULT_P_NU, F.DEFAULT_P_CHI,
+         F.DEFAULT_LINS, F.DEFAULT_BOUNDS)
+    m = F.initial_mesh(5.0, 10, 4, 3, 4, *p)
+    a = A.get_action_empty("su2", r, m)
+    A.init_action(lat, r, a)
+    Lam, Lf, bmin, bmax = 5.0, 0.5, 1e-4, 0.1
+    dLam = bmax * Lam
+    cps = [5.0, 0.5]
+    lams, chis = [], []
+    chi_prev = np.zeros((r.num_sites, 4))
+    while Lam > Lf:
+        P = O.Problem(r, m)
+        inter, err = oracle_bs_step(O, P, a, Lam, dLam, 1, get_eval(Lam, 10, 100), ode_tol=(1e-3, 1e-3))
+        assert err < 10.0
+
+        def next_dlam(dl, lam):
+            dl = max(bmin, min(bmax * lam, 0.85 * (1.0 / err) ** (1.0 / 3.0) * dl))
+            lower = [c for c in cps if c - lam < 0.0]
+            return min(dl, lam - (lower[0] if lower else 0.0))
+
+        if err <= 1.0 or dLam <= bmin:
+            Lam -= dLam
+            dLam = next_dlam(dLam, Lam)
+            chi = O.chi(P, Lam, inter, m.chi)
+            lams.append(Lam)
+            chis.append(chi[:, 0].copy())
+            assert chi[0, 0] / chi_prev[0, 0] >= 0.995 if chi_prev[0, 0] else True
+            chi_prev = chi
+            a_inter = A.Action.empty_like(a)
+            a_inter.buf[:] = inter
+            a_new = A.Action.empty_like(a)
+            m = resample_from_to(Lam, *p, m, a_inter, a_new, [chi])
+            a = a_new
+        else:
+            dLam = next_dlam(dLam, Lam)
+    assert res.finished and len(res.Lam) == len(lams)
+    assert np.allclose(res.Lam, lams, rtol=1e-12, atol=0.0)
+    for (Lg, mesh, cg), c in zip(res.chi, chis):
+        assert np.max(np.abs(cg[:, 0] - c)) <= 1e-6 * np.max(np.abs(c)), Lg
