@@ -183,7 +183,7 @@ int pffrg_set_async_waves(pffrg_ctx* ctx, int on);
 
 /* Team shape of the quadrature passes: `lanes` threads share a batch of nodes
  * and each holds `sites_per_lane` sites (built: 8x1, 16x1, 16x3, 16x4, 32x1,
- * 32x2, 32x4, 32x8; 0x0 = chosen from the number of sites).  A shape that
+ * 32x2, 32x3, 32x4, 32x8; 0x0 = chosen from the number of sites).  A shape that
  * does not cover the sites is ignored.  Results agree to rounding (the
  * t-channel overlap sums are split over the lanes differently).  No
  * counterpart in the reference. */
@@ -210,7 +210,9 @@ int pffrg_autotune_team_shape(pffrg_ctx* ctx, int loops, double Lam, int a_slot,
 int pffrg_set_capacities(pffrg_ctx* ctx, int64_t queue_chunks, int64_t gk_segments);
 
 /* Overlap rows of the t-channel sums (flow_su2_t.jl:66-75): 0 = staged in
- * shared memory when the block's staging stays within 75 KB (default), 1 =
+ * shared memory when the block's staging still lets the FP32 eval kernel's
+ * blocks fit an SM (55 KB for SU(2) teams of up to two sites per lane, 75 KB
+ * otherwise; default), 1 =
  * read through L1/L2, 2 = staged whenever they fit the 227 KB of a block.
  * Results agree to rounding.  No counterpart in the reference. */
 int pffrg_set_overlap_staging(pffrg_ctx* ctx, int mode);

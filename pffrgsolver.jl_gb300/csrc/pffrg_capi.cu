@@ -1144,7 +1144,7 @@ int pffrg_autotune_team_shape(pffrg_ctx* ctx, int loops, double Lam, int a_slot,
     if (!ctx) return PFFRG_E_ARGS;
     CK(cudaSetDevice(ctx->device));
     const int Ns = ctx->L.Ns;
-    static const int shapes[][2] = {{8, 1}, {16, 1}, {32, 1}, {16, 3}, {16, 4}, {32, 2}, {32, 4}, {32, 8}};
+    static const int shapes[][2] = {{8, 1}, {16, 1}, {32, 1}, {16, 3}, {16, 4}, {32, 2}, {32, 3}, {32, 4}, {32, 8}};
     cudaEvent_t ev[2];
     CK(cudaEventCreate(&ev[0]));
     if (cudaEventCreate(&ev[1]) != cudaSuccess) {
@@ -1528,7 +1528,8 @@ int pffrg_set_chi_integrand(pffrg_ctx* ctx, int precision) {
 
 int pffrg_set_team_shape(pffrg_ctx* ctx, int lanes, int sites_per_lane) {
     if (!ctx) return PFFRG_E_ARGS;
-    static const int shapes[][2] = {{0, 0}, {8, 1}, {16, 1}, {16, 3}, {16, 4}, {32, 1}, {32, 2}, {32, 4}, {32, 8}};
+    static const int shapes[][2] = {{0, 0}, {8, 1}, {16, 1}, {16, 3}, {16, 4}, {32, 1}, {32, 2}, {32, 3}, {32, 4},
+                                    {32, 8}};
     for (const auto& sh : shapes)
         if (sh[0] == lanes && sh[1] == sites_per_lane) {
             ctx->team_T = lanes;

@@ -1120,10 +1120,15 @@ __global__ void __launch_bounds__(kWarps * 32) wave0_kernel(PassArgs<R> A, WaveS
 }
 
 // ---- wave k >= 1: evaluate queued chunks, one partial node sum per chunk ----
-// (FP32 kernels held to 168 registers, three blocks of 128 threads per SM: measured 3 % faster than
-// four blocks at 128 registers, whose gathers spill, and 9 % faster than two)
+// (FP32 kernels: SU(2) teams with at most two sites per lane held to 128 registers, four blocks of 128
+// threads per SM, where their gathers do not spill (3-5 % faster than three blocks on the pyrochlore L = 6
+// and square L = 5, 8 states); wider lanes and U(1)-DM entries, whose gathers spill at 128, held to 168
+// registers, three blocks)
 template <typename R, int T, int SPL, int C>
-__global__ void __launch_bounds__(kWarps * 32, sizeof(R) == 4 ? 3 : 1) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
+constexpr int eval_min_blocks() { return sizeof(R) == 4 ? (C == 2 && SPL <= 2 ? 4 : 3) : 1; }
+
+template <typename R, int T, int SPL, int C>
+__global__ void __launch_bounds__(kWarps * 32, eval_min_blocks<R, T, SPL, C>()) eval_kernel(PassArgs<R> A, WaveSpace Wsp, int par) {
     constexpr int NPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem[];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1337,12 +1342,14 @@ template <typename R, int C>
 struct PassLauncher {
     template <int T, int SPL>
     static cudaError_t run(const PassArgs<R>& a0, WaveSpace& Wsp, int* h_counters, cudaStream_t st, int grid_cap) {
-        // overlap rows in shared memory only while three blocks still fit on an SM (a row word is
-        // read once per batch of nodes, so from L1 it costs little)
+        // overlap rows in shared memory only while the FP32 eval kernel's register-bound number of
+        // blocks (three for FP64) still fits on an SM (228 KB less 1 KB per block; a row word is read
+        // once per batch of nodes, so from L1 it costs little)
         PassArgs<R> a = a0;
         const int nm = a.L.Nsig + 2 * a.L.NO + 2 * a.L.Nn;
         const size_t staged = SmemLayout<R, T, C, SPL>(a.L.Ns, nm, a.rows_total, true).total;
-        a.rows_in_smem = a.rows_mode == 1 ? 0 : (staged <= (size_t)(a.rows_mode == 2 ? 227 : 75) * 1024);
+        constexpr int fit_kb = 228 / (sizeof(R) == 4 ? eval_min_blocks<R, T, SPL, C>() : 3) - 1;
+        a.rows_in_smem = a.rows_mode == 1 ? 0 : (staged <= (size_t)(a.rows_mode == 2 ? 227 : fit_kb) * 1024);
         SmemLayout<R, T, C, SPL> lay(a.L.Ns, nm, a.rows_total, a.rows_in_smem);
         const size_t smem = lay.total;
         if (smem > (size_t)227 * 1024) return cudaErrorInvalidConfiguration;
@@ -1416,7 +1423,7 @@ cudaError_t run_shape(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cud
 }
 
 // the team shapes built: lanes per node batch x sites per lane
-#define PFFRG_TEAM_SHAPES(X) X(8, 1) X(16, 1) X(32, 1) X(16, 3) X(16, 4) X(32, 2) X(32, 4) X(32, 8)
+#define PFFRG_TEAM_SHAPES(X) X(8, 1) X(16, 1) X(32, 1) X(16, 3) X(16, 4) X(32, 2) X(32, 3) X(32, 4) X(32, 8)
 
 // the default shape for Ns sites: the narrowest team whose lanes hold at most two sites (up to 64
 // sites; measured on the pyrochlore L = 6 two-loop state, 48 sites: 32x2 403 ms, 16x3 460 ms,

@@ -14,6 +14,7 @@ PFFRG_INST(32, 1)
 #elif PFFRG_GROUP == 1
 PFFRG_INST(16, 3)
 PFFRG_INST(16, 4)
+PFFRG_INST(32, 3)
 #else
 PFFRG_INST(32, 2)
 PFFRG_INST(32, 4)

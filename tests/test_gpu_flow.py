@@ -223,7 +223,9 @@ def test_flow_matches_oracle_flow(pkg, O):
     """The whole flow loop against the oracle: launch! in FP64 on the GPU (device steps, device scans and
     resampling, χ after every step) and the same loop of launcher_1l.jl:56-198 restated here on the
     oracle's right-hand side, host scans and resampling (launcher.resample_from_to) and the oracle's χ.
-    Square L = 3, 10/4/3 frequencies, Λ 5 → 0.5: both take the same steps, and χ(ω = 0) agrees at every
+    Square L = 3, 10/4/3 frequencies, Λ 5 → 0.7 (step control rejects steps from Λ ≈ 0.93 on; with these
+    small meshes the flow turns unstable near 0.6): both take the same accepted and rejected steps (the
+    cutoffs agree to 1e-8, the error ratios differing in the last digits), and χ(ω = 0) agrees at every
     accepted cutoff within the stated 1e-6 of max|χ|."""
     from pffrg_gb300 import action as A
     from pffrg_gb300 import frequency as F
@@ -231,7 +233,7 @@ def test_flow_matches_oracle_flow(pkg, O):
     from pffrg_gb300.flow import get_eval
     from pffrg_gb300.launcher import launch, resample_from_to
 
-    kw = dict(num_sigma=10, num_omega=4, num_nu=3, num_chi=4, initial=5.0, final=0.5, parquet=False,
+    kw = dict(num_sigma=10, num_omega=4, num_nu=3, num_chi=4, initial=5.0, final=0.7, parquet=False,
               ode_tol=(1e-3, 1e-3))
     res = launch("", "square", 3, "heisenberg", "su2", [[1.0]], precision="fp64", **kw)
     # the same loop on the oracle
@@ -242,10 +244,10 @@ def test_flow_matches_oracle_flow(pkg, O):
     m = F.initial_mesh(5.0, 10, 4, 3, 4, *p)
     a = A.get_action_empty("su2", r, m)
     A.init_action(lat, r, a)
-    Lam, Lf, bmin, bmax = 5.0, 0.5, 1e-4, 0.1
+    Lam, Lf, bmin, bmax = 5.0, 0.7, 1e-4, 0.1
     dLam = bmax * Lam
-    cps = [5.0, 0.5]
-    lams, chis = [], []
+    cps = [5.0, 0.7]
+    lams, chis, rejected = [], [], 0
     chi_prev = np.zeros((r.num_sites, 4))
     while Lam > Lf:
         P = O.Problem(r, m)
@@ -267,12 +269,16 @@ def test_flow_matches_oracle_flow(pkg, O):
             chi_prev = chi
             a_inter = A.Action.empty_like(a)
             a_inter.buf[:] = inter
-            a_new = A.Action.empty_like(a)
+            a_new = a_inter.copy()  # the resampling keeps the bare couplings of the state
             m = resample_from_to(Lam, *p, m, a_inter, a_new, [chi])
             a = a_new
         else:
             dLam = next_dlam(dLam, Lam)
-    assert res.finished and len(res.Lam) == len(lams)
-    assert np.allclose(res.Lam, lams, rtol=1e-12, atol=0.0)
+            rejected += 1
+    assert rejected > 0
+    n = min(len(res.Lam), len(lams))
+    assert np.allclose(res.Lam[:n], lams[:n], rtol=1e-8, atol=0.0)
     for (Lg, mesh, cg), c in zip(res.chi, chis):
         assert np.max(np.abs(cg[:, 0] - c)) <= 1e-6 * np.max(np.abs(c)), Lg
+    assert res.finished and len(res.Lam) == len(lams), (res.reason, len(res.Lam), len(lams))
+    assert res.rejected == rejected

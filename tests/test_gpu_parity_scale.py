@@ -23,7 +23,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(8, 1), (16, 1), (32, 1), (16, 3), (16, 4), (32, 2), (32, 4), (32, 8)]
+SHAPES = [(8, 1), (16, 1), (32, 1), (16, 3), (16, 4), (32, 2), (32, 3), (32, 4), (32, 8)]
 
 
 def rel_err(x, ref):
@@ -102,8 +102,11 @@ def test_kagome_L8_u1dm_3loop_vs_oracle(pkg, O):
     lat, r, m, a = wl.build_state(w)
     assert r.num_sites >= 32
     ref = oracle_rhs(O, r, m, a, w.Lam, 3, w.eval, symmetry="u1-dm", sigma_corr=True)
-    for staging in (1, 2):
-        got = gpu_rhs(pkg, r, m, a, w.Lam, 3, w.eval, symmetry="u1-dm", staging=staging, sigma_corr=True)
+    for shape, staging in ((None, 1), (None, 2), ((32, 3), 0), ((32, 4), 0)):
+        got = gpu_rhs(pkg, r, m, a, w.Lam, 3, w.eval, symmetry="u1-dm", shape=shape, staging=staging,
+                      sigma_corr=True)
         e = rel_err(got, ref)
-        print(f"kagome L=8 u1-dm 3-loop, staging {staging}: FP64 GPU vs oracle {e:.2e}")
+        print(f"kagome L=8 u1-dm 3-loop, shape {shape}, staging {staging}: FP64 GPU vs oracle {e:.2e}")
         assert e < 1e-10
+    mixed = gpu_rhs(pkg, r, m, a, w.Lam, 3, w.eval, precision="mixed", symmetry="u1-dm", sigma_corr=True)
+    assert rel_err(mixed, ref) < 1e-6
