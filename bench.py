@@ -86,7 +86,7 @@ def config(args, w, extra=None):
     c = {"workload": w.name, "lattice": w.lattice, "L": w.size, "model": w.model, "J": w.J, "symmetry": w.symmetry,
          "loops": w.loops, "Lambda": w.Lam, "num_sigma": w.num_sigma, "num_omega": w.num_omega, "num_nu": w.num_nu,
          "eval": w.eval, "gamma_tol": list(GAMMA_TOL), "sigma_tol": list(SIGMA_TOL), "noise": w.noise, "seed": w.seed,
-         "l2": "flushed between timed steps (256 MiB write); the vertex (5.3 MB) is L2-resident within a step",
+         "l2": "flushed between timed steps (256 MiB write); the vertex is L2-resident within a step",
          "parallelism": f"replicas x{args.gpus}"}
     if extra:
         c.update(extra)
@@ -175,12 +175,17 @@ def ncu_profile_summary():
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (CPU restatement) over every channel task, timed in full
 # ---------------------------------------------------------------------------
+def sigma_corr_of(w) -> bool:
+    """The Σ corrections of compute_dΓ_ml! belong to three or more loops (the launcher's default)."""
+    return w.loops >= 3
+
+
 def cpu_rhs_seconds(O, P, a, w):
     """Wall seconds of one full right-hand side of the oracle (dΣ, then dΓ over all channel tasks)."""
     da = np.zeros_like(a.buf)
     t0 = time.perf_counter()
     O.dsigma(P, w.Lam, a.buf, da, *SIGMA_TOL)
-    O.dgamma(P, w.loops, w.Lam, a.buf, da, w.eval, gtol=GAMMA_TOL)
+    O.dgamma(P, w.loops, w.Lam, a.buf, da, w.eval, gtol=GAMMA_TOL, sigma_corr=sigma_corr_of(w), stol=SIGMA_TOL)
     return time.perf_counter() - t0
 
 
@@ -195,7 +200,7 @@ def reference_arm(args):
     w = wl.WORKLOADS[args.workload]
     lat, r, m, a = wl.build_state(w)
     threads = os.cpu_count() or 1
-    P = O.Problem(r, m, num_threads=threads)
+    P = O.Problem(r, m, symmetry=w.symmetry, S=w.S, num_threads=threads)
     # Every step is one full right-hand side (no task sample).  A step takes seconds on the CPU, so
     # the run does at most one untimed warm-up step and as many of the requested timed steps as fit
     # in the time budget (--ref-seconds); "steps" and "warmup" report what was run.
@@ -277,7 +282,7 @@ def ours(args):
         if dist:
             dist.barrier()
 
-    ctx = FlowContext(r, m, precision="mixed", device=local)
+    ctx = FlowContext(r, m, symmetry=w.symmetry, S=w.S, precision="mixed", device=local)
     ctx.upload(C.SLOT_A, a)
     # the team shape of the quadrature passes, picked by timing one right-hand side per candidate
     # (or given, for profiling runs that must launch the same kernels every time)
@@ -288,7 +293,7 @@ def ours(args):
         team = ctx.autotune_team_shape(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
 
     def rhs():
-        ctx.rhs(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL)
+        ctx.rhs(w.Lam, w.eval, loops=w.loops, gamma_tol=GAMMA_TOL, sigma_tol=SIGMA_TOL, sigma_corr=sigma_corr_of(w))
 
     # warm-up
     for _ in range(args.warmup):
@@ -356,7 +361,7 @@ def ours(args):
     if world == 1 and not args.no_cpu:
         O = entry.load_oracle()
         threads = os.cpu_count() or 1
-        secs = cpu_rhs_seconds(O, O.Problem(r, m, num_threads=threads), a, w)
+        secs = cpu_rhs_seconds(O, O.Problem(r, m, symmetry=w.symmetry, S=w.S, num_threads=threads), a, w)
         cpu = {"value": 1.0 / secs, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"one full right-hand side (dΣ + dΓ over every channel task), {secs:.1f} s; "
                          "CPU restatement of the reference algorithm"}
@@ -365,7 +370,7 @@ def ours(args):
         "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 integrand / f64 quadrature bookkeeping", "data": "synthetic",
         "config": config(args, w, {"precision": "mixed", "wall_ms_per_step": t_wall * 1e3 / args.steps,
-                                   "team_shape": "%dx%d" % team}),
+                                   "team_shape": "%dx%d" % team, "vertex_bytes": action_bytes}),
         "e2e": e2e,
         "gpu_launches": int(round(launches_step * args.steps)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -619,7 +624,8 @@ def end_to_end(args, ctx, pkg, C, a, w, flush, dev, dist, world):
     for _ in range(1):
         D_host.buf[:] = 0.0
         ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
-        ctx.compute_dgamma(w.Lam, A_host, D_host, w.eval, GAMMA_TOL, loops=w.loops)
+        ctx.compute_dgamma(w.Lam, A_host, D_host, w.eval, GAMMA_TOL, loops=w.loops, sigma_corr=sigma_corr_of(w),
+                           sigma_tol=SIGMA_TOL)
     e2e_times = []
     for _ in range(args.steps):
         flush.zero_()
@@ -627,7 +633,8 @@ def end_to_end(args, ctx, pkg, C, a, w, flush, dev, dist, world):
         D_host.buf[:] = 0.0
         t0 = time.perf_counter()
         ctx.compute_dsigma(w.Lam, A_host, D_host, SIGMA_TOL)
-        ctx.compute_dgamma(w.Lam, A_host, D_host, w.eval, GAMMA_TOL, loops=w.loops)
+        ctx.compute_dgamma(w.Lam, A_host, D_host, w.eval, GAMMA_TOL, loops=w.loops, sigma_corr=sigma_corr_of(w),
+                           sigma_tol=SIGMA_TOL)
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(float(np.mean(e2e_times)), dist, dev)
     e2e_value = replica_throughput(world, e2e_s)

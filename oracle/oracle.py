@@ -294,3 +294,185 @@ def num_threads() -> int:
 
 def test_hcubature(which: int, x0: float, x1: float, y0: float, y1: float, atol: float, rtol: float) -> float:
     return float(lib().oracle_test_hcubature(which, x0, x1, y0, y1, atol, rtol))
+
+
+# ---------------------------------------------------------------------------
+# Mesh scans and resampling, restated in numpy from the reference (independent of the package's
+# own host and device code, which the tests check against it)
+# ---------------------------------------------------------------------------
+def get_mesh(linear: float, upper: float, num: int, p: float) -> np.ndarray:
+    """get_mesh (src/Frequency/mesh.jl:86-122): 0, num_lin linear points of width linear / num_lin,
+    then num - num_lin points growing by (upper / linear)^(1 / num_log)."""
+    assert linear > 0.0 and upper > 0.0 and linear < upper
+    num_lin = int(np.ceil(p * num))
+    num_log = num - num_lin
+    assert num_log > 0
+    h = linear / num_lin
+    xi = (upper / linear) ** (1.0 / num_log)
+    mesh = np.zeros(num + 1)
+    for i in range(1, num_lin + 1):
+        mesh[i] = i * h
+    for i in range(1, num_log + 1):
+        mesh[num_lin + i] = xi ** i * linear
+    return mesh
+
+
+def get_param(val: float, lst: np.ndarray):
+    """get_indices + get_param (src/Frequency/param.jl:25-87), 0-based indices: the neighbours of val in
+    the sorted list (both the last entry at or beyond it) and the linear weights."""
+    n = len(lst)
+    if val >= lst[n - 1]:
+        lo = hi = n - 1
+    else:
+        i = 0
+        while val > lst[i]:
+            i += 1
+        lo = hi = i
+        if val < lst[i]:
+            lo -= 1
+    if lo < hi:
+        d = 1.0 / (lst[hi] - lst[lo])
+        return lo, hi, d * (lst[hi] - val), d * (val - lst[lo])
+    return lo, hi, 1.0, 0.0
+
+
+def _sign(x: float) -> float:
+    return 0.0 if x == 0.0 else (np.nan if x != x else (1.0 if x > 0.0 else -1.0))
+
+
+def scan(x: np.ndarray, y: np.ndarray, p0: float, p1: float, p2: float, p3: float, p4: float) -> float:
+    """scan (src/Action/Action.jl:369-446): the linear extent of a new mesh from a cut y(x)."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    n = len(x)
+    num_lin = int(np.ceil(p0 * (n - 1)))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        # a) the first peak at a finite frequency and where the cut has fallen to 75 % of it
+        da = np.inf
+        idx = 0
+        slope = np.float64(y[1] - y[0]) / np.float64(x[1] - x[0])
+        for i in range(1, n - 1):
+            s = np.float64(y[i + 1] - y[i]) / np.float64(x[i + 1] - x[i])
+            if _sign(s) != _sign(slope):
+                idx = i
+                break
+            slope = s
+        if idx > 0:
+            for i in range(idx + 1, n):
+                if abs(np.float64(y[i]) / np.float64(y[idx])) <= 0.75:
+                    da = max(x[i], num_lin * x[idx] / np.ceil(0.5 * num_lin))
+                    break
+        # b) a finite value at the origin: the relative step to the first frequency within (p1, p2)
+        db = num_lin * x[1]
+        if abs(y[0]) / np.max(np.abs(y)) > 1e-2:
+            D = abs(y[1] - y[0]) / max(abs(y[1]), abs(y[0]))
+            while not (p1 < D < p2):
+                if D >= p2:
+                    db *= 0.98
+                elif D <= p1:
+                    db *= 1.02
+                if db >= x[-1]:
+                    break
+                xp = get_mesh(db, x[-1], n - 1, p0)
+                yp = np.empty_like(y)
+                for i in range(n):
+                    lo, hi, wl, wh = get_param(xp[i], x)
+                    yp[i] = wl * y[lo] + wh * y[hi]
+                D = abs(yp[1] - yp[0]) / max(abs(yp[1]), abs(yp[0]))
+    return min(max(num_lin * p3, min(da, db)), p4)
+
+
+def scan_channel(Lam: float, p_O, p_n, O: np.ndarray, nu: np.ndarray, q3: np.ndarray):
+    """scan_channel (src/Action/Action.jl:449-480): scans of the cuts through max |q3| (q3[site, Ω, ν, ν'],
+    the first maximum in column-major order)."""
+    s, w, v, vp = np.unravel_index(int(np.argmax(np.abs(q3).reshape(-1, order="F"))), q3.shape, order="F")
+    cut_O = q3[s, :, v, vp]
+    cut_1 = np.array([q3[s, w, k, k] - q3[s, w, -1, -1] for k in range(len(nu))])
+    cut_2 = np.array([q3[s, w, k, vp] - q3[s, w, -1, vp] for k in range(len(nu))])
+    cut_3 = np.array([q3[s, w, v, k] - q3[s, w, v, -1] for k in range(len(nu))])
+    O_lin = scan(O, cut_O, p_O[0], p_O[1], p_O[2], p_O[3] * Lam, p_O[4] * Lam)
+    n_lin = min(scan(nu, c, p_n[0], p_n[1], p_n[2], p_n[3] * Lam, p_n[4] * Lam) for c in (cut_1, cut_2, cut_3))
+    return O_lin, n_lin
+
+
+def sigma_at(w: float, sigma_mesh: np.ndarray, Sigma: np.ndarray) -> float:
+    """get_Σ (src/Action/Action.jl:8-26): odd in w, interpolated on the mesh, 1 / w beyond it."""
+    if abs(w) <= sigma_mesh[-1]:
+        lo, hi, wl, wh = get_param(abs(w), sigma_mesh)
+        return _sign(w) * (wl * Sigma[lo] + wh * Sigma[hi])
+    return sigma_mesh[-1] * Sigma[-1] / w
+
+
+def resample_channel(O_old, n_old, ch_old: dict, O_new, n_new, ch_new: dict) -> None:
+    """resample_from_to! of a channel (src/Action/channel.jl:416-466): q1, q2_1, q2_2, q3 at the new
+    meshes by linear, bilinear and trilinear interpolation in the reference's term order."""
+    q1, q21, q22, q3 = (ch_old[k] for k in ("q1", "q2_1", "q2_2", "q3"))
+    pO = [get_param(x, O_old) for x in O_new]
+    pn = [get_param(x, n_old) for x in n_new]
+    for w, (l1, h1, a1, b1) in enumerate(pO):
+        ch_new["q1"][:, w] = a1 * q1[:, l1]
+        ch_new["q1"][:, w] += b1 * q1[:, h1]
+    for v, (l2, h2, a2, b2) in enumerate(pn):
+        for w, (l1, h1, a1, b1) in enumerate(pO):
+            for key, q in (("q2_1", q21), ("q2_2", q22)):
+                val = a1 * a2 * q[:, l1, l2]
+                val += b1 * a2 * q[:, h1, l2]
+                val += a1 * b2 * q[:, l1, h2]
+                val += b1 * b2 * q[:, h1, h2]
+                ch_new[key][:, w, v] = val
+    for vp, (l3, h3, a3, b3) in enumerate(pn):
+        for v, (l2, h2, a2, b2) in enumerate(pn):
+            for w, (l1, h1, a1, b1) in enumerate(pO):
+                val = a1 * a2 * a3 * q3[:, l1, l2, l3]
+                val += b1 * a2 * a3 * q3[:, h1, l2, l3]
+                val += a1 * b2 * a3 * q3[:, l1, h2, l3]
+                val += b1 * b2 * a3 * q3[:, h1, h2, l3]
+                val += a1 * a2 * b3 * q3[:, l1, l2, h3]
+                val += b1 * a2 * b3 * q3[:, h1, l2, h3]
+                val += a1 * b2 * b3 * q3[:, l1, h2, h3]
+                val += b1 * b2 * b3 * q3[:, h1, h2, h3]
+                ch_new["q3"][:, w, v, vp] = val
+
+
+def resample_from_to(Lam: float, p_sigma, p_Os, p_ns, p_Ot, p_nt, p_chi, lins, bounds, m_old: dict,
+                     Sigma_old: np.ndarray, G_old: list, Sigma_new: np.ndarray, G_new: list, chi: list) -> dict:
+    """resample_from_to (src/Action/Action.jl:483-548).  Meshes are dicts with sigma, omega_s, nu_s,
+    omega_t, nu_t, chi; a vertex is a list of components, each {"s"|"t"|"u": {"q1", "q2_1", "q2_2",
+    "q3": arrays [site, Ω(, ν(, ν'))]}}; chi is the list of χ[site, ω] arrays.  Fills Sigma_new and
+    G_new and returns the new meshes."""
+    s_lin, Os_lin, ns_lin = lins[1] * Lam, lins[2] * Lam, lins[3] * Lam
+    Ot_lin, nt_lin, chi_lin = lins[2] * Lam, lins[3] * Lam, lins[4] * Lam
+    if Lam < lins[0]:
+        s_lin = p_sigma[1] * m_old["sigma"][int(np.argmax(np.abs(Sigma_old)))]
+        Os_l, ns_l, Ot_l, nt_l = [], [], [], []
+        for comp in G_old:
+            a_s = scan_channel(Lam, p_Os, p_ns, m_old["omega_s"], m_old["nu_s"], comp["s"]["q3"])
+            a_u = scan_channel(Lam, p_Os, p_ns, m_old["omega_s"], m_old["nu_s"], comp["u"]["q3"])
+            Os_l.append(min(a_s[0], a_u[0]))
+            ns_l.append(min(a_s[1], a_u[1]))
+            a_t = scan_channel(Lam, p_Ot, p_nt, m_old["omega_t"], m_old["nu_t"], comp["t"]["q3"])
+            Ot_l.append(a_t[0])
+            nt_l.append(a_t[1])
+        Os_lin, ns_lin, Ot_lin, nt_lin = min(Os_l), min(ns_l), min(Ot_l), min(nt_l)
+        chi_l = []
+        for c in chi:
+            site = np.unravel_index(int(np.argmax(np.abs(c).reshape(-1, order="F"))), c.shape, order="F")[0]
+            chi_l.append(scan(m_old["chi"], c[site, :], p_chi[0], p_chi[1], p_chi[2], p_chi[3] * Lam,
+                              p_chi[4] * Lam))
+        chi_lin = min(chi_l)
+    up = max(Lam, bounds[0])
+    m_new = {
+        "sigma": get_mesh(s_lin, bounds[1] * up, len(m_old["sigma"]) - 1, p_sigma[0]) * p_sigma[2],
+        "omega_s": get_mesh(Os_lin, bounds[2] * up, len(m_old["omega_s"]) - 1, p_Os[0]) * p_Os[5],
+        "nu_s": get_mesh(ns_lin, bounds[3] * up, len(m_old["nu_s"]) - 1, p_ns[0]) * p_ns[5],
+        "omega_t": get_mesh(Ot_lin, bounds[2] * up, len(m_old["omega_t"]) - 1, p_Ot[0]) * p_Ot[5],
+        "nu_t": get_mesh(nt_lin, bounds[3] * up, len(m_old["nu_t"]) - 1, p_nt[0]) * p_nt[5],
+        "chi": get_mesh(chi_lin, bounds[4] * up, len(m_old["chi"]) - 1, p_chi[0]) * p_chi[5],
+    }
+    for k, w in enumerate(m_new["sigma"]):
+        Sigma_new[k] = sigma_at(w, m_old["sigma"], Sigma_old)
+    for old, new in zip(G_old, G_new):
+        resample_channel(m_old["omega_s"], m_old["nu_s"], old["s"], m_new["omega_s"], m_new["nu_s"], new["s"])
+        resample_channel(m_old["omega_t"], m_old["nu_t"], old["t"], m_new["omega_t"], m_new["nu_t"], new["t"])
+        resample_channel(m_old["omega_s"], m_old["nu_s"], old["u"], m_new["omega_s"], m_new["nu_s"], new["u"])
+    return m_new

@@ -218,8 +218,11 @@ __device__ __forceinline__ R gather_one(const PassArgs<R>& A, const NodeScratch<
 // all components of one slot on this lane's sites, v[c][k] = Γ_c(site tl + k T) (the U(1)-DM passes;
 // SU(2) reads its pair-layout copies in Team::gather_su2): bare + Σ_ch sgn Σ_q w_q q_c'[off_q + site]
 // with the read component c' and sign of apply_flags_u1_dm, channels and corners in the reference's
-// order.  The plan is held in registers per channel and the loop over the lane's sites has no branch
-// (padding sites read site 0 and are zeroed at the end), so a channel's reads can be in flight together.
+// order.  The loop over a channel's corners is not unrolled: one corner's reads of all components
+// and sites are in flight together, and the kernel's code stays small enough for the instruction
+// cache (unrolled over the eight corners, six components and the lane's sites, the reads of two
+// slots made the three-loop U(1)-DM kernels wait on instruction fetch 15 cycles per issue).  Padding
+// sites read site 0 and are zeroed at the end.
 template <typename R, int T, int SPL, int C>
 __device__ __forceinline__ void gather_slot(const PassArgs<R>& A, const NodeScratch<R, C>& ns, int slot, int tl,
                                             const int* site_ex, R v[C][SPL]) {
@@ -241,29 +244,34 @@ __device__ __forceinline__ void gather_slot(const PassArgs<R>& A, const NodeScra
         const int kern = P.kernel;
         if (!kern) continue;
         const int nc = corners_of(kern);
-        const int ex = P.exch;
-        R w[8];
-        int off[8];
+        int st[SPL];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            w[q] = q < nc ? P.w[q] : (R)0;
-            off[q] = q < nc ? P.off[q] : 0;
-        }
+        for (int k = 0; k < SPL; ++k) st[k] = P.exch ? site_ex[k] : si[k];
+        const R* q0[C];
+        R sg[C];
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            R sgn;
-            const int cs = comp_read(P, C, c, sgn);
-            const R* q0 = src + A.L.qbase(cs, P.src_ch, kern - 1);
-#pragma unroll
-            for (int k = 0; k < SPL; ++k) {
-                const int st = ex ? site_ex[k] : si[k];
-                R a = (R)0;
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (q < nc) a += w[q] * ldg(q0 + off[q] + st);
-                v[c][k] += sgn * a;
-            }
+            const int cs = comp_read(P, C, c, sg[c]);
+            q0[c] = src + A.L.qbase(cs, P.src_ch, kern - 1);
         }
+        R a[C][SPL];
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) a[c][k] = (R)0;
+#pragma unroll 1
+        for (int q = 0; q < nc; ++q) {
+            const R w = P.w[q];
+            const int off = P.off[q];
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) a[c][k] += w * ldg(q0[c] + off + st[k]);
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c)
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) v[c][k] += sg[c] * a[c][k];
     }
 #pragma unroll
     for (int k = 0; k < SPL; ++k)
@@ -1427,12 +1435,15 @@ cudaError_t run_shape(const PassArgs<R>& a, WaveSpace& Wsp, int* h_counters, cud
 
 // the default shape for Ns sites: the narrowest team whose lanes hold at most two sites (up to 64
 // sites; measured on the pyrochlore L = 6 two-loop state, 48 sites: 32x2 403 ms, 16x3 460 ms,
-// 16x4 511 ms), beyond that at most four or eight
+// 16x4 511 ms), beyond that 32-lane teams with the fewest sites per lane that cover them (32x3 against
+// 32x4: kagome L = 8 U(1)-DM three-loop state, 82 sites, mixed 1445 vs 1823 ms, FP64 4935 vs 5506 ms;
+// pyrochlore L = 7 one-loop, 70 sites, mixed 455 vs 502 ms, FP64 2312 vs 2432 ms)
 __host__ __device__ inline void default_team_shape(int Ns, int& T, int& SPL) {
     if (Ns <= 8) T = 8, SPL = 1;
     else if (Ns <= 16) T = 16, SPL = 1;
     else if (Ns <= 32) T = 32, SPL = 1;
     else if (Ns <= 64) T = 32, SPL = 2;
+    else if (Ns <= 96) T = 32, SPL = 3;
     else if (Ns <= 128) T = 32, SPL = 4;
     else T = 32, SPL = 8;
 }

@@ -47,6 +47,13 @@ WORKLOADS = {
     # the same lattice and state on small meshes (11/4/3 positive frequencies, eval 2, 1 loop): profiling case
     "pyrochlore-L6-reduced": Workload("pyrochlore-L6-reduced", "pyrochlore", 6, "heisenberg", [[1.0]], 1, 1.0, 11, 4,
                                       3, 0.05, 1, bare_on_t=True, eval=2),
+    # kagome L=8 XXZ + DM (J⊥ = 1, Jz = 0.8, Dz = 0.2), U(1)-DM, 3 loops with the Σ corrections, one
+    # right-hand side at Λ=1 on N(0, 0.05) seed 5: the largest workload's meshes (60/20/15) and smaller
+    # ones (30/10/8) for profiling and quick timing
+    "kagome-L8-3l-u1dm": Workload("kagome-L8-3l-u1dm", "kagome", 8, "kagome-xxz-dm", [[1.0, 0.8, 0.2]], 3, 1.0, 60,
+                                  20, 15, 0.05, 5, symmetry="u1-dm"),
+    "kagome-L8-3l-u1dm-reduced": Workload("kagome-L8-3l-u1dm-reduced", "kagome", 8, "kagome-xxz-dm",
+                                          [[1.0, 0.8, 0.2]], 3, 1.0, 30, 10, 8, 0.05, 5, symmetry="u1-dm"),
 }
 
 

@@ -6,6 +6,7 @@ same 3rd-order solution and error ratio in FP64 (1e-10 relative).
 """
 import numpy as np
 import pytest
+from test_oracle_resample import mesh_dict, oracle_view
 
 pytestmark = pytest.mark.gpu
 
@@ -176,9 +177,9 @@ def test_sweep_matches_single_runs(pkg):
 
 
 @pytest.mark.parametrize("symmetry", ["su2", "u1-dm"])
-def test_device_resample_matches_host(pkg, symmetry):
+def test_device_resample_matches_host(pkg, O, symmetry):
     """Mesh scans from the device cuts and the device resampling (pffrg_scan_cuts, pffrg_resample)
-    against the host restatement of resample_from_to (Action.jl:483-557)."""
+    against the host path of resample_from_to (Action.jl:483-557) and the oracle's restatement."""
     import pffrg_gb300._capi as C
     import pffrg_gb300.workloads as wl
     from pffrg_gb300 import frequency as F
@@ -217,6 +218,13 @@ def test_device_resample_matches_host(pkg, symmetry):
             dev = Action.empty_like(a)
             ctx.download(C.SLOT_A, dev)
         assert np.max(np.abs(dev.buf - host.buf)) <= 1e-13 * np.max(np.abs(host.buf))
+        ref = a.copy()
+        S_old, G_old = oracle_view(a)
+        S_new, G_new = oracle_view(ref)
+        m_ref = O.resample_from_to(Lam, *P, mesh_dict(m), S_old, G_old, S_new, G_new, chi)
+        for name, v in m_ref.items():
+            assert np.allclose(getattr(m_dev, name), v, rtol=1e-15, atol=0.0), name
+        assert np.max(np.abs(dev.buf - ref.buf)) <= 1e-13 * np.max(np.abs(ref.buf))
 
 
 def test_flow_matches_oracle_flow(pkg, O):
