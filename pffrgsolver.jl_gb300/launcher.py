@@ -10,6 +10,7 @@ reference's ``*_obs`` / ``*_cp`` HDF5 files (through ``disk`` and ``hdf5``).
 """
 from __future__ import annotations
 
+import bisect
 import math
 import os
 import time
@@ -47,6 +48,20 @@ def params(vals: np.ndarray, x: np.ndarray):
     return lo, hi, wl, wu
 
 
+def _interp1(v: float, x: list, y: list) -> float:
+    """y interpolated at one value v on the sorted list x: get_param (param.jl:26-87) and its linear
+    read-out, scalar (the same arithmetic as params for one value)."""
+    n = len(x)
+    if v >= x[n - 1]:
+        return 1.0 * y[n - 1] + 0.0 * y[n - 1]
+    hi = bisect.bisect_left(x, v)
+    lo = max(hi - 1 if v < x[hi] else hi, 0)
+    if lo < hi:
+        d = 1.0 / (x[hi] - x[lo])
+        return d * (x[hi] - v) * y[lo] + d * (v - x[lo]) * y[hi]
+    return 1.0 * y[lo] + 0.0 * y[hi]
+
+
 def get_sigma(w: float, sigma_mesh: np.ndarray, Sig: np.ndarray) -> float:
     """get_Σ (Action.jl:8-26)."""
     if abs(w) <= sigma_mesh[-1]:
@@ -80,6 +95,7 @@ def scan(x, y, p0, p1, p2, p3, p4) -> float:
     # b) finite value at the origin: p1 < Δ < p2
     db = num_lin * x[1]
     if abs(y[0]) / np.max(np.abs(y)) > 1e-2:
+        xl, yl = x.tolist(), y.tolist()
         delta = abs(y[1] - y[0]) / max(abs(y[1]), abs(y[0]))
         while not (p1 < delta < p2):
             if delta >= p2:
@@ -88,10 +104,12 @@ def scan(x, y, p0, p1, p2, p3, p4) -> float:
                 db *= 1.02
             if db >= x[-1]:
                 break
-            xp = F.get_mesh(db, x[-1], len(x) - 1, p0)
-            lo, hi, wl, wu = params(xp, x)
-            yp = wl * y[lo] + wu * y[hi]
-            delta = abs(yp[1] - yp[0]) / max(abs(yp[1]), abs(yp[0]))
+            # Δ reads only the first two points of the trial mesh get_mesh(δb, x[end], len(x) - 1, p0):
+            # 0 and its first linear point δb / num_lin (the same values as building the whole mesh
+            # and interpolating y on it; the loop can take a few hundred 2 % steps, so it stays scalar)
+            yp0 = _interp1(0.0, xl, yl)
+            yp1 = _interp1(1 * (db / num_lin), xl, yl)
+            delta = abs(yp1 - yp0) / max(abs(yp1), abs(yp0))
     # c) merge and bound
     return min(max(num_lin * p3, min(da, db)), p4)
 

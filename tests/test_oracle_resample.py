@@ -103,3 +103,26 @@ def test_host_resample_matches_oracle(pkg, O, symmetry, Lam):
     for k, v in m_ref.items():
         assert np.allclose(getattr(m_host, k), v, rtol=1e-15, atol=0.0), k
     assert np.max(np.abs(host.buf - ref.buf)) <= 1e-13 * np.max(np.abs(ref.buf))
+
+
+def test_host_scan_bit_exact_vs_oracle(pkg, O):
+    """launcher.scan (whose δb loop reads only the two trial-mesh points that Δ uses) returns exactly
+    the oracle's scan, which rebuilds the whole trial mesh every step as the reference does, on cuts
+    that decay, peak at a finite frequency or are noise."""
+    from pffrg_gb300 import frequency as F
+    from pffrg_gb300 import launcher as LA
+
+    rng = np.random.default_rng(0)
+    for t in range(300):
+        n = int(rng.integers(6, 40))
+        x = F.get_mesh(rng.uniform(0.1, 3.0), rng.uniform(5.0, 50.0), n - 1, 0.4)
+        kind = t % 3
+        if kind == 0:
+            y = np.exp(-x / rng.uniform(0.1, 5.0)) * rng.normal()
+        elif kind == 1:
+            y = rng.normal(size=n)
+        else:
+            y = 1.0 / (1.0 + (x - rng.uniform(0.0, 3.0)) ** 2)
+        p = (0.4, rng.uniform(0.005, 0.05), rng.uniform(0.05, 0.2), 0.05 * rng.uniform(0.1, 5.0),
+             40.0 * rng.uniform(0.1, 5.0))
+        assert LA.scan(x, y, *p) == O.scan(x, y, *p), t
