@@ -96,6 +96,7 @@ def scan(x, y, p0, p1, p2, p3, p4) -> float:
     db = num_lin * x[1]
     if abs(y[0]) / np.max(np.abs(y)) > 1e-2:
         xl, yl = x.tolist(), y.tolist()
+        yp0 = _interp1(0.0, xl, yl)  # the trial meshes all start at 0
         delta = abs(y[1] - y[0]) / max(abs(y[1]), abs(y[0]))
         while not (p1 < delta < p2):
             if delta >= p2:
@@ -107,7 +108,6 @@ def scan(x, y, p0, p1, p2, p3, p4) -> float:
             # Δ reads only the first two points of the trial mesh get_mesh(δb, x[end], len(x) - 1, p0):
             # 0 and its first linear point δb / num_lin (the same values as building the whole mesh
             # and interpolating y on it; the loop can take a few hundred 2 % steps, so it stays scalar)
-            yp0 = _interp1(0.0, xl, yl)
             yp1 = _interp1(1 * (db / num_lin), xl, yl)
             delta = abs(yp1 - yp0) / max(abs(yp1), abs(yp0))
     # c) merge and bound
