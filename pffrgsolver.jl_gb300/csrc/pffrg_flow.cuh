@@ -587,17 +587,18 @@ struct Team {
         }
     }
 
-    // second half: the overlap sums (flow_su2_t.jl:66-75) of the whole batch.  The team's lanes
-    // are (node j of the batch, row group q of G = T / NB): all lanes walk the sites in the same
-    // order, a lane adds every G-th row of a site for its node (the row word is the same for the NB
-    // lanes of a group, the vertex pairs of neighbouring nodes are neighbours in shared memory),
-    // the G partial sums meet by shuffles, and the owner of a site adds -p (-2) (2S) times them to
-    // its nodes' local parts and hands the nodes to the sink.  Nodes past `count` hold stale values
-    // whose sums are never used.
+    // second half: the overlap sums (flow_su2_t.jl:66-75) of the whole batch.  All lanes walk the
+    // sites in the same order; a lane takes every T-th row of a site, decodes it once and adds the
+    // row's product for every node of the batch (the (spin, density) pairs of a site's nodes are
+    // neighbours in shared memory: two 16-byte reads per vertex slot and row); the 2 NB partial sums
+    // of the lanes meet by shuffles that halve the values a lane carries at every step, and one
+    // lane per value stores its total.  Then the owner of a site adds -p (-2) (2S) times them to
+    // its nodes' local parts and hands the nodes to the sink.  (The earlier split, NB lanes per row
+    // each adding one node, decoded every row NB times: 376 against 352 ms for the config-2
+    // right-hand side.)  Nodes past `count` hold stale values whose sums are never used.
     template <class Sink>
     __device__ __forceinline__ void eval_t_overlap(int count, Sink& sink) {
         constexpr int NB = BatchOf<T, C, SPL>::NB;
-        constexpr int G = T / NB;  // row groups per node
         using R2 = typename std::conditional<sizeof(R) == 4, float2, double2>::type;
         const int Ns = A.L.Ns;
         constexpr int SS = t_site_stride<R, NB>();
@@ -605,25 +606,61 @@ struct Team {
         const R2* tb2 = tb1 + (size_t)Ns * SS;
         R2* ov = const_cast<R2*>(tb2) + (size_t)Ns * SS;  // [Ns][NB] overlap sums
         const R2* tloc = ov + (size_t)Ns * NB;
-        const int j = tl % NB, q = tl / NB;
         const unsigned team_mask = (T == 32) ? kFull : (((1u << T) - 1u) << ((threadIdx.x & 31) / T * T));
+        constexpr int V = 2 * NB;  // sums per site: (spin, density) of every node of the batch
+        R* ovr = reinterpret_cast<R*>(ov);
         for (int i = 0; i < Ns; ++i) {
-            R Ss = (R)0, Sd = (R)0;
+            R x[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) x[v] = (R)0;
             const int j1 = row_off[i + 1];
-            for (int r = row_off[i] + q; r < j1; r += G) {
+            for (int r = row_off[i] + tl; r < j1; r += T) {
                 const unsigned row = rows[r];
                 const int ia = row & 0xff, ib = (row >> 8) & 0xff;
                 const R m = (R)(row >> 16);
-                const R2 a = tb1[(size_t)ia * SS + j], b = tb2[(size_t)ib * SS + j];
-                Ss += m * a.x * b.x;
-                Sd += m * a.y * b.y;
-            }
+                const R2* pa = tb1 + (size_t)ia * SS;
+                const R2* pb = tb2 + (size_t)ib * SS;
+                if constexpr (sizeof(R) == 4 && NB % 2 == 0) {
 #pragma unroll
-            for (int o = NB; o < T; o <<= 1) {
-                Ss += __shfl_xor_sync(team_mask, Ss, o);
-                Sd += __shfl_xor_sync(team_mask, Sd, o);
+                    for (int j2 = 0; j2 < NB / 2; ++j2) {
+                        const float4 a = reinterpret_cast<const float4*>(pa)[j2];
+                        const float4 b = reinterpret_cast<const float4*>(pb)[j2];
+                        x[4 * j2 + 0] += m * a.x * b.x;
+                        x[4 * j2 + 1] += m * a.y * b.y;
+                        x[4 * j2 + 2] += m * a.z * b.z;
+                        x[4 * j2 + 3] += m * a.w * b.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < NB; ++j) {
+                        const R2 a = pa[j], b = pb[j];
+                        x[2 * j] += m * a.x * b.x;
+                        x[2 * j + 1] += m * a.y * b.y;
+                    }
+                }
             }
-            if (q == 0) ov[(size_t)i * NB + j] = R2{Ss, Sd};
+            // sum over the team's lanes, halving the values each lane carries at every step
+            int n = V, idx = 0;
+#pragma unroll
+            for (int o = T / 2; o >= 1; o >>= 1) {
+                if (n > 1) {
+                    n >>= 1;
+                    const bool up = (tl & o) != 0;
+#pragma unroll
+                    for (int k = 0; k < V / 2; ++k) {
+                        if (k < n) {
+                            const R send = up ? x[k] : x[k + n];
+                            const R keep = up ? x[k + n] : x[k];
+                            x[k] = keep + __shfl_xor_sync(team_mask, send, o);
+                        }
+                    }
+                    if (up) idx += n;
+                } else {
+                    x[0] += __shfl_xor_sync(team_mask, x[0], o);
+                }
+            }
+            // every lane now holds the total of value idx; one lane per value writes it
+            if ((tl & (T / V - 1)) == 0) ovr[((size_t)i * NB) * 2 + idx] = x[0];
         }
         __syncwarp(team_mask);
         const R twoS = (R)A.twoS;
