@@ -97,8 +97,20 @@ struct pffrg_ctx {
     int* chi_split = nullptr;
     size_t chi_reg_bytes = 0;
     int* chi_jobs = nullptr;  // job list of a cubature launch
-    int* chi_over = nullptr;  // per-job overflow flags
+    int* chi_over = nullptr;  // per job: 1 overflow, else minus the regions it needed
     int* chi_ctl = nullptr;   // per-job round orders of a cluster
+    // the integrals that needed a cluster's capacity at the previous call run first, on a second
+    // stream with their own region records, alongside the others
+    cudaStream_t st_chi = nullptr;
+    cudaEvent_t ev_chi = nullptr;
+    double* chi_reg2 = nullptr;
+    int* chi_split2 = nullptr;
+    size_t chi_reg_bytes2 = 0;
+    int* chi_jobs2 = nullptr;
+    int* chi_over2 = nullptr;
+    int* chi_ctl2 = nullptr;
+    long long chi_n2 = 0;             // jobs the second stream's job and overflow words hold
+    std::vector<long long> chi_need;  // per integral: the capacity it needed at the previous call
     double* chi_box = nullptr;
     double* chi_out = nullptr;
     double* chi_mesh = nullptr;
@@ -574,16 +586,22 @@ int check_finite(pffrg_ctx* ctx, const double* a) {
 }
 
 // compute_χ! (correlation_su2.jl:58-86, correlation_u1_dm.jl:152-190) on a
-// device action.  Every (ω, site, component, box) integral starts with a
-// small region capacity; the integrals that run out of it are run again with
-// 8x the capacity, up to the reference's bound of 10^7 integrand evaluations
-// per cubature (10^7 / 34 cuts).
+// device action.  Every (ω, site, component, box) integral starts with the
+// region capacity it needed at the previous call (512 at the first); the
+// integrals that run out of it are run again with 8x the capacity, up to the
+// reference's bound of 10^7 integrand evaluations per cubature (10^7 / 34
+// cuts).  The integrals that needed a cluster's capacity run on a second
+// stream alongside the others, so the longest ones start first and the SMs
+// their last waves leave idle take the small ones.  An integral's result
+// does not depend on its capacity or on the stream.
 int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh, int num_chi, double atol,
             double rtol, double* chi) {
     if (num_chi < 1 || !chi_mesh || !chi) return ctx->fail(PFFRG_E_ARGS, "empty correlation mesh or output");
     const int Ns = ctx->L.Ns;
     const int ncomp = ctx->L.C == 2 ? 1 : 3;  // χ, or χxx, χzz, χxy
     const long long njobs = 9ll * ncomp * Ns * num_chi;
+    // a call that failed may have left integrals running on the second stream
+    if (ctx->st_chi) CK(cudaStreamSynchronize(ctx->st_chi));
     if (num_chi > ctx->chi_n) {
         for (double** p : {&ctx->chi_mesh, &ctx->chi_box, &ctx->chi_out}) {
             CK(stream_free(ctx->st, *p));
@@ -628,56 +646,183 @@ int chi_dev(pffrg_ctx* ctx, double Lam, const double* a, const double* chi_mesh,
     c.evals = ctx->counter + 2;  // [2..5] of the context's counters
     CK(cudaMemsetAsync(c.evals, 0, 4 * sizeof(unsigned long long), ctx->st));
     const long long cap_max = 10000000 / 34 + 2;
-    const size_t budget = (size_t)16 << 30;
-    std::vector<int> todo(njobs), over;
-    for (long long j = 0; j < njobs; ++j) todo[j] = (int)j;
-    long long cap = 512;
-    while (!todo.empty()) {
-        const size_t per_job = (size_t)cap * (10 * sizeof(double) + 4 * sizeof(int));
-        const long long batch = std::max<long long>(1, std::min<long long>((long long)todo.size(),
-                                                                           (long long)(budget / per_job)));
-        if (per_job * (size_t)batch > ctx->chi_reg_bytes) {
-            CK(stream_free(ctx->st, ctx->chi_reg));
-            CK(stream_free(ctx->st, ctx->chi_split));
-            ctx->chi_reg = nullptr;
-            ctx->chi_split = nullptr;
-            ctx->chi_reg_bytes = 0;
-            CK(cudaMalloc(&ctx->chi_reg, sizeof(double) * 10 * (size_t)cap * batch));
-            CK(cudaMalloc(&ctx->chi_split, sizeof(int) * 4 * (size_t)cap * batch));
-            ctx->chi_reg_bytes = per_job * (size_t)batch;
+    const size_t budget = (size_t)16 << 30;  // region records of one launch (each stream)
+    const size_t rec = 10 * sizeof(double) + 4 * sizeof(int);
+    // capacity ladder: 512, 4096, 32768, 262144 regions, then the bound of 10^7 evaluations; an
+    // integral that outgrows a capacity starts again from its first region with the next one
+    auto next_cap = [&](long long cap) { return cap * 64 > cap_max ? cap_max : cap * 8; };
+    auto cap_for = [&](long long n) {
+        long long cap = 512;
+        while (cap < n && cap < cap_max) cap = next_cap(cap);
+        return cap;
+    };
+    // every integral starts at the capacity it needed at the previous call on the same jobs (with
+    // a quarter's room to grow): a flow measures χ after every step, on a state that changes
+    // little, so the integrals that need clusters are known before they are run
+    if ((long long)ctx->chi_need.size() != njobs) ctx->chi_need.assign(njobs, 512);
+    auto record = [&](int job, int ov) { ctx->chi_need[job] = cap_for((long long)(-ov) + (-ov) / 4); };
+    auto ensure_reg = [&](double*& reg, int*& split, size_t& bytes, cudaStream_t st, long long cap,
+                          long long batch) -> int {
+        const size_t need = (size_t)cap * rec * (size_t)batch;
+        if (need <= bytes) return 0;
+        CK(stream_free(st, reg));
+        CK(stream_free(st, split));
+        reg = nullptr;
+        split = nullptr;
+        bytes = 0;
+        CK(cudaMalloc(&reg, sizeof(double) * 10 * (size_t)cap * batch));
+        CK(cudaMalloc(&split, sizeof(int) * 4 * (size_t)cap * batch));
+        bytes = need;
+        return 0;
+    };
+    auto launch = [&](ChiArgs cc, const int* jobs_dev, int nb, int* over_dev, long long cap, cudaStream_t st) -> int {
+        ++ctx->launches;
+        // the integrals that need large capacities are few and long: a cluster of blocks evaluates
+        // each round's regions of one integral
+        const int cl = cap >= ctx->chi_cluster_min ? ctx->chi_cluster_blocks : 1;
+        cc.cap = cap;
+        cudaError_t le = launch_chi_boxes(cc, jobs_dev, nb, over_dev, cl, st);
+        if (le != cudaSuccess && cl > 8) {
+            // a 16-block cluster did not launch (non-portable size): clusters of 8 from now on
+            // (measured on the GB300: 16-block clusters were 20-30 % slower than 8, so 8 is the default)
+            cudaGetLastError();
+            ctx->chi_cluster_blocks = 8;
+            le = launch_chi_boxes(cc, jobs_dev, nb, over_dev, 8, st);
         }
-        c.reg = ctx->chi_reg;
-        c.reg_split = ctx->chi_split;
-        c.ctl = ctx->chi_ctl;
-        c.cap = cap;
-        std::vector<int> next;
-        for (size_t s = 0; s < todo.size(); s += (size_t)batch) {
-            const int nb = (int)std::min<size_t>((size_t)batch, todo.size() - s);
-            CK(cudaMemcpyAsync(ctx->chi_jobs, todo.data() + s, sizeof(int) * nb, cudaMemcpyHostToDevice, ctx->st));
-            ++ctx->launches;
-            // the integrals that outgrew the first capacities are few and long: a cluster of
-            // blocks evaluates each round's regions of one integral
-            const int cl = cap >= ctx->chi_cluster_min ? ctx->chi_cluster_blocks : 1;
-            cudaError_t le = launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, cl, ctx->st);
-            if (le != cudaSuccess && cl > 8) {
-                // a 16-block cluster did not launch (non-portable size): clusters of 8 from now on
-                // (measured on the GB300: 16-block clusters were 20-30 % slower than 8, so 8 is the default)
-                cudaGetLastError();
-                ctx->chi_cluster_blocks = 8;
-                le = launch_chi_boxes(c, ctx->chi_jobs, nb, ctx->chi_over, 8, ctx->st);
+        CK(le);
+        return 0;
+    };
+    // 1. the integrals that needed a cluster last time: one launch per capacity on the second
+    //    stream, their overflow words read after the rest
+    std::vector<std::vector<int>> big(8);
+    std::vector<long long> big_cap(8, 0);
+    std::vector<int> todo;
+    for (long long j = 0; j < njobs; ++j) {
+        const long long cap = ctx->chi_need[j];
+        if (cap < ctx->chi_cluster_min) {
+            todo.push_back((int)j);
+            continue;
+        }
+        int level = 0;
+        for (long long c2 = 512; c2 < cap; c2 = next_cap(c2)) ++level;
+        big[level].push_back((int)j);
+        big_cap[level] = cap;
+    }
+    std::vector<int> big_jobs;  // in launch order, each launch's words at its offset
+    std::vector<long long> big_cap_of;
+    for (int l = 7; l >= 0; --l)
+        for (int j : big[l]) {
+            big_jobs.push_back(j);
+            big_cap_of.push_back(big_cap[l]);
+        }
+    if (!big_jobs.empty()) {
+        if (!ctx->st_chi) {
+            CK(cudaStreamCreateWithFlags(&ctx->st_chi, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&ctx->ev_chi, cudaEventDisableTiming));
+        }
+        if (!ctx->chi_jobs2 || ctx->chi_n2 < njobs) {
+            for (int** q : {&ctx->chi_jobs2, &ctx->chi_over2, &ctx->chi_ctl2}) {
+                CK(stream_free(ctx->st_chi, *q));
+                *q = nullptr;
             }
-            CK(le);
-            over.resize(nb);
-            CK(cudaMemcpyAsync(over.data(), ctx->chi_over, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->st));
-            CK(cudaStreamSynchronize(ctx->st));
-            for (int q = 0; q < nb; ++q)
-                if (over[q]) next.push_back(todo[s + q]);
+            CK(cudaMalloc(&ctx->chi_jobs2, sizeof(int) * (size_t)njobs));
+            CK(cudaMalloc(&ctx->chi_over2, sizeof(int) * (size_t)njobs));
+            CK(cudaMalloc(&ctx->chi_ctl2, sizeof(int) * 4 * (size_t)njobs));
+            ctx->chi_n2 = njobs;
         }
-        todo.swap(next);
-        if (!todo.empty()) {
-            if (cap >= cap_max) return ctx->fail(PFFRG_E_LIMIT, "cubature of χ needs more than %lld regions", cap_max);
-            // a job that outgrows 8x would restart close to the cap: take the cap at once
-            cap = cap * 64 > cap_max ? cap_max : cap * 8;
+        long long reg_cap = 0, reg_batch = 0;
+        for (size_t k = 0; k < big_jobs.size();) {
+            size_t e = k;
+            while (e < big_jobs.size() && big_cap_of[e] == big_cap_of[k]) ++e;
+            const long long cap = big_cap_of[k];
+            const long long batch = std::max<long long>(1, std::min<long long>((long long)(e - k),
+                                                                               (long long)(budget / (cap * rec))));
+            if ((size_t)cap * batch > (size_t)reg_cap * reg_batch) reg_cap = cap, reg_batch = batch;
+            k = e;
+        }
+        if (int rc = ensure_reg(ctx->chi_reg2, ctx->chi_split2, ctx->chi_reg_bytes2, ctx->st_chi, reg_cap, reg_batch))
+            return rc;
+        // the second stream starts after the inputs of this call (mesh, status, counters, FP32 copy)
+        CK(cudaEventRecord(ctx->ev_chi, ctx->st));
+        CK(cudaStreamWaitEvent(ctx->st_chi, ctx->ev_chi, 0));
+        CK(cudaMemcpyAsync(ctx->chi_jobs2, big_jobs.data(), sizeof(int) * big_jobs.size(), cudaMemcpyHostToDevice,
+                           ctx->st_chi));
+        ChiArgs c2 = c;
+        c2.reg = ctx->chi_reg2;
+        c2.reg_split = ctx->chi_split2;
+        c2.ctl = ctx->chi_ctl2;
+        for (size_t k = 0; k < big_jobs.size();) {
+            const long long cap = big_cap_of[k];
+            size_t e = k;
+            while (e < big_jobs.size() && big_cap_of[e] == cap) ++e;
+            const long long batch = std::max<long long>(1, (long long)(budget / (cap * rec)));
+            for (size_t b = k; b < e; b += (size_t)batch) {
+                const int nb = (int)std::min<size_t>((size_t)batch, e - b);
+                if (int rc = launch(c2, ctx->chi_jobs2 + b, nb, ctx->chi_over2 + b, cap, ctx->st_chi)) return rc;
+            }
+            k = e;
+        }
+    }
+    // 2. the rest on the context's stream, up the ladder from their capacities
+    std::vector<int> over;
+    long long cap = 512;
+    for (int j : todo) cap = std::max(cap, ctx->chi_need[j]);
+    auto run_ladder = [&](std::vector<int>& jobs, long long cap) -> int {
+        while (!jobs.empty()) {
+            const long long batch = std::max<long long>(1, std::min<long long>((long long)jobs.size(),
+                                                                               (long long)(budget / (cap * rec))));
+            if (int rc = ensure_reg(ctx->chi_reg, ctx->chi_split, ctx->chi_reg_bytes, ctx->st, cap, batch)) return rc;
+            c.reg = ctx->chi_reg;
+            c.reg_split = ctx->chi_split;
+            c.ctl = ctx->chi_ctl;
+            std::vector<int> next;
+            for (size_t s0 = 0; s0 < jobs.size(); s0 += (size_t)batch) {
+                const int nb = (int)std::min<size_t>((size_t)batch, jobs.size() - s0);
+                CK(cudaMemcpyAsync(ctx->chi_jobs, jobs.data() + s0, sizeof(int) * nb, cudaMemcpyHostToDevice,
+                                   ctx->st));
+                if (int rc = launch(c, ctx->chi_jobs, nb, ctx->chi_over, cap, ctx->st)) return rc;
+                over.resize(nb);
+                CK(cudaMemcpyAsync(over.data(), ctx->chi_over, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->st));
+                CK(cudaStreamSynchronize(ctx->st));
+                for (int q = 0; q < nb; ++q) {
+                    if (over[q] > 0) next.push_back(jobs[s0 + q]);
+                    else record(jobs[s0 + q], over[q]);
+                }
+            }
+            jobs.swap(next);
+            if (!jobs.empty()) {
+                if (cap >= cap_max)
+                    return ctx->fail(PFFRG_E_LIMIT, "cubature of χ needs more than %lld regions", cap_max);
+                cap = next_cap(cap);
+            }
+        }
+        return 0;
+    };
+    // the small integrals all start at the largest of their remembered capacities (a launch has
+    // one capacity; an integral's result does not depend on it)
+    if (int rc = run_ladder(todo, cap)) return rc;
+    // 3. the second stream's integrals: those that outgrew their capacity go up the ladder here
+    if (!big_jobs.empty()) {
+        CK(cudaStreamSynchronize(ctx->st_chi));
+        over.resize(big_jobs.size());
+        CK(cudaMemcpy(over.data(), ctx->chi_over2, sizeof(int) * big_jobs.size(), cudaMemcpyDeviceToHost));
+        std::vector<std::vector<int>> grow(8);
+        for (size_t k = 0; k < big_jobs.size(); ++k) {
+            if (over[k] <= 0) {
+                record(big_jobs[k], over[k]);
+                continue;
+            }
+            if (big_cap_of[k] >= cap_max)
+                return ctx->fail(PFFRG_E_LIMIT, "cubature of χ needs more than %lld regions", cap_max);
+            int level = 0;
+            for (long long c2 = 512; c2 < next_cap(big_cap_of[k]); c2 = next_cap(c2)) ++level;
+            grow[level].push_back(big_jobs[k]);
+        }
+        for (int l = 0; l < 8; ++l) {
+            if (grow[l].empty()) continue;
+            long long cl = 512;
+            for (int q = 0; q < l; ++q) cl = next_cap(cl);
+            if (int rc = run_ladder(grow[l], cl)) return rc;
         }
     }
     for (;;) {
@@ -889,12 +1034,14 @@ void pffrg_destroy(pffrg_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
+    if (ctx->st_chi) cudaStreamSynchronize(ctx->st_chi);
     void* ptrs[] = {ctx->lat.exch, ctx->lat.mult, ctx->lat.ov_off, ctx->lat.ov_rows, ctx->wave_mem,
                     ctx->mesh, ctx->log_bounds, ctx->da_l, ctx->da_c, ctx->da_temp, ctx->da_sig, ctx->sig_tmp, ctx->f_a, ctx->f_da,
                     ctx->f_dal, ctx->f_dtemp, ctx->corrs, ctx->corrs_sde, ctx->partial, ctx->scalars, ctx->status,
                     ctx->counter, ctx->tasks_sym, ctx->tasks_full, ctx->tasks_red, ctx->chi_reg, ctx->chi_split,
                     ctx->chi_box, ctx->chi_out, ctx->chi_mesh, ctx->chi_jobs, ctx->chi_over, ctx->chi_ctl, ctx->gk_seg,
-                    ctx->mesh_new, ctx->mesh_ff, ctx->scan_arg, ctx->scan_cuts};
+                    ctx->mesh_new, ctx->mesh_ff, ctx->scan_arg, ctx->scan_cuts, ctx->chi_reg2, ctx->chi_split2,
+                    ctx->chi_jobs2, ctx->chi_over2, ctx->chi_ctl2};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < PFFRG_NUM_SLOTS; ++k)
@@ -904,6 +1051,8 @@ void pffrg_destroy(pffrg_ctx* ctx) {
     for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->rhs_ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->ev_chi) cudaEventDestroy(ctx->ev_chi);
+    if (ctx->st_chi) cudaStreamDestroy(ctx->st_chi);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
 }

@@ -1008,7 +1008,7 @@ __global__ void __launch_bounds__(kChiThreads, 1) chi_box_kernel(ChiArgs A, cons
         double I = 0.0;
         for (int t = 0; t < kChiSumBlocks; ++t) I += S.f[t];
         A.box_out[job] = I;
-        overflow[slot] = over;
+        overflow[slot] = over ? 1 : -n;  // the regions the integral needed, when it fitted
         if (A.evals && !over) {
             atomicAdd(A.evals, (unsigned long long)S.numeval);
             atomicMax(A.evals + 1, (unsigned long long)n);

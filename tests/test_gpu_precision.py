@@ -143,3 +143,29 @@ def test_chi_mixed_vs_fp64(pkg):
     e = rel_err(out["mixed"], out["fp64"])
     print(f"χ mixed vs FP64: {e:.2e}")
     assert e < 1e-6
+
+
+def test_chi_remembered_capacities_identical(pkg):
+    """χ of the same state twice in one context: the second call starts every integral at the capacity the
+    first one needed and runs those that need a cluster on a second stream, alongside the others; the
+    values and the evaluation counts are those of the first call."""
+    import dataclasses
+
+    import pffrg_gb300._capi as C
+    import pffrg_gb300.workloads as wl
+    from pffrg_gb300.flow import FlowContext
+
+    w = dataclasses.replace(wl.WORKLOADS["square-L3-1l"], noise=0.1)
+    lat, r, m, a = wl.build_state(w)
+    chi_mesh = np.array([0.0, 0.1, 0.5, 2.0])
+    with FlowContext(r, m, precision="fp64") as ctx:
+        ctx.upload(C.SLOT_A, a)
+        got = []
+        for _ in range(3):
+            got.append(ctx.chi_slot(0.15, C.SLOT_A, chi_mesh))
+            st = ctx.read_stats()
+            got.append((st["chi_evals"], st["chi_regions_max"]))
+    print("χ evaluations, most regions of one integral:", got[1])
+    assert got[1][1] > 32768  # some integrals need a cluster, so the later calls use the second stream
+    assert np.array_equal(got[0], got[2]) and np.array_equal(got[0], got[4])
+    assert got[1] == got[3] == got[5]
