@@ -594,8 +594,9 @@ struct Team {
     // of the lanes meet by shuffles that halve the values a lane carries at every step, and one
     // lane per value stores its total.  Then the owner of a site adds -p (-2) (2S) times them to
     // its nodes' local parts and hands the nodes to the sink.  (The earlier split, NB lanes per row
-    // each adding one node, decoded every row NB times: 376 against 352 ms for the config-2
-    // right-hand side.)  Nodes past `count` hold stale values whose sums are never used.
+    // each adding one node, decoded every row NB times: 376 against 352 ms for the pyrochlore
+    // L = 6 two-loop right-hand side at 50/15/10 frequencies.)  Nodes past `count` hold stale
+    // values whose sums are never used.
     template <class Sink>
     __device__ __forceinline__ void eval_t_overlap(int count, Sink& sink) {
         constexpr int NB = BatchOf<T, C, SPL>::NB;

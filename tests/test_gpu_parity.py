@@ -50,7 +50,7 @@ def test_dgamma_fp64_small(pkg, O, lattice, size, loops):
     assert rel_err(da.buf, ref) < 1e-10
 
 
-def test_dgamma_fp64_config1_full(pkg, O):
+def test_dgamma_fp64_square_L3_full(pkg, O):
     """Square L=3, 50/15/10 frequencies, Λ=1, N(0, 0.1) seed 0, 1 loop (the CPU-runnable benchmark case)."""
     from pffrg_gb300.flow import FlowContext
 
@@ -63,7 +63,7 @@ def test_dgamma_fp64_config1_full(pkg, O):
     assert rel_err(da.buf, ref) < 1e-10
 
 
-def test_dgamma_mixed_config1(pkg, O):
+def test_dgamma_mixed_square_L3(pkg, O):
     """Mixed precision against the FP64 oracle (the stated bound: 1e-6 relative in the max norm)."""
     from pffrg_gb300.flow import FlowContext
 
