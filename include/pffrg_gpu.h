@@ -7,7 +7,8 @@
  * (Julia Vector/Array{Float64}, column-major, site index fastest) and the
  * output arrays are overwritten in place.  Index tables are passed 1-based
  * exactly as the reference stores them.  A context owns all device memory
- * (device-resident actions and scratch) and one CUDA stream; calls on one
+ * (device-resident actions and scratch) and its CUDA streams (one, plus a
+ * second one that the χ calls use for their largest integrals); calls on one
  * context are synchronous on return and must come from one host thread at a
  * time; separate contexts are independent.
  *
@@ -247,7 +248,10 @@ int pffrg_set_chi_integrand(pffrg_ctx* ctx, int precision);
  * action `a` at Λ on the frequencies chi_mesh[0..num_chi), written
  * column-major into chi (host): Ns * num_chi values for su2, three such
  * blocks χxx | χzz | χxy for u1-dm.  Tolerances are χ_tol = (atol, rtol)
- * (default (1e-8, 1e-4) in src/Launcher/Launcher.jl:111). */
+ * (default (1e-8, 1e-4) in src/Launcher/Launcher.jl:111).  The context
+ * remembers each integral's region capacity from its previous χ call with
+ * the same number of sites and frequencies and starts there (the results do
+ * not depend on it). */
 int pffrg_chi(pffrg_ctx* ctx, double Lam, const pffrg_action_view* a, const double* chi_mesh, int num_chi,
               double atol, double rtol, double* chi);
 /* the same on the device-resident action in `slot` (the measure step of
