@@ -420,6 +420,8 @@ struct ChiScratch {
             unsigned cnt[kChiThreads / 32][256];
         } sort;
     };
+    // the FP64 integrand's propagator factors of a chunk's regions: [region][7 x | 7 y] coordinates
+    double gfac[kChiChunk * 14];
     unsigned wsum[kChiThreads / 32];
     double tot_val, tot_err;
     long long numeval;
@@ -544,30 +546,44 @@ __device__ void block_merge(const unsigned long long* ak, const int* ai, int na,
     __syncthreads();
 }
 
-// point k of the 17 Genz-Malik points of region (c, h), the library's order
-__device__ __forceinline__ void gm_point(int k, double c0, double c1, double h0, double h1, double& x, double& y) {
-    x = c0;
-    y = c1;
+// coordinate j of the seven a region's Genz-Malik points take along one axis (centre c, half width
+// h): c, c - λ2 h, c + λ2 h, c - λ4 h, c + λ4 h, c - λ5 h, c + λ5 h (rounded products and sums, so
+// that every use of a coordinate gets the same value)
+__device__ __forceinline__ double gm_coord(int j, double c, double h) {
+    if (j == 0) return c;
+    const double off = __dmul_rn(h, j <= 2 ? kGL2 : (j <= 4 ? kGL4 : kGL5));
+    return __dadd_rn(c, (j & 1) ? -off : off);
+}
+
+// the coordinates (indices of gm_coord) of point k of the 17, the library's order: the centre, the
+// four points on each axis (-λ2, +λ2, -λ4, +λ4), the corners at λ4 ((-,-), (+,-), (+,+), (-,+)) and
+// at λ5 ((+,+), (-,+), (-,-), (+,-))
+__device__ __forceinline__ void gm_index(int k, int& xi, int& yi) {
+    xi = yi = 0;
     if (k == 0) return;
     if (k <= 8) {
-        const int d = (k - 1) >> 2, q = (k - 1) & 3;
-        const double hw = d == 0 ? h0 : h1;
-        const double off = (q < 2 ? hw * kGL2 : hw * kGL4) * ((q & 1) ? 1.0 : -1.0);
-        if (d == 0) x = c0 + off;
-        else y = c1 + off;
+        const int d = (k - 1) >> 2, j = ((k - 1) & 3) + 1;
+        if (d == 0) xi = j;
+        else yi = j;
         return;
     }
     if (k <= 12) {
-        const double a = h0 * kGL4, b = h1 * kGL4;
-        const int q = k - 9;  // (-,-), (+,-), (+,+), (-,+)
-        x = c0 + ((q == 1 || q == 2) ? a : -a);
-        y = c1 + ((q >= 2) ? b : -b);
+        const int q = k - 9;
+        xi = (q == 1 || q == 2) ? 4 : 3;
+        yi = q >= 2 ? 4 : 3;
         return;
     }
-    const double a = h0 * kGL5, b = h1 * kGL5;
-    const int q = k - 13;  // (+,+), (-,+), (-,-), (+,-)
-    x = c0 + ((q == 0 || q == 3) ? a : -a);
-    y = c1 + ((q <= 1) ? b : -b);
+    const int q = k - 13;
+    xi = (q == 0 || q == 3) ? 6 : 5;
+    yi = q <= 1 ? 6 : 5;
+}
+
+// point k of the 17 Genz-Malik points of region (c, h), the library's order
+__device__ __forceinline__ void gm_point(int k, double c0, double c1, double h0, double h1, double& x, double& y) {
+    int xi, yi;
+    gm_index(k, xi, yi);
+    x = gm_coord(xi, c0, h0);
+    y = gm_coord(yi, c1, h1);
 }
 
 // rule75genzmalik_evalError for dim = 2 on the 17 values v
@@ -607,18 +623,28 @@ __device__ __forceinline__ void gm_rule(const double* v, double vol, double& val
 // the mixed path); the compactified coordinates and their Jacobians are formed in FP64.
 template <typename R>
 struct ChiKernel {
+    static constexpr bool kSplit = true;  // core(x, y) * gfac(x) * gfac(y), see chi_eval_block
     const ChiArgs& A;
     const SMesh<R>& M;
     const R* a;  // the state in R
     int site;
     int k;
     double w;
-    __device__ double operator()(double x, double y) const {
+    // G(v - ω/2) G(v + ω/2) dv/dx at the compactified coordinate x (and the same at y): the factors
+    // that depend on one coordinate only
+    __device__ R gfac(double x) const {
+        const R v = (R)((2.0 * x - 1.0) / ((1.0 - x) * x));
+        const R dv = (R)((2.0 * x * x - 2.0 * x + 1) / ((1.0 - x) * (1.0 - x) * x * x));
+        const R wr = (R)w, h = (R)0.5;
+        const R Lam = (R)A.Lam;
+        return G_full(M, A.L.Nsig, a, Lam, v - h * wr) * G_full(M, A.L.Nsig, a, Lam, v + h * wr) * dv;
+    }
+    __device__ double operator()(double x, double y) const { return (double)(core(x, y) * gfac(x) * gfac(y)); }
+    // the vertex part of the integrand; the integrand is (core * gfac(x)) * gfac(y)
+    __device__ R core(double x, double y) const {
         const Layout& L = A.L;
         const R v = (R)((2.0 * x - 1.0) / ((1.0 - x) * x));
         const R vp = (R)((2.0 * y - 1.0) / ((1.0 - y) * y));
-        const R dv = (R)((2.0 * x * x - 2.0 * x + 1) / ((1.0 - x) * (1.0 - x) * x * x));
-        const R dvp = (R)((2.0 * y * y - 2.0 * y + 1) / ((1.0 - y) * (1.0 - y) * y * y));
         const R wr = (R)w, h = (R)0.5;
         Plan<R> p1[3];
         make_plan<R>(p1[0], 0, v + vp, h * (v - wr - vp), h * (-v - wr + vp), M, L.Ns, L.NO, L.Nn);
@@ -651,10 +677,7 @@ struct ChiKernel {
                 val -= (vzd - vdz) / ((R)2 * tp2);
             }
         }
-        const R Lam = (R)A.Lam;
-        val *= G_full(M, L.Nsig, a, Lam, v - h * wr) * G_full(M, L.Nsig, a, Lam, v + h * wr) * dv;
-        val *= G_full(M, L.Nsig, a, Lam, vp - h * wr) * G_full(M, L.Nsig, a, Lam, vp + h * wr) * dvp;
-        return (double)val;
+        return val;
     }
 };
 
@@ -663,6 +686,7 @@ struct ChiKernel {
 // in float-float arithmetic as in the quadrature passes, and plans near a buffer switch built in
 // FP64 from the same FP64 arguments as the FP64 integrand.
 struct ChiKernelFF {
+    static constexpr bool kSplit = false;
     const ChiArgs& A;
     const MeshFF& M;
     const float* a;  // the FP32 copy of the state
@@ -742,11 +766,30 @@ __device__ void chi_eval_block(const F& f, const ChiRegions& R, const Reg& reg, 
     const int tid = threadIdx.x;
     for (int cb = first * kChiChunk; cb < count; cb += stride * kChiChunk) {
         const int cnt = min(kChiChunk, count - cb);
-        for (int p = tid; p < cnt * 17; p += kChiThreads) {
-            const int r = reg(cb + p / 17);
-            double x, y;
-            gm_point(p % 17, __ldcg(R.c0 + r), __ldcg(R.c1 + r), __ldcg(R.h0 + r), __ldcg(R.h1 + r), x, y);
-            S.f[p] = f(x, y);
+        if constexpr (F::kSplit) {
+            // the propagator factors depend on one coordinate: seven per axis and region instead of
+            // four per point (the integrand is (core(x, y) gfac(x)) gfac(y) either way)
+            for (int p = tid; p < cnt * 14; p += kChiThreads) {
+                const int r = reg(cb + p / 14), j = p % 14;
+                S.gfac[p] = j < 7 ? f.gfac(gm_coord(j, __ldcg(R.c0 + r), __ldcg(R.h0 + r)))
+                                  : f.gfac(gm_coord(j - 7, __ldcg(R.c1 + r), __ldcg(R.h1 + r)));
+            }
+            __syncthreads();
+            for (int p = tid; p < cnt * 17; p += kChiThreads) {
+                const int q = p / 17, r = reg(cb + q);
+                int xi, yi;
+                gm_index(p % 17, xi, yi);
+                const double x = gm_coord(xi, __ldcg(R.c0 + r), __ldcg(R.h0 + r));
+                const double y = gm_coord(yi, __ldcg(R.c1 + r), __ldcg(R.h1 + r));
+                S.f[p] = (double)(f.core(x, y) * S.gfac[14 * q + xi] * S.gfac[14 * q + 7 + yi]);
+            }
+        } else {
+            for (int p = tid; p < cnt * 17; p += kChiThreads) {
+                const int r = reg(cb + p / 17);
+                double x, y;
+                gm_point(p % 17, __ldcg(R.c0 + r), __ldcg(R.c1 + r), __ldcg(R.h0 + r), __ldcg(R.h1 + r), x, y);
+                S.f[p] = f(x, y);
+            }
         }
         __syncthreads();
         for (int q = tid; q < cnt; q += kChiThreads) {
