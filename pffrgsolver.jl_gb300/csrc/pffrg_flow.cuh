@@ -438,11 +438,12 @@ struct Team {
 
     // One non-local vertex slot of an SU(2) node on this lane's sites (get_Γ_avx!,
     // action_su2.jl:115-134): bare + Σ_ch sgn Σ_q w_q q[off_q + site], channels in the reference's
-    // order.  A channel's corners are walked by a loop that is not unrolled (smaller code and fewer
-    // live registers: 113 instead of 127 for the FP32 32x2 kernel, 155 instead of 229 for the FP64
-    // one; 4-8 % faster), the reads of one corner for both components and all of the lane's sites in
-    // flight together; the loop over the sites has no branch (padding sites read site 0 and are
-    // zeroed at the end).
+    // order.  A channel's corners are walked by a loop (smaller code and fewer live registers than
+    // all eight unrolled: 113 instead of 127 for the FP32 32x2 kernel, 155 instead of 229 for the
+    // FP64 one; 4-8 % faster), the FP32 loop two corners at a time (the reads of two corners for both
+    // components and all of the lane's sites in flight together: a further 3-4 %; four at a time
+    // was slower); the loop over the sites has no branch (padding sites read site 0 and are zeroed
+    // at the end).
     __device__ __forceinline__ void gather_su2(const NodeScratch<R, C>& ns, int slot, R v[2][SPL]) {
         const int Ns = A.L.Ns;
         const R* __restrict__ src = A.src[slot];
@@ -477,7 +478,7 @@ struct Team {
                     st[k] = ex ? site_ex[k] : si[k];
                     a0[k] = a1[k] = (R)0;
                 }
-#pragma unroll 1
+#pragma unroll 2
                 for (int c = 0; c < nc; ++c) {
                     const R w = P.w[c];
                     const int off = P.off[c];
