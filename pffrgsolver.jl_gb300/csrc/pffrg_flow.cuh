@@ -616,6 +616,7 @@ struct Team {
 #pragma unroll
             for (int v = 0; v < V; ++v) x[v] = (R)0;
             const int j1 = row_off[i + 1];
+#pragma unroll 2
             for (int r = row_off[i] + tl; r < j1; r += T) {
                 const unsigned row = rows[r];
                 const int ia = row & 0xff, ib = (row >> 8) & 0xff;
